@@ -1,0 +1,311 @@
+"""Benchmark: ray-segments/s of the stochastic energy tracer on one GB300.
+
+Workload (the 50k-triangle multi-room scene): 40 box rooms on an 8 x 5 grid
+with shared walls, 1 x 2.1 m door holes and glass panes, 49k primitives after
+tessellation; 64 source/listener pairs x 4096 rays x 3 bands, 2000 x 1 ms
+bins (2 s), <= 200 bounces, energy floor 1e-6; plus the 512-ray golden-spiral
+dome fan for each of the 64 listeners. A step traces all 64 pairs and all 64
+domes. Inputs (scene, jobs) are resident in HBM; the BVH (~3 MB) fits in L2,
+so L2 is flushed (a 256 MB write) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Rank 0 prints one JSON line. `--impl reference` times the CPU restatement of
+the reference tracer (the oracle port; the reference itself is Rust and has
+no toolchain here) on the host cores, on the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ray-segments/s on 1 GB300 (% HBM roofline); surrogate vs tracer ms/room at <=5% RT60 err"
+UNIT = "ray-segments/s"
+N_PAIRS = 64
+N_RAYS = 4096
+DOME_RAYS = 512
+CFG = dict(n_bands=3, n_bins=2000, bin_dt=0.001, max_time=2.0, max_bounces=200, energy_floor=1e-6)
+WORKLOAD = "multiroom-40rooms-49k-prims: 64 pairs x 4096 rays x 3 bands, 2000 x 1 ms bins, 200 bounces, " \
+           "floor 1e-6, + 64 x 512-ray dome fans"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[5:9]) if v.strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def build_case():
+    from omg_audio_gb300 import workloads as W
+    return W.multiroom(seed=2, n_pairs=N_PAIRS)
+
+
+def oracle_mesh(case, real="f32"):
+    from oracle import oracle as O
+    mb = O.MeshBuilder()
+    case.recorder.replay(mb, lambda m: O.Material.make(m.absorption, m.scattering, m.transmission))
+    return mb.build(real)
+
+
+def cpu_sample(case, n_pairs, threads, n_rays=N_RAYS, ray_end=None):
+    """The f32 oracle (the reference's algorithm and arithmetic) on pairs
+    [0, n_pairs): segments, seconds and the traversal counters."""
+    from oracle import oracle as O
+    mesh = oracle_mesh(case)
+    P = O.params(**CFG)
+    pan = [(mn, mx, O.Material.make(m.absorption, m.scattering, m.transmission)) for (mn, mx, m) in case.panels]
+    seg = nodes = prims = hits = 0
+    t0 = time.perf_counter()
+    for p in range(n_pairs):
+        src, lis = case.pairs[p]
+        _, _, st = O.trace_mesh(mesh, src, lis, n_rays, P=P, seed=1000 + p, panels=pan, threads=threads,
+                                ray_end=ray_end)
+        seg += st["segments"]
+        nodes += st["node_reads"]
+        prims += st["prim_tests"]
+        hits += st["receiver_hits"]
+    dt = time.perf_counter() - t0
+    return dict(segments=seg, seconds=dt, node_reads=nodes, prim_tests=prims, receiver_hits=hits)
+
+
+def bytes_per_segment(st, nb=3):
+    """B_seg = 32 N_node + 48 N_prim + 4 (NB + 3) h: bytes the reference's ordered
+    traversal reads per segment (32 B nodes, 48 B primitives) plus histogram writes."""
+    s = max(st["segments"], 1)
+    n_node, n_prim, h = st["node_reads"] / s, st["prim_tests"] / s, st["receiver_hits"] / s
+    return 32.0 * n_node + 48.0 * n_prim + 4.0 * (nb + 3) * h, dict(n_node=n_node, n_prim=n_prim, h=h)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    case = build_case()
+    threads = os.cpu_count() or 1
+    pairs = max(1, min(N_PAIRS, args.ref_pairs))
+    for _ in range(max(0, args.warmup)):
+        cpu_sample(case, 1, threads, ray_end=256)
+    times, segs = [], []
+    for _ in range(args.steps):
+        st = cpu_sample(case, pairs, threads)
+        times.append(st["seconds"])
+        segs.append(st["segments"])
+    v = float(np.sum(segs) / np.sum(times))
+    sample = f"{pairs} of {N_PAIRS} pairs x {N_RAYS} rays per step (the full fans skipped)"
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": WORKLOAD, "sample": sample, "l2": "n/a (CPU)"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from omg_audio_gb300 import build as B
+    B.build()
+    from omg_audio_gb300 import Context, DomeProbe, Job, MeshBuilder, TraceConfig
+    from omg_audio_gb300 import _lib
+
+    case = build_case()
+    ctx = Context(TraceConfig(device=local, timeout_ms=60000, **CFG))
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    mb = MeshBuilder()
+    case.recorder.replay(mb)
+    bvh = _lib.BVH_LBVH if args.bvh == "lbvh" else _lib.BVH_SAH
+    scene = ctx.upload_builder(mb, 3, bvh)
+    jobs = [Job(src, lis, N_RAYS, seed=1000 + p, scene=scene, panel_offset=0, n_panels=len(case.panels))
+            for p, (src, lis) in enumerate(case.pairs)]
+    batch = ctx.batch(jobs, case.panels)
+    tune = batch.autotune(reps=1) if args.autotune else None
+    dome = DomeProbe(ctx, scene, case.glass, n_fan=DOME_RAYS)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        batch.launch(1)
+        if ev:
+            ev[1].record(stream)
+        batch.launch(2)
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+        dome.sample(case.listeners, n_rays=DOME_RAYS)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    dome_ms = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.zero_()
+            step(evs[k])
+        torch.cuda.synchronize()
+        # the dome fan of every listener, same steps (its own host round trip)
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            dres = dome.sample(case.listeners, n_rays=DOME_RAYS)
+            dome_ms.append(1e3 * (time.perf_counter() - t0))
+        torch.cuda.synchronize()
+    trace_ms = np.array([e[0].elapsed_time(e[1]) for e in evs])
+    step_ms = np.array([e[0].elapsed_time(e[2]) for e in evs])
+    segments = batch.segments()
+    dome_seg = dres["segments"]["escape_events"] + dres["segments"]["through_calls"]
+    t_step = float(np.mean(step_ms)) + float(np.mean(dome_ms))
+    if ws > 1:
+        t = torch.tensor([t_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = ws * (segments + dome_seg) / (t_step * 1e-3)
+
+    # end to end: the host-buffer C-ABI call (H2D jobs, launch, D2H echograms) + the dome call
+    e2e_ms = []
+    for k in range(max(1, args.steps)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.trace_batch(jobs, case.panels)
+        dome.sample(case.listeners, n_rays=DOME_RAYS)
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    h2d, d2h = ctx.io_bytes()
+    d2h += 64 * 9 * (3 + 3) * 4 + 64 * DOME_RAYS * (1 + 12)
+    h2d += 64 * 12
+    e2e = ws * (segments + dome_seg) / (float(np.mean(e2e_ms)) * 1e-3)
+
+    line = None
+    if rank == 0:
+        # CPU baseline + bytes per segment from the oracle's reference traversal
+        threads = os.cpu_count() or 1
+        cpu = cpu_sample(case, args.ref_pairs, threads)
+        bseg, parts = bytes_per_segment(cpu)
+        peak, peak_kind = peaks()
+        t_trace = float(np.mean(trace_ms)) * 1e-3
+        achieved = segments * bseg / t_trace / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": WORKLOAD, "prims": scene.info()["prims"], "bvh": args.bvh,
+                       "l2": "flushed (256 MB write) before every timed step", "segments_per_step": segments,
+                       "dome_segments_per_step": dome_seg, "trace_ms": float(np.mean(trace_ms)),
+                       "finalize_reverb_ms": float(np.mean(step_ms - trace_ms)),
+                       "dome_ms": float(np.mean(dome_ms)), "autotune": tune,
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "ms_per_step": float(np.mean(e2e_ms))},
+            "gpu_launches": int(args.steps * (batch.kernel_count() + 2)),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "bytes_per_segment": bseg, **{k: round(v, 4) for k, v in parts.items()},
+                         "kernel": "trace_kernel<3> (clear + trace part, CUDA events)"},
+            "cpu_baseline": {"value": cpu["segments"] / cpu["seconds"], "unit": UNIT, "cores": threads,
+                             "kind": "port",
+                             "sample": f"{args.ref_pairs} of {N_PAIRS} pairs x {N_RAYS} rays (f32 oracle, "
+                                       f"{threads} threads)"},
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--bvh", choices=["sah", "lbvh"], default="sah")
+    ap.add_argument("--ref-pairs", type=int, default=4)
+    ap.add_argument("--autotune", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,303 @@
+/*
+ * omg_cuda.h — C ABI of the GB300 stochastic energy path tracer.
+ *
+ * Drop-in for omg-audio's late-field backend seam (crates/omg-scene/src/late.rs)
+ * and its ambient dome (crates/omg-scene/src/dome.rs). Plain C types only: a
+ * Rust `extern "C"` block, ctypes, or any FFI binds it directly.
+ *
+ * Conventions (every entry point):
+ *  - returns int32_t status: OMG_OK (0), OMG_PENDING (>0), or a negative error;
+ *  - never panics, never blocks without a bound (waits take a timeout);
+ *  - never retains caller pointers past the call;
+ *  - a context is used by one thread at a time (the reference serialises its
+ *    backends behind one global Mutex, late.rs:51,93; do the same).
+ * All buffers passed in are HOST memory unless the name says `_dev`.
+ */
+#ifndef OMG_CUDA_H
+#define OMG_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OMG_ABI_VERSION 1
+#define OMG_MAX_BANDS 8
+#define OMG_DOME_BINS 9          /* dome.rs:30: 8 azimuth sectors + zenith */
+
+/* status codes */
+#define OMG_OK 0
+#define OMG_PENDING 1            /* async result not ready (poll again) */
+#define OMG_E_INVALID (-1)       /* bad argument */
+#define OMG_E_OOM (-2)           /* device or host allocation failed */
+#define OMG_E_DEVICE (-3)        /* CUDA error; the context is unusable */
+#define OMG_E_TIMEOUT (-4)       /* a bounded wait ran out */
+#define OMG_E_OVERFLOW (-5)      /* traversal stack / crossing list overflow (kernel flag) */
+#define OMG_E_NOT_FOUND (-6)     /* unknown scene / probe / ticket id */
+#define OMG_E_NO_DEVICE (-7)     /* no usable CUDA device */
+
+/* BVH builders for omg_scene_upload */
+#define OMG_BVH_SAH 0            /* the reference's binned-SAH tree (mesh.rs:241-405), built on the host */
+#define OMG_BVH_LBVH 1           /* Morton/Karras LBVH built on the GPU */
+
+typedef struct omg_ctx omg_ctx;
+
+/* Per-band surface acoustics: crates/omg-core/src/material.rs:7-16 (NBANDS
+ * there is 3; here the band count is a runtime value <= 8). Amplitude
+ * transmission T: the energy fraction is T*T. */
+typedef struct omg_material {
+    float absorption[OMG_MAX_BANDS];
+    float scattering;
+    float transmission[OMG_MAX_BANDS];
+} omg_material;
+
+/* Tracer constants made runtime values. Defaults (omg_params_default) are the
+ * reference constants: tracer.rs:12-16 (BIN_DT 0.010, MAX_TIME 3.0,
+ * NBINS 300, RECEIVER_RADIUS 0.5, WALL_EPS 1e-3), 64 bounces (tracer.rs:103),
+ * energy floor 1e-7 x per-ray energy (tracer.rs:163,179), c = 343 (lib.rs:18),
+ * 3 bands (lib.rs:22), direction band 1 (tracer.rs:123-125). */
+typedef struct omg_params {
+    uint32_t n_bands;
+    uint32_t n_bins;
+    float bin_dt;
+    float max_time;
+    uint32_t max_bounces;
+    float energy_floor;
+    float receiver_radius;
+    float wall_eps;
+    float speed_of_sound;
+    uint32_t dir_band;
+    int32_t device;              /* CUDA device ordinal */
+    uint32_t timeout_ms;         /* bound on every wait (0 = 10000) */
+} omg_params;
+
+/* LateBackend::trace job (late.rs:28-40): analytic shoebox [0,size]^3, walls in
+ * Shoebox order x-,x+,y-,y+,z-,z+ (scene.rs:23-26). */
+typedef struct omg_box_job {
+    float size[3];
+    omg_material walls[6];
+    float src[3];
+    float lis[3];
+    uint32_t n_rays;
+    float energy[OMG_MAX_BANDS];
+    uint32_t seed;               /* per-ray stream seed (see omg_trace_box) */
+} omg_box_job;
+
+/* Panel overlay box (scene.rs:90-137; late.rs:88 `panels: &[(Vec3, Vec3, Material)]`). */
+typedef struct omg_panel {
+    float mn[3];
+    float mx[3];
+    omg_material material;
+} omg_panel;
+
+/* WorldLateBackend::trace_world job (late.rs:81-91) over an uploaded mesh. */
+typedef struct omg_world_job {
+    float src[3];
+    float lis[3];
+    uint32_t n_rays;
+    float energy[OMG_MAX_BANDS];
+    uint32_t seed;
+} omg_world_job;
+
+/* One job of a batch: either geometry kind, its own rays, bands and histogram
+ * length (the per-job values override omg_params). */
+#define OMG_GEOM_BOX 0
+#define OMG_GEOM_MESH 1
+typedef struct omg_job {
+    uint32_t geom;               /* OMG_GEOM_BOX or OMG_GEOM_MESH */
+    uint32_t scene_id;           /* OMG_GEOM_MESH: an uploaded scene */
+    float box_size[3];           /* OMG_GEOM_BOX */
+    omg_material box_walls[6];   /* OMG_GEOM_BOX */
+    float src[3];
+    float lis[3];
+    uint32_t n_rays;
+    float energy[OMG_MAX_BANDS];
+    uint32_t seed;
+    uint32_t n_bands;            /* 0 = context default */
+    uint32_t n_bins;             /* 0 = context default */
+    float max_time;              /* 0 = context default */
+    uint32_t panel_offset;       /* into the batch's panel array */
+    uint32_t n_panels;
+} omg_job;
+
+/* estimate_reverb output (tracer.rs:204-257, params.rs:17-37) plus the
+ * least-squares T20 fit of the FP64 Schroeder curve and the segment count. */
+typedef struct omg_reverb {
+    float rt60[OMG_MAX_BANDS];
+    float level[OMG_MAX_BANDS];
+    float rt60_fit[OMG_MAX_BANDS];
+    uint64_t segments;           /* ray segments traced for this job */
+} omg_reverb;
+
+/* Ambient-dome panel (dome.rs:41-69) with its per-band AMPLITUDE transmission:
+ * a pane (glass=1) passes rays with T^2 (glass_transmission, walkthrough.rs:310-320);
+ * a door leaf (glass=0) blocks escapes and seeps T^2 straight through
+ * (DOOR/HEAVY_PANEL_TRANSMISSION, walkthrough.rs:322-326). */
+typedef struct omg_dome_panel {
+    int32_t axis;                /* 0: plane of constant x, 1: constant y */
+    float plane;
+    float lat0, lat1;
+    float z0, z1;
+    int32_t glass;
+    float trans[OMG_MAX_BANDS];
+} omg_dome_panel;
+
+typedef struct omg_dome_bin {    /* dome.rs:71-77 */
+    float dir[3];
+    float energy[OMG_MAX_BANDS];
+} omg_dome_bin;
+
+/* ------------------------------------------------------------------ context */
+
+/* Fill the reference defaults. */
+void omg_params_default(omg_params* p);
+
+/* Create a context on p->device. NULL = no usable device: the caller keeps the
+ * CPU path (GpuTracer::new -> Option, crates/omg-gpu/src/lib.rs:33-37). */
+omg_ctx* omg_create(const omg_params* p);
+void omg_destroy(omg_ctx* ctx);
+int32_t omg_abi_version(void);
+const char* omg_status_string(int32_t status);
+/* Last CUDA error text of the context (empty when none). */
+const char* omg_last_error(const omg_ctx* ctx);
+/* Launch work of this context on a caller stream (a cudaStream_t; NULL = the
+ * context's own stream). */
+int32_t omg_set_stream(omg_ctx* ctx, void* cuda_stream);
+
+/* ------------------------------------------------------------- mesh builder */
+/* Incremental mesh assembly with 0.1 mm vertex dedup: MeshBuilder,
+ * crates/omg-core/src/mesh.rs:70-165. */
+typedef struct omg_mesh_builder omg_mesh_builder;
+omg_mesh_builder* omg_mb_create(void);
+void omg_mb_destroy(omg_mesh_builder* mb);
+uint32_t omg_mb_material(omg_mesh_builder* mb, const omg_material* m);     /* mesh.rs:93-96 */
+uint32_t omg_mb_begin_surface(omg_mesh_builder* mb);                       /* mesh.rs:103-106 */
+void omg_mb_coarse(omg_mesh_builder* mb, float max_edge);                  /* mesh.rs:132-134 */
+void omg_mb_tri(omg_mesh_builder* mb, const float a[3], const float b[3], const float c[3], uint32_t material); /* :116-126 */
+void omg_mb_quad(omg_mesh_builder* mb, const float a[3], const float b[3], const float c[3], const float d[3],
+                 uint32_t material);                                       /* mesh.rs:137-140 */
+void omg_mb_abox(omg_mesh_builder* mb, const float mn[3], const float mx[3], uint32_t material); /* :144-153 */
+/* Bulk form: quad i has corners q[12i..12i+11]; begin_surface is called
+ * new_surface[i] times first; coarse(max_edge[i]) applies before it (NULL arrays skip). */
+void omg_mb_quads(omg_mesh_builder* mb, const float* q, const uint16_t* material, const uint8_t* new_surface,
+                  const float* max_edge, uint32_t n);
+void omg_mb_counts(const omg_mesh_builder* mb, uint32_t* n_verts, uint32_t* n_tris, uint32_t* n_materials);
+void omg_mb_export(const omg_mesh_builder* mb, float* positions, uint32_t* indices, uint16_t* tri_material,
+                   uint16_t* tri_surface, float* tri_max_edge);
+
+/* ------------------------------------------------------------------- scenes */
+/* Upload a mesh and build its BVH (MeshBuilder::build + GpuMeshTracer::new,
+ * mesh.rs:155-221, omg-gpu/src/lib.rs:274-287). Oversized triangles are
+ * tessellated exactly as mesh.rs:241-287; hits report the ORIGINAL triangle id.
+ * n_bands fixes the band count of this scene's materials. */
+int32_t omg_scene_upload(omg_ctx* ctx, const float* positions, uint32_t n_verts, const uint32_t* indices,
+                         uint32_t n_tris, const uint16_t* tri_material, const float* tri_max_edge,
+                         const omg_material* materials, uint32_t n_materials, uint32_t n_bands,
+                         uint32_t bvh_kind, uint32_t* scene_id);
+/* Same, straight from a builder. */
+int32_t omg_scene_from_builder(omg_ctx* ctx, const omg_mesh_builder* mb, uint32_t n_bands, uint32_t bvh_kind,
+                               uint32_t* scene_id);
+int32_t omg_scene_release(omg_ctx* ctx, uint32_t scene_id);
+/* Node / primitive counts of an uploaded scene. */
+int32_t omg_scene_info(omg_ctx* ctx, uint32_t scene_id, uint32_t* n_nodes, uint32_t* n_prims, uint32_t* n_tris);
+/* The uploaded BVH in the reference's flattened form (mesh.rs:463-481,
+ * omg-gpu/src/layout.rs:96-122): nodes {bmin[3], a, bmax[3], b} as boxes[n*6]
+ * + ab[n*2], prims {a, e1, e2} as geo[p*9] + tri[p] + material[p]. */
+int32_t omg_scene_export_bvh(omg_ctx* ctx, uint32_t scene_id, float* node_boxes, uint32_t* node_ab,
+                             float* prim_geo, uint32_t* prim_tri, uint16_t* prim_mat);
+
+/* ---------------------------------------------------------------- tracing */
+/* The stream: ray r of a job draws from PCG-RXS-M-XS seeded
+ * (seed ^ r*0x9E3779B9) + 1 with two warm-up draws
+ * (crates/omg-gpu/shaders/trace_mesh.wgsl:90-105, 211-213).
+ * Outputs: bins[n_bins*n_bands] (bin-major), dirs[n_bins*3], FP32 values of
+ * compensated (two-float) sums. The caller's buffers are overwritten, as the
+ * reference clears the Echogram first (tracer.rs:89). */
+
+/* LateBackend::trace (late.rs:28-40, omg-gpu/src/lib.rs:1051-1068). */
+int32_t omg_trace_box(omg_ctx* ctx, const omg_box_job* job, float* bins, float* dirs, omg_reverb* reverb);
+
+/* WorldLateBackend::trace_world (late.rs:81-91, omg-gpu/src/lib.rs:845-874)
+ * over WithPanels{mesh, panels} (scene.rs:90-137). */
+int32_t omg_trace_world(omg_ctx* ctx, uint32_t scene_id, const omg_world_job* job, const omg_panel* panels,
+                        uint32_t n_panels, float* bins, float* dirs, omg_reverb* reverb);
+
+/* Many jobs (uneven rays, bands, histogram lengths, scenes) in one persistent
+ * launch captured in a CUDA graph. bins/dirs are the jobs' outputs back to
+ * back, in job order; reverb (nullable) gets one entry per job. */
+int32_t omg_trace_batch(omg_ctx* ctx, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                        uint32_t n_panels, float* bins, float* dirs, omg_reverb* reverb);
+
+/* Device-resident batches: upload once, launch many times, read back. */
+int32_t omg_batch_create(omg_ctx* ctx, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                         uint32_t n_panels, uint32_t* batch_id);
+/* Launch on the context stream without host copies or waits (stream order). */
+int32_t omg_batch_launch(omg_ctx* ctx, uint32_t batch_id);
+/* The same launch in two parts (part 1: clear scratch + trace kernel; part 2:
+ * finalize + reverb kernels; part 0: both), for timing the trace kernel alone. */
+int32_t omg_batch_launch_part(omg_ctx* ctx, uint32_t batch_id, uint32_t part);
+/* Host->device and device->host bytes copied by the last one-shot trace call
+ * (omg_trace_box / omg_trace_world / omg_trace_batch). */
+int32_t omg_io_bytes(omg_ctx* ctx, uint64_t* h2d, uint64_t* d2h);
+/* Wait (bounded) and copy results to host; any pointer may be NULL. */
+int32_t omg_batch_read(omg_ctx* ctx, uint32_t batch_id, float* bins, float* dirs, omg_reverb* reverb);
+/* Float counts of one batch's bins and dirs outputs. */
+int32_t omg_batch_sizes(omg_ctx* ctx, uint32_t batch_id, uint64_t* n_bin_floats, uint64_t* n_dir_floats);
+/* Total segments traced by the last launch of the batch (device counter). */
+int32_t omg_batch_segments(omg_ctx* ctx, uint32_t batch_id, uint64_t* segments);
+int32_t omg_batch_destroy(omg_ctx* ctx, uint32_t batch_id);
+/* Number of kernel launches one omg_batch_launch issues. */
+int32_t omg_batch_kernel_count(omg_ctx* ctx, uint32_t batch_id, uint32_t* n_kernels);
+
+/* Asynchronous form of the seam (LateBackend::poll_into, late.rs:42-48):
+ * submit returns a ticket at once; poll returns OMG_PENDING until done. */
+int32_t omg_submit_world(omg_ctx* ctx, uint32_t scene_id, const omg_world_job* job, const omg_panel* panels,
+                         uint32_t n_panels, uint32_t* ticket);
+int32_t omg_poll(omg_ctx* ctx, uint32_t ticket, float* bins, float* dirs, omg_reverb* reverb);
+
+/* Autotuner: time launch shapes (threads per block x blocks per SM x rays
+ * fetched per warp) on the batch and keep the fastest for it. */
+typedef struct omg_tune_result {
+    uint32_t block_threads;
+    uint32_t blocks_per_sm;
+    uint32_t refill_min;
+    float ms;
+} omg_tune_result;
+int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t batch_id, uint32_t reps, omg_tune_result* best);
+
+/* ----------------------------------------------------------- mesh queries */
+/* Closest hit per ray (Mesh::raycast, mesh.rs:484-541): t (-1 on miss) and the
+ * ORIGINAL triangle id (0xFFFFFFFF on miss). */
+int32_t omg_raycast(omg_ctx* ctx, uint32_t scene_id, const float* origins, const float* dirs, uint32_t n,
+                    float* t, uint32_t* tri);
+
+/* ------------------------------------------------------------------- reverb */
+/* estimate_reverb (tracer.rs:204-257) of n_jobs echograms back to back on the
+ * GPU: FP64 Schroeder integral, 2-point -5/-25 dB slope, least-squares fit. */
+int32_t omg_estimate_reverb(omg_ctx* ctx, const float* bins, uint32_t n_bins, uint32_t n_bands, float bin_dt,
+                            uint32_t n_jobs, omg_reverb* out);
+
+/* --------------------------------------------------------------------- dome */
+/* DomeProbe::new over an uploaded world mesh (dome.rs:312-326): n_fan
+ * golden-spiral directions (384 in the reference), fixed glass panes. */
+int32_t omg_dome_create(omg_ctx* ctx, uint32_t scene_id, const omg_dome_panel* glass, uint32_t n_glass,
+                        uint32_t n_fan, uint32_t n_bands, uint32_t* probe_id);
+int32_t omg_dome_destroy(omg_ctx* ctx, uint32_t probe_id);
+/* DomeProbe::sample (dome.rs:424-478) for n_eyes listener positions at once.
+ * out: n_eyes x 9 bins (EMA'd, 0.35; the first call primes with 1.0);
+ * raw_energy (nullable): n_eyes x 9 x n_bands energies before the EMA;
+ * escape (nullable): n_eyes x n_rays per-ray sky-escape flags (1 = escaped);
+ * ray_tp (nullable): n_eyes x n_rays x n_bands per-ray throughput.
+ * Every listener keeps its own EMA state inside the probe (slot = eye index). */
+int32_t omg_dome_sample(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint32_t n_eyes,
+                        const omg_dome_panel* leaves, uint32_t n_leaves, uint32_t n_rays, uint32_t max_events,
+                        omg_dome_bin* out, float* raw_energy, uint8_t* escape, float* ray_tp);
+/* Work of the probe's last sample: trace_escape events (dome.rs:333-380) and
+ * trace_through calls (dome.rs:390-422), summed over listeners. */
+int32_t omg_dome_segments(omg_ctx* ctx, uint32_t probe_id, uint64_t* escape_events, uint64_t* through_calls);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OMG_CUDA_H */

@@ -1,0 +1,157 @@
+"""ctypes bindings of libomg_cuda.so (include/omg_cuda.h).
+
+The library is built in-tree by omg_audio_gb300.build. Loading fails loudly
+when it is missing: there is no CPU path behind these bindings.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libomg_cuda.so")
+
+MAX_BANDS = 8
+DOME_BINS = 9
+
+OK, PENDING = 0, 1
+E_INVALID, E_OOM, E_DEVICE, E_TIMEOUT, E_OVERFLOW, E_NOT_FOUND, E_NO_DEVICE = -1, -2, -3, -4, -5, -6, -7
+BVH_SAH, BVH_LBVH = 0, 1
+GEOM_BOX, GEOM_MESH = 0, 1
+
+F8 = C.c_float * MAX_BANDS
+F3 = C.c_float * 3
+
+
+class omg_material(C.Structure):
+    _fields_ = [("absorption", F8), ("scattering", C.c_float), ("transmission", F8)]
+
+
+class omg_params(C.Structure):
+    _fields_ = [("n_bands", C.c_uint32), ("n_bins", C.c_uint32), ("bin_dt", C.c_float), ("max_time", C.c_float),
+                ("max_bounces", C.c_uint32), ("energy_floor", C.c_float), ("receiver_radius", C.c_float),
+                ("wall_eps", C.c_float), ("speed_of_sound", C.c_float), ("dir_band", C.c_uint32),
+                ("device", C.c_int32), ("timeout_ms", C.c_uint32)]
+
+
+class omg_box_job(C.Structure):
+    _fields_ = [("size", F3), ("walls", omg_material * 6), ("src", F3), ("lis", F3), ("n_rays", C.c_uint32),
+                ("energy", F8), ("seed", C.c_uint32)]
+
+
+class omg_panel(C.Structure):
+    _fields_ = [("mn", F3), ("mx", F3), ("material", omg_material)]
+
+
+class omg_world_job(C.Structure):
+    _fields_ = [("src", F3), ("lis", F3), ("n_rays", C.c_uint32), ("energy", F8), ("seed", C.c_uint32)]
+
+
+class omg_job(C.Structure):
+    _fields_ = [("geom", C.c_uint32), ("scene_id", C.c_uint32), ("box_size", F3), ("box_walls", omg_material * 6),
+                ("src", F3), ("lis", F3), ("n_rays", C.c_uint32), ("energy", F8), ("seed", C.c_uint32),
+                ("n_bands", C.c_uint32), ("n_bins", C.c_uint32), ("max_time", C.c_float),
+                ("panel_offset", C.c_uint32), ("n_panels", C.c_uint32)]
+
+
+class omg_reverb(C.Structure):
+    _fields_ = [("rt60", F8), ("level", F8), ("rt60_fit", F8), ("segments", C.c_uint64)]
+
+
+class omg_dome_panel(C.Structure):
+    _fields_ = [("axis", C.c_int32), ("plane", C.c_float), ("lat0", C.c_float), ("lat1", C.c_float),
+                ("z0", C.c_float), ("z1", C.c_float), ("glass", C.c_int32), ("trans", F8)]
+
+
+class omg_dome_bin(C.Structure):
+    _fields_ = [("dir", F3), ("energy", F8)]
+
+
+class omg_tune_result(C.Structure):
+    _fields_ = [("block_threads", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("refill_min", C.c_uint32),
+                ("ms", C.c_float)]
+
+
+P, U32, U64, I32, F = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int32, C.c_float
+PU32, PU64 = C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)
+
+# name -> (restype, argtypes); every symbol include/omg_cuda.h declares
+SIGNATURES = {
+    "omg_params_default": (None, [C.POINTER(omg_params)]),
+    "omg_create": (P, [C.POINTER(omg_params)]),
+    "omg_destroy": (None, [P]),
+    "omg_abi_version": (I32, []),
+    "omg_status_string": (C.c_char_p, [I32]),
+    "omg_last_error": (C.c_char_p, [P]),
+    "omg_set_stream": (I32, [P, P]),
+    "omg_mb_create": (P, []),
+    "omg_mb_destroy": (None, [P]),
+    "omg_mb_material": (U32, [P, C.POINTER(omg_material)]),
+    "omg_mb_begin_surface": (U32, [P]),
+    "omg_mb_coarse": (None, [P, F]),
+    "omg_mb_tri": (None, [P, P, P, P, U32]),
+    "omg_mb_quad": (None, [P, P, P, P, P, U32]),
+    "omg_mb_abox": (None, [P, P, P, U32]),
+    "omg_mb_quads": (None, [P, P, P, P, P, U32]),
+    "omg_mb_counts": (None, [P, PU32, PU32, PU32]),
+    "omg_mb_export": (None, [P, P, P, P, P, P]),
+    "omg_scene_upload": (I32, [P, P, U32, P, U32, P, P, P, U32, U32, U32, PU32]),
+    "omg_scene_from_builder": (I32, [P, P, U32, U32, PU32]),
+    "omg_scene_release": (I32, [P, U32]),
+    "omg_scene_info": (I32, [P, U32, PU32, PU32, PU32]),
+    "omg_scene_export_bvh": (I32, [P, U32, P, P, P, P, P]),
+    "omg_trace_box": (I32, [P, C.POINTER(omg_box_job), P, P, P]),
+    "omg_trace_world": (I32, [P, U32, C.POINTER(omg_world_job), P, U32, P, P, P]),
+    "omg_trace_batch": (I32, [P, P, U32, P, U32, P, P, P]),
+    "omg_batch_create": (I32, [P, P, U32, P, U32, PU32]),
+    "omg_batch_launch": (I32, [P, U32]),
+    "omg_batch_launch_part": (I32, [P, U32, U32]),
+    "omg_io_bytes": (I32, [P, PU64, PU64]),
+    "omg_batch_read": (I32, [P, U32, P, P, P]),
+    "omg_batch_sizes": (I32, [P, U32, PU64, PU64]),
+    "omg_batch_segments": (I32, [P, U32, PU64]),
+    "omg_batch_destroy": (I32, [P, U32]),
+    "omg_batch_kernel_count": (I32, [P, U32, PU32]),
+    "omg_submit_world": (I32, [P, U32, C.POINTER(omg_world_job), P, U32, PU32]),
+    "omg_poll": (I32, [P, U32, P, P, P]),
+    "omg_batch_autotune": (I32, [P, U32, U32, C.POINTER(omg_tune_result)]),
+    "omg_raycast": (I32, [P, U32, P, P, U32, P, P]),
+    "omg_estimate_reverb": (I32, [P, P, U32, U32, F, U32, P]),
+    "omg_dome_create": (I32, [P, U32, P, U32, U32, U32, PU32]),
+    "omg_dome_destroy": (I32, [P, U32]),
+    "omg_dome_sample": (I32, [P, U32, P, U32, P, U32, U32, U32, P, P, P, P]),
+    "omg_dome_segments": (I32, [P, U32, PU64, PU64]),
+}
+
+_lib = None
+
+
+class OmgError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {status_string(status)} ({status})" if what else status_string(status))
+
+
+def lib() -> C.CDLL:
+    """Load libomg_cuda.so; raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with omg_audio_gb300.build.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def status_string(s: int) -> str:
+    return lib().omg_status_string(s).decode()
+
+
+def check(status: int, what: str = ""):
+    if status < 0:
+        raise OmgError(status, what)
+    return status

@@ -1,0 +1,683 @@
+// C ABI of the GB300 tracer (include/omg_cuda.h), part 1: contexts, batches,
+// CUDA-graph launches, bounded waits, async tickets, the autotuner.
+#include "runtime.h"
+
+using namespace omg;
+
+namespace omg {
+
+int32_t fail(omg_ctx* ctx, cudaError_t e, const char* where) {
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "%s: %s", where, cudaGetErrorString(e));
+  ctx->last_error = buf;
+  cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? OMG_E_OOM : OMG_E_DEVICE;
+}
+
+uint32_t timeout_of(const omg_ctx* ctx) { return ctx->prm.timeout_ms ? ctx->prm.timeout_ms : 10000u; }
+
+// Bounded wait on an event: poll, never block indefinitely.
+int32_t wait_event(omg_ctx* ctx, cudaEvent_t ev, uint32_t timeout_ms) {
+  auto t0 = std::chrono::steady_clock::now();
+  while (true) {
+    cudaError_t q = cudaEventQuery(ev);
+    if (q == cudaSuccess) return OMG_OK;
+    if (q != cudaErrorNotReady) return fail(ctx, q, "cudaEventQuery");
+    auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+    if ((uint64_t)ms >= timeout_ms) {
+      ctx->last_error = "timeout waiting for the device";
+      return OMG_E_TIMEOUT;
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+bool valid_material(const omg_material& m, uint32_t nb) {
+  for (uint32_t b = 0; b < nb; b++) {
+    if (!std::isfinite(m.absorption[b]) || !std::isfinite(m.transmission[b])) return false;
+  }
+  return std::isfinite(m.scattering);
+}
+
+bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+int32_t sync_scene_table(omg_ctx* ctx) {
+  uint32_t need = ctx->next_scene + 1;
+  if (need > ctx->scene_cap) {
+    uint32_t cap = std::max<uint32_t>(16, need * 2);
+    DevBuf<DScene> nt;
+    CK(nt.alloc(cap));
+    CK(cudaMemset(nt.p, 0, cap * sizeof(DScene)));
+    std::swap(ctx->d_scenes.p, nt.p);
+    std::swap(ctx->d_scenes.n, nt.n);
+    ctx->scene_cap = cap;
+  }
+  std::vector<DScene> table(ctx->scene_cap);
+  std::memset(table.data(), 0, table.size() * sizeof(DScene));
+  for (auto& kv : ctx->scenes) {
+    SceneRec& s = *kv.second;
+    DScene& d = table[kv.first];
+    d.nodes = s.nodes.p;
+    d.prims = s.prims.p;
+    d.normals = s.normals.p;
+    d.mats = s.mats.p;
+    d.tri_surface = s.tri_surface.p;
+    d.root = s.root;
+    d.n_nodes = s.n_nodes;
+    d.n_prims = s.n_prims;
+    d.n_bands = s.n_bands;
+  }
+  CK(cudaMemcpy(ctx->d_scenes.p, table.data(), table.size() * sizeof(DScene), cudaMemcpyHostToDevice));
+  return OMG_OK;
+}
+
+}  // namespace omg
+
+namespace {
+
+// ---------------------------------------------------------------- batches
+uint64_t batch_signature(const omg_job* jobs, uint32_t n, uint32_t n_panels, const omg_params& P) {
+  uint64_t h = 1469598103934665603ULL ^ n ^ ((uint64_t)n_panels << 32);
+  auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ULL; };
+  for (uint32_t i = 0; i < n; i++) {
+    const omg_job& j = jobs[i];
+    mix(j.geom);
+    mix(j.scene_id);
+    mix(j.n_rays);
+    mix(j.n_bands ? j.n_bands : P.n_bands);
+    mix(j.n_bins ? j.n_bins : P.n_bins);
+    mix(j.n_panels);
+    mix(j.panel_offset);
+  }
+  return h;
+}
+
+// Fill the host-side job arrays of a batch (no device work).
+int32_t fill_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                   uint32_t n_panels) {
+  const omg_params& P = ctx->prm;
+  B.n_jobs = n_jobs;
+  B.jobs.assign(n_jobs, DJob{});
+  B.job_mats.clear();
+  B.panels.clear();
+  B.rjobs.assign(n_jobs, DReverbJob{});
+  uint64_t acc = 0, out = 0, rays = 0;
+  B.max_nb = 0;
+  B.max_bins = 0;
+  B.n_bin_floats = 0;
+  B.n_dir_floats = 0;
+  // per-job panel materials are placed after all box wall materials
+  for (uint32_t i = 0; i < n_jobs; i++) {
+    const omg_job& j = jobs[i];
+    DJob& d = B.jobs[i];
+    std::memset(&d, 0, sizeof(d));
+    uint32_t nb = j.n_bands ? j.n_bands : P.n_bands;
+    uint32_t n_bins = j.n_bins ? j.n_bins : P.n_bins;
+    float max_time = j.max_time > 0.0f ? j.max_time : P.max_time;
+    if (nb == 0 || nb > (uint32_t)MAXB || n_bins == 0 || j.n_rays == 0) return OMG_E_INVALID;
+    if (P.dir_band >= nb) return OMG_E_INVALID;
+    if (!finite3(j.src) || !finite3(j.lis)) return OMG_E_INVALID;
+    if ((uint64_t)j.panel_offset + j.n_panels > n_panels) return OMG_E_INVALID;
+    d.geom = j.geom;
+    d.n_rays = j.n_rays;
+    d.seed = j.seed;
+    for (int k = 0; k < 3; k++) {
+      d.src[k] = j.src[k];
+      d.lis[k] = j.lis[k];
+    }
+    d.per_ray = 1.0f / (float)j.n_rays;                     // tracer.rs:90
+    d.floor_e = P.energy_floor * d.per_ray;                 // tracer.rs:163
+    for (uint32_t b = 0; b < nb; b++) d.e0[b] = d.per_ray * j.energy[b];  // tracer.rs:95
+    d.nb = nb;
+    d.n_bins = n_bins;
+    d.max_bounces = P.max_bounces;
+    d.dir_band = P.dir_band;
+    d.bin_dt = P.bin_dt;
+    d.max_time = max_time;
+    d.rr = P.receiver_radius;
+    d.wall_eps = P.wall_eps;
+    d.c = P.speed_of_sound;
+    if (j.geom == OMG_GEOM_BOX) {
+      if (!finite3(j.box_size)) return OMG_E_INVALID;
+      for (int k = 0; k < 3; k++) d.box[k] = j.box_size[k];
+      d.box_mat = (uint32_t)B.job_mats.size();
+      for (int w = 0; w < 6; w++) {
+        if (!valid_material(j.box_walls[w], nb)) return OMG_E_INVALID;
+        B.job_mats.push_back(make_dmat(j.box_walls[w], nb));
+      }
+    } else if (j.geom == OMG_GEOM_MESH) {
+      auto it = ctx->scenes.find(j.scene_id);
+      if (it == ctx->scenes.end()) return OMG_E_NOT_FOUND;
+      if (it->second->n_bands != nb) return OMG_E_INVALID;
+      d.scene = j.scene_id;
+    } else {
+      return OMG_E_INVALID;
+    }
+    d.panel_off = (uint32_t)B.panels.size();
+    d.n_panels = j.n_panels;
+    for (uint32_t k = 0; k < j.n_panels; k++) {
+      const omg_panel& p = panels[j.panel_offset + k];
+      if (!finite3(p.mn) || !finite3(p.mx) || !valid_material(p.material, nb)) return OMG_E_INVALID;
+      DPanel dp;
+      std::memset(&dp, 0, sizeof(dp));
+      for (int c = 0; c < 3; c++) {
+        dp.mn[c] = p.mn[c];
+        dp.mx[c] = p.mx[c];
+      }
+      dp.mat = (uint32_t)B.job_mats.size();
+      B.job_mats.push_back(make_dmat(p.material, nb));
+      B.panels.push_back(dp);
+    }
+    d.ray_base = (uint32_t)rays;
+    rays += j.n_rays;
+    if (rays > 0xFFFFFFFFull) return OMG_E_INVALID;
+    d.acc_off = acc;
+    d.out_off = out;
+    acc += acc_floats(n_bins, nb);
+    out += out_floats(n_bins, nb);
+    B.max_nb = std::max(B.max_nb, nb);
+    B.max_bins = std::max(B.max_bins, n_bins);
+    B.n_bin_floats += (uint64_t)n_bins * nb;
+    B.n_dir_floats += (uint64_t)n_bins * 3;
+    DReverbJob& r = B.rjobs[i];
+    r.bins_off = d.out_off;
+    r.n_bins = n_bins;
+    r.nb = nb;
+    r.bin_dt = P.bin_dt;
+  }
+  B.total_rays = (uint32_t)rays;
+  B.n_acc = acc;
+  B.n_out = out;
+  return OMG_OK;
+}
+
+int32_t alloc_batch(omg_ctx* ctx, BatchRec& B) {
+  CK(B.d_jobs.alloc(B.n_jobs));
+  CK(B.d_job_mats.alloc(B.job_mats.size()));
+  CK(B.d_panels.alloc(B.panels.size()));
+  CK(B.d_acc.alloc(B.n_acc));
+  CK(B.d_out.alloc(B.n_out));
+  CK(B.d_hdr.alloc(1));
+  CK(B.d_seg.alloc(B.n_jobs));
+  CK(B.d_rjobs.alloc(B.n_jobs));
+  CK(B.d_reverb.alloc(B.n_jobs));
+  CK(B.h_out.alloc(B.n_out));
+  CK(B.h_reverb.alloc(B.n_jobs));
+  CK(B.h_hdr.alloc(1));
+  CK(B.h_seg.alloc(B.n_jobs));
+  CK(B.h_jobs.alloc(B.n_jobs));
+  if (!B.done) CK(cudaEventCreateWithFlags(&B.done, cudaEventDisableTiming));
+  return OMG_OK;
+}
+
+// Upload the job-dependent arrays (synchronous on the context stream).
+int32_t upload_batch(omg_ctx* ctx, BatchRec& B) {
+  std::memcpy(B.h_jobs.p, B.jobs.data(), B.n_jobs * sizeof(DJob));
+  CK(cudaMemcpyAsync(B.d_jobs.p, B.h_jobs.p, B.n_jobs * sizeof(DJob), cudaMemcpyHostToDevice, ctx->stream));
+  if (!B.job_mats.empty())
+    CK(cudaMemcpyAsync(B.d_job_mats.p, B.job_mats.data(), B.job_mats.size() * sizeof(DMat), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  if (!B.panels.empty())
+    CK(cudaMemcpyAsync(B.d_panels.p, B.panels.data(), B.panels.size() * sizeof(DPanel), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  CK(cudaMemcpyAsync(B.d_rjobs.p, B.rjobs.data(), B.n_jobs * sizeof(DReverbJob), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return OMG_OK;
+}
+
+// The device-side work of one launch (recorded into a graph).
+// part 1: clear the scratch and trace; part 2: finalize and reverb.
+int32_t record_launch(omg_ctx* ctx, BatchRec& B, cudaStream_t s, int parts = 3) {
+  if (parts & 1) {
+    CK(cudaMemsetAsync(B.d_hdr.p, 0, sizeof(DLaunch), s));
+    CK(cudaMemsetAsync(B.d_acc.p, 0, B.n_acc * sizeof(float), s));
+    CK(cudaMemsetAsync(B.d_seg.p, 0, B.n_jobs * sizeof(uint32_t), s));
+    CK(launch_trace(B.d_jobs.p, B.n_jobs, B.total_rays, B.max_nb, ctx->d_scenes.p, B.d_job_mats.p, B.d_panels.p,
+                    B.d_acc.p, B.d_hdr.p, B.d_seg.p, B.shape, ctx->n_sms, s));
+  }
+  if (parts & 2) {
+    CK(launch_finalize(B.d_jobs.p, B.n_jobs, B.d_acc.p, B.d_out.p, B.n_out, s));
+    CK(launch_reverb(B.d_rjobs.p, B.n_jobs, B.max_bins, B.d_out.p, B.d_reverb.p, B.d_seg.p, s));
+  }
+  return OMG_OK;
+}
+
+int32_t record_readback(omg_ctx* ctx, BatchRec& B, cudaStream_t s) {
+  CK(cudaMemcpyAsync(B.h_out.p, B.d_out.p, B.n_out * sizeof(float), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(B.h_reverb.p, B.d_reverb.p, B.n_jobs * sizeof(omg_reverb), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(B.h_hdr.p, B.d_hdr.p, sizeof(DLaunch), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(B.h_seg.p, B.d_seg.p, B.n_jobs * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  return OMG_OK;
+}
+
+int32_t build_graphs(omg_ctx* ctx, BatchRec& B) {
+  for (cudaGraphExec_t* g : {&B.graph, &B.graph_io, &B.graph_a, &B.graph_b}) {
+    if (*g) cudaGraphExecDestroy(*g);
+    *g = nullptr;
+  }
+  cudaStream_t cs;
+  CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  auto capture = [&](bool io, cudaGraphExec_t* out, int parts = 3) -> int32_t {
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail(ctx, e, "cudaStreamBeginCapture");
+    int32_t rc = OMG_OK;
+    if (io) {
+      e = cudaMemcpyAsync(B.d_jobs.p, B.h_jobs.p, B.n_jobs * sizeof(DJob), cudaMemcpyHostToDevice, cs);
+      if (e != cudaSuccess) rc = fail(ctx, e, "cudaMemcpyAsync jobs");
+    }
+    if (rc == OMG_OK) rc = record_launch(ctx, B, cs, parts);
+    if (rc == OMG_OK && io) rc = record_readback(ctx, B, cs);
+    e = cudaStreamEndCapture(cs, &g);
+    if (rc != OMG_OK) return rc;
+    if (e != cudaSuccess) return fail(ctx, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(ctx, e, "cudaGraphInstantiate");
+    return OMG_OK;
+  };
+  int32_t rc = capture(false, &B.graph);
+  if (rc == OMG_OK) rc = capture(true, &B.graph_io);
+  if (rc == OMG_OK) rc = capture(false, &B.graph_a, 1);
+  if (rc == OMG_OK) rc = capture(false, &B.graph_b, 2);
+  cudaStreamDestroy(cs);
+  return rc;
+}
+
+int32_t prepare_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                      uint32_t n_panels) {
+  int32_t rc = fill_batch(ctx, B, jobs, n_jobs, panels, n_panels);
+  if (rc) return rc;
+  if ((rc = alloc_batch(ctx, B))) return rc;
+  if ((rc = upload_batch(ctx, B))) return rc;
+  if ((rc = build_graphs(ctx, B))) return rc;
+  B.signature = batch_signature(jobs, n_jobs, n_panels, ctx->prm);
+  return OMG_OK;
+}
+
+int32_t check_kernel_flags(omg_ctx* ctx, const BatchRec& B) {
+  if (B.h_hdr.p->error) {
+    ctx->last_error = "traversal stack overflow in the trace kernel";
+    return OMG_E_OVERFLOW;
+  }
+  return OMG_OK;
+}
+
+void copy_results(const BatchRec& B, float* bins, float* dirs, omg_reverb* reverb) {
+  uint64_t bo = 0, dof = 0;
+  for (uint32_t i = 0; i < B.n_jobs; i++) {
+    const DJob& j = B.jobs[i];
+    uint64_t nbb = (uint64_t)j.n_bins * j.nb, nd = (uint64_t)j.n_bins * 3;
+    if (bins) std::memcpy(bins + bo, B.h_out.p + j.out_off, nbb * sizeof(float));
+    if (dirs) std::memcpy(dirs + dof, B.h_out.p + j.out_off + nbb, nd * sizeof(float));
+    bo += nbb;
+    dof += nd;
+  }
+  if (reverb) {
+    std::memcpy(reverb, B.h_reverb.p, B.n_jobs * sizeof(omg_reverb));
+    for (uint32_t i = 0; i < B.n_jobs; i++) reverb[i].segments = B.h_seg.p[i];
+  }
+}
+
+// One synchronous pass through the io graph: H2D jobs, launch, D2H, bounded wait.
+int32_t run_io(omg_ctx* ctx, BatchRec& B, float* bins, float* dirs, omg_reverb* reverb) {
+  std::memcpy(B.h_jobs.p, B.jobs.data(), B.n_jobs * sizeof(DJob));
+  ctx->last_h2d += B.n_jobs * sizeof(DJob);
+  ctx->last_d2h = B.n_out * sizeof(float) + B.n_jobs * (sizeof(omg_reverb) + sizeof(uint32_t)) + sizeof(DLaunch);
+  CK(cudaGraphLaunch(B.graph_io, ctx->stream));
+  CK(cudaEventRecord(B.done, ctx->stream));
+  int32_t rc = wait_event(ctx, B.done, timeout_of(ctx));
+  if (rc) return rc;
+  if ((rc = check_kernel_flags(ctx, B))) return rc;
+  copy_results(B, bins, dirs, reverb);
+  return OMG_OK;
+}
+
+// Synchronous one-shot through the context's cached batch (rebuilt only when
+// the job layout changes; per-call values travel in the job array).
+int32_t one_shot(omg_ctx* ctx, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels, uint32_t n_panels,
+                 float* bins, float* dirs, omg_reverb* reverb) {
+  ctx->last_h2d = 0;
+  uint64_t sig = batch_signature(jobs, n_jobs, n_panels, ctx->prm);
+  if (!ctx->cached || ctx->cached->signature != sig) {
+    ctx->cached.reset(new BatchRec());
+    int32_t rc = prepare_batch(ctx, *ctx->cached, jobs, n_jobs, panels, n_panels);
+    if (rc) {
+      ctx->cached.reset();
+      return rc;
+    }
+  } else {
+    BatchRec& B = *ctx->cached;
+    std::vector<DMat> old_mats = B.job_mats;
+    std::vector<DPanel> old_panels = B.panels;
+    int32_t rc = fill_batch(ctx, B, jobs, n_jobs, panels, n_panels);
+    if (rc) return rc;
+    // materials and panels change rarely: re-upload only when they differ
+    bool mats_same = old_mats.size() == B.job_mats.size() &&
+                     std::memcmp(old_mats.data(), B.job_mats.data(), old_mats.size() * sizeof(DMat)) == 0;
+    bool pan_same = old_panels.size() == B.panels.size() &&
+                    std::memcmp(old_panels.data(), B.panels.data(), old_panels.size() * sizeof(DPanel)) == 0;
+    if (!mats_same && !B.job_mats.empty()) ctx->last_h2d += B.job_mats.size() * sizeof(DMat);
+    if (!pan_same && !B.panels.empty()) ctx->last_h2d += B.panels.size() * sizeof(DPanel);
+    if (!mats_same && !B.job_mats.empty())
+      CK(cudaMemcpyAsync(B.d_job_mats.p, B.job_mats.data(), B.job_mats.size() * sizeof(DMat),
+                         cudaMemcpyHostToDevice, ctx->stream));
+    if (!pan_same && !B.panels.empty())
+      CK(cudaMemcpyAsync(B.d_panels.p, B.panels.data(), B.panels.size() * sizeof(DPanel), cudaMemcpyHostToDevice,
+                         ctx->stream));
+  }
+  return run_io(ctx, *ctx->cached, bins, dirs, reverb);
+}
+
+void job_from_world(omg_job& j, uint32_t scene_id, const omg_world_job& w, uint32_t n_panels) {
+  std::memset(&j, 0, sizeof(j));
+  j.geom = OMG_GEOM_MESH;
+  j.scene_id = scene_id;
+  for (int k = 0; k < 3; k++) {
+    j.src[k] = w.src[k];
+    j.lis[k] = w.lis[k];
+  }
+  j.n_rays = w.n_rays;
+  for (int b = 0; b < OMG_MAX_BANDS; b++) j.energy[b] = w.energy[b];
+  j.seed = w.seed;
+  j.n_panels = n_panels;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+void omg_params_default(omg_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->n_bands = 3;
+  p->n_bins = 300;
+  p->bin_dt = 0.010f;
+  p->max_time = 3.0f;
+  p->max_bounces = 64;
+  p->energy_floor = 1e-7f;
+  p->receiver_radius = 0.5f;
+  p->wall_eps = 1e-3f;
+  p->speed_of_sound = 343.0f;
+  p->dir_band = 1;
+  p->device = 0;
+  p->timeout_ms = 10000;
+}
+
+int32_t omg_abi_version(void) { return OMG_ABI_VERSION; }
+
+const char* omg_status_string(int32_t s) {
+  switch (s) {
+    case OMG_OK: return "ok";
+    case OMG_PENDING: return "pending";
+    case OMG_E_INVALID: return "invalid argument";
+    case OMG_E_OOM: return "out of memory";
+    case OMG_E_DEVICE: return "device error";
+    case OMG_E_TIMEOUT: return "timeout";
+    case OMG_E_OVERFLOW: return "traversal overflow";
+    case OMG_E_NOT_FOUND: return "not found";
+    case OMG_E_NO_DEVICE: return "no device";
+    default: return "unknown status";
+  }
+}
+
+const char* omg_last_error(const omg_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+omg_ctx* omg_create(const omg_params* p) {
+  omg_params prm;
+  if (p) prm = *p;
+  else omg_params_default(&prm);
+  if (prm.n_bands == 0 || prm.n_bands > OMG_MAX_BANDS || prm.n_bins == 0 || !(prm.bin_dt > 0.0f) ||
+      prm.dir_band >= prm.n_bands || !(prm.speed_of_sound > 0.0f))
+    return nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= prm.device || prm.device < 0) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (cudaSetDevice(prm.device) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  omg_ctx* ctx = new omg_ctx();
+  ctx->prm = prm;
+  ctx->device = prm.device;
+  cudaDeviceGetAttribute(&ctx->n_sms, cudaDevAttrMultiProcessorCount, prm.device);
+  if (cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return nullptr;
+  }
+  ctx->stream = ctx->own;
+  if (sync_scene_table(ctx) != OMG_OK) {
+    cudaStreamDestroy(ctx->own);
+    delete ctx;
+    return nullptr;
+  }
+  return ctx;
+}
+
+void omg_destroy(omg_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->tickets.clear();
+  ctx->batches.clear();
+  ctx->cached.reset();
+  ctx->probes.clear();
+  ctx->scenes.clear();
+  if (ctx->own) cudaStreamDestroy(ctx->own);
+  delete ctx;
+}
+
+int32_t omg_set_stream(omg_ctx* ctx, void* s) {
+  if (!ctx) return OMG_E_INVALID;
+  ctx->stream = s ? (cudaStream_t)s : ctx->own;
+  return OMG_OK;
+}
+
+
+// ------------------------------------------------------------------ batches
+int32_t omg_batch_create(omg_ctx* ctx, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                         uint32_t n_panels, uint32_t* batch_id) {
+  if (!ctx || !jobs || !n_jobs || !batch_id || (n_panels && !panels)) return OMG_E_INVALID;
+  std::unique_ptr<BatchRec> B(new BatchRec());
+  int32_t rc = prepare_batch(ctx, *B, jobs, n_jobs, panels, n_panels);
+  if (rc) return rc;
+  *batch_id = ctx->next_batch++;
+  ctx->batches[*batch_id] = std::move(B);
+  return OMG_OK;
+}
+
+int32_t omg_batch_launch(omg_ctx* ctx, uint32_t id) { return omg_batch_launch_part(ctx, id, 0); }
+
+int32_t omg_batch_launch_part(omg_ctx* ctx, uint32_t id, uint32_t part) {
+  if (!ctx || part > 2) return OMG_E_INVALID;
+  auto it = ctx->batches.find(id);
+  if (it == ctx->batches.end()) return OMG_E_NOT_FOUND;
+  BatchRec& B = *it->second;
+  CK(cudaGraphLaunch(part == 0 ? B.graph : (part == 1 ? B.graph_a : B.graph_b), ctx->stream));
+  return OMG_OK;
+}
+
+int32_t omg_io_bytes(omg_ctx* ctx, uint64_t* h2d, uint64_t* d2h) {
+  if (!ctx) return OMG_E_INVALID;
+  if (h2d) *h2d = ctx->last_h2d;
+  if (d2h) *d2h = ctx->last_d2h;
+  return OMG_OK;
+}
+
+int32_t omg_batch_read(omg_ctx* ctx, uint32_t id, float* bins, float* dirs, omg_reverb* reverb) {
+  if (!ctx) return OMG_E_INVALID;
+  auto it = ctx->batches.find(id);
+  if (it == ctx->batches.end()) return OMG_E_NOT_FOUND;
+  BatchRec& B = *it->second;
+  int32_t rc = record_readback(ctx, B, ctx->stream);
+  if (rc) return rc;
+  CK(cudaEventRecord(B.done, ctx->stream));
+  if ((rc = wait_event(ctx, B.done, timeout_of(ctx)))) return rc;
+  if ((rc = check_kernel_flags(ctx, B))) return rc;
+  copy_results(B, bins, dirs, reverb);
+  return OMG_OK;
+}
+
+int32_t omg_batch_sizes(omg_ctx* ctx, uint32_t id, uint64_t* nb, uint64_t* nd) {
+  if (!ctx) return OMG_E_INVALID;
+  auto it = ctx->batches.find(id);
+  if (it == ctx->batches.end()) return OMG_E_NOT_FOUND;
+  if (nb) *nb = it->second->n_bin_floats;
+  if (nd) *nd = it->second->n_dir_floats;
+  return OMG_OK;
+}
+
+int32_t omg_batch_segments(omg_ctx* ctx, uint32_t id, uint64_t* segments) {
+  if (!ctx || !segments) return OMG_E_INVALID;
+  auto it = ctx->batches.find(id);
+  if (it == ctx->batches.end()) return OMG_E_NOT_FOUND;
+  BatchRec& B = *it->second;
+  CK(cudaMemcpyAsync(B.h_seg.p, B.d_seg.p, B.n_jobs * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaEventRecord(B.done, ctx->stream));
+  int32_t rc = wait_event(ctx, B.done, timeout_of(ctx));
+  if (rc) return rc;
+  uint64_t s = 0;
+  for (uint32_t i = 0; i < B.n_jobs; i++) s += B.h_seg.p[i];
+  *segments = s;
+  return OMG_OK;
+}
+
+int32_t omg_batch_destroy(omg_ctx* ctx, uint32_t id) {
+  if (!ctx) return OMG_E_INVALID;
+  auto it = ctx->batches.find(id);
+  if (it == ctx->batches.end()) return OMG_E_NOT_FOUND;
+  cudaStreamSynchronize(ctx->stream);
+  ctx->batches.erase(it);
+  return OMG_OK;
+}
+
+int32_t omg_batch_kernel_count(omg_ctx* ctx, uint32_t id, uint32_t* n) {
+  if (!ctx || !n) return OMG_E_INVALID;
+  if (ctx->batches.find(id) == ctx->batches.end()) return OMG_E_NOT_FOUND;
+  *n = 3;  // trace, finalize, reverb
+  return OMG_OK;
+}
+
+// ------------------------------------------------------------------ tracing
+int32_t omg_trace_box(omg_ctx* ctx, const omg_box_job* job, float* bins, float* dirs, omg_reverb* reverb) {
+  if (!ctx || !job) return OMG_E_INVALID;
+  omg_job j;
+  std::memset(&j, 0, sizeof(j));
+  j.geom = OMG_GEOM_BOX;
+  for (int k = 0; k < 3; k++) {
+    j.box_size[k] = job->size[k];
+    j.src[k] = job->src[k];
+    j.lis[k] = job->lis[k];
+  }
+  for (int w = 0; w < 6; w++) j.box_walls[w] = job->walls[w];
+  j.n_rays = job->n_rays;
+  for (int b = 0; b < OMG_MAX_BANDS; b++) j.energy[b] = job->energy[b];
+  j.seed = job->seed;
+  return one_shot(ctx, &j, 1, nullptr, 0, bins, dirs, reverb);
+}
+
+int32_t omg_trace_world(omg_ctx* ctx, uint32_t scene_id, const omg_world_job* job, const omg_panel* panels,
+                        uint32_t n_panels, float* bins, float* dirs, omg_reverb* reverb) {
+  if (!ctx || !job || (n_panels && !panels)) return OMG_E_INVALID;
+  omg_job j;
+  job_from_world(j, scene_id, *job, n_panels);
+  return one_shot(ctx, &j, 1, panels, n_panels, bins, dirs, reverb);
+}
+
+int32_t omg_trace_batch(omg_ctx* ctx, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                        uint32_t n_panels, float* bins, float* dirs, omg_reverb* reverb) {
+  if (!ctx || !jobs || !n_jobs || (n_panels && !panels)) return OMG_E_INVALID;
+  return one_shot(ctx, jobs, n_jobs, panels, n_panels, bins, dirs, reverb);
+}
+
+// ------------------------------------------------------------ async tickets
+int32_t omg_submit_world(omg_ctx* ctx, uint32_t scene_id, const omg_world_job* job, const omg_panel* panels,
+                         uint32_t n_panels, uint32_t* ticket) {
+  if (!ctx || !job || !ticket || (n_panels && !panels)) return OMG_E_INVALID;
+  omg_job j;
+  job_from_world(j, scene_id, *job, n_panels);
+  Ticket t;
+  t.batch.reset(new BatchRec());
+  int32_t rc = prepare_batch(ctx, *t.batch, &j, 1, panels, n_panels);
+  if (rc) return rc;
+  BatchRec& B = *t.batch;
+  std::memcpy(B.h_jobs.p, B.jobs.data(), sizeof(DJob));
+  CK(cudaGraphLaunch(B.graph_io, ctx->stream));
+  CK(cudaEventRecord(B.done, ctx->stream));
+  *ticket = ctx->next_ticket++;
+  ctx->tickets[*ticket] = std::move(t);
+  return OMG_OK;
+}
+
+int32_t omg_poll(omg_ctx* ctx, uint32_t ticket, float* bins, float* dirs, omg_reverb* reverb) {
+  if (!ctx) return OMG_E_INVALID;
+  auto it = ctx->tickets.find(ticket);
+  if (it == ctx->tickets.end()) return OMG_E_NOT_FOUND;
+  BatchRec& B = *it->second.batch;
+  cudaError_t q = cudaEventQuery(B.done);
+  if (q == cudaErrorNotReady) return OMG_PENDING;
+  if (q != cudaSuccess) return fail(ctx, q, "cudaEventQuery");
+  int32_t rc = check_kernel_flags(ctx, B);
+  if (rc == OMG_OK) copy_results(B, bins, dirs, reverb);
+  ctx->tickets.erase(it);
+  return rc;
+}
+
+// ---------------------------------------------------------------- autotuner
+int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_result* best) {
+  if (!ctx || !best) return OMG_E_INVALID;
+  auto it = ctx->batches.find(id);
+  if (it == ctx->batches.end()) return OMG_E_NOT_FOUND;
+  BatchRec& B = *it->second;
+  if (reps == 0) reps = 3;
+  const uint32_t threads[] = {64, 128, 256};
+  const uint32_t per_sm[] = {2, 4, 8, 16};
+  const uint32_t refill[] = {1, 8, 16};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  LaunchShape keep = B.shape;
+  float best_ms = 1e30f;
+  LaunchShape best_shape = keep;
+  int32_t rc = OMG_OK;
+  for (uint32_t th : threads)
+    for (uint32_t ps : per_sm)
+      for (uint32_t rf : refill) {
+        if (th * ps > 2048) continue;
+        B.shape.block_threads = th;
+        B.shape.blocks_per_sm = ps;
+        B.shape.refill_min = rf;
+        // warm-up, then timed repetitions on the context stream
+        if ((rc = record_launch(ctx, B, ctx->stream))) goto done;
+        if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { rc = OMG_E_DEVICE; goto done; }
+        for (uint32_t r = 0; r < reps; r++)
+          if ((rc = record_launch(ctx, B, ctx->stream))) goto done;
+        if (cudaEventRecord(e1, ctx->stream) != cudaSuccess) { rc = OMG_E_DEVICE; goto done; }
+        if ((rc = wait_event(ctx, e1, timeout_of(ctx) * (reps + 1)))) goto done;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= reps;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best_shape = B.shape;
+        }
+      }
+done:
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  B.shape = rc == OMG_OK ? best_shape : keep;
+  if (rc) return rc;
+  if ((rc = build_graphs(ctx, B))) return rc;
+  best->block_threads = best_shape.block_threads;
+  best->blocks_per_sm = best_shape.blocks_per_sm;
+  best->refill_min = best_shape.refill_min;
+  best->ms = best_ms;
+  return OMG_OK;
+}
+
+}  // extern "C"

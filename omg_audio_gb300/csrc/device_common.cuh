@@ -1,0 +1,187 @@
+// Device routines shared by the tracer (trace.cu) and the dome (dome.cu):
+// the per-ray stream, unit_sphere, normalize, the slab and Möller–Trumbore
+// tests and the ordered closest-hit traversal. All f32 arithmetic follows the
+// reference's operation order; the including files build with -fmad=false.
+#pragma once
+#include <cfloat>
+
+#include "omg_internal.h"
+
+namespace omg {
+
+static constexpr float TAU_F = 6.28318530717958647692f;   // core::f32::consts::TAU
+static constexpr float ONE_EPS = 1.0f + 1e-6f;              // mesh.rs:446,451 (f32 sum)
+
+// Per-ray PCG-RXS-M-XS stream (trace_mesh.wgsl:90-98, seeding :211-213).
+struct Pcg {
+  uint32_t s;
+  __device__ __forceinline__ void init(uint32_t seed, uint32_t ray) {
+    s = (seed ^ (ray * 0x9E3779B9u)) + 1u;
+    next();
+    next();
+  }
+  __device__ __forceinline__ uint32_t next() {
+    s = s * 747796405u + 2891336453u;
+    uint32_t w = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
+    return (w >> 22u) ^ w;
+  }
+  // (x >> 8) / 2^24 (rng.rs:19-21 form); the product by 2^-24 is exact
+  __device__ __forceinline__ float f32() { return (float)(next() >> 8u) * 5.9604644775390625e-8f; }
+};
+
+// rng.rs:24-29
+__device__ __forceinline__ void unit_sphere(Pcg& g, float& x, float& y, float& z) {
+  float u1 = g.f32();
+  z = 1.0f - 2.0f * u1;
+  float r = sqrtf(fmaxf(1.0f - z * z, 0.0f));
+  float phi = TAU_F * g.f32();
+  double sd, cd;
+  sincos((double)phi, &sd, &cd);
+  x = r * (float)cd;
+  y = r * (float)sd;
+}
+
+// vec3.rs:19-26 (multiply by the reciprocal; (1,0,0) below 1e-12)
+__device__ __forceinline__ void normalize3(float& x, float& y, float& z) {
+  float l = sqrtf(x * x + y * y + z * z);
+  if (l > 1e-12f) {
+    float inv = 1.0f / l;
+    x = x * inv;
+    y = y * inv;
+    z = z * inv;
+  } else {
+    x = 1.0f;
+    y = 0.0f;
+    z = 0.0f;
+  }
+}
+
+// mesh.rs:407-426. Swap by comparison (a NaN entry stays in place and fmaxf /
+// fminf then ignore it, as Rust's f32::max/min do); the single final check is
+// equivalent to the per-axis early exit because t0 only grows and t1 only
+// shrinks.
+__device__ __forceinline__ bool ray_aabb(float lx, float ly, float lz, float hx, float hy, float hz, float ox,
+                                         float oy, float oz, float ix, float iy, float iz, float tmax, float& tout) {
+  float t0 = 0.0f, t1 = tmax;
+  float ta = (lx - ox) * ix, tb = (hx - ox) * ix;
+  float lo = ta > tb ? tb : ta, hi = ta > tb ? ta : tb;
+  t0 = fmaxf(t0, lo);
+  t1 = fminf(t1, hi);
+  ta = (ly - oy) * iy;
+  tb = (hy - oy) * iy;
+  lo = ta > tb ? tb : ta;
+  hi = ta > tb ? ta : tb;
+  t0 = fmaxf(t0, lo);
+  t1 = fminf(t1, hi);
+  ta = (lz - oz) * iz;
+  tb = (hz - oz) * iz;
+  lo = ta > tb ? tb : ta;
+  hi = ta > tb ? ta : tb;
+  t0 = fmaxf(t0, lo);
+  t1 = fminf(t1, hi);
+  tout = t0;
+  return t0 <= t1;
+}
+
+// mesh.rs:436-456 — Möller–Trumbore, both faces, reference epsilons.
+__device__ __forceinline__ bool ray_tri(const float4& p0, const float4& p1, const float4& p2, float ox, float oy,
+                                        float oz, float dx, float dy, float dz, float& tout) {
+  const float e1x = p1.x, e1y = p1.y, e1z = p1.z;
+  const float e2x = p2.x, e2y = p2.y, e2z = p2.z;
+  float px = dy * e2z - dz * e2y;
+  float py = dz * e2x - dx * e2z;
+  float pz = dx * e2y - dy * e2x;
+  float det = e1x * px + e1y * py + e1z * pz;
+  if (fabsf(det) < 1e-9f) return false;
+  float inv = 1.0f / det;
+  float sx = ox - p0.x, sy = oy - p0.y, sz = oz - p0.z;
+  float u = (sx * px + sy * py + sz * pz) * inv;
+  if (!(u >= -1e-6f && u <= ONE_EPS)) return false;
+  float qx = sy * e1z - sz * e1y;
+  float qy = sz * e1x - sx * e1z;
+  float qz = sx * e1y - sy * e1x;
+  float v = (dx * qx + dy * qy + dz * qz) * inv;
+  if (v < -1e-6f || u + v > ONE_EPS) return false;
+  float t = (e2x * qx + e2y * qy + e2z * qz) * inv;
+  if (t > 1e-5f) {
+    tout = t;
+    return true;
+  }
+  return false;
+}
+
+// mesh.rs:484-541 — ordered closest-hit traversal over the child-box BVH2.
+// Visit order, culling (t_enter >= best) and the strict `<` on hits are the
+// reference's, so over the reference tree the same triangle wins every tie.
+__device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy, float oz, float dx, float dy, float dz,
+                             float& t_best, int& prim_best, uint32_t* err) {
+  if (S.n_prims == 0) return false;
+  const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+  const float4* __restrict__ nodes = S.nodes;
+  const float4* __restrict__ prims = S.prims;
+  bool have = false;
+  t_best = FLT_MAX;
+  int stack_ref[STACK_DEPTH];
+  float stack_t[STACK_DEPTH];
+  int sp = 0;
+  int cur = S.root;
+  while (true) {
+    if (cur >= 0) {
+      const float4 n0 = __ldg(nodes + 4 * cur + 0);
+      const float4 n1 = __ldg(nodes + 4 * cur + 1);
+      const float4 n2 = __ldg(nodes + 4 * cur + 2);
+      const float4 n3 = __ldg(nodes + 4 * cur + 3);
+      const float tmax = have ? t_best : FLT_MAX;
+      float ta, tb;
+      const bool h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ox, oy, oz, ix, iy, iz, tmax, ta);
+      const bool h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ox, oy, oz, ix, iy, iz, tmax, tb);
+      const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+      if (h0 && h1) {
+        int nr, fr;
+        float nt, ft;
+        if (ta <= tb) { nr = c0; nt = ta; fr = c1; ft = tb; }
+        else { nr = c1; nt = tb; fr = c0; ft = ta; }
+        if (sp < STACK_DEPTH) {
+          stack_ref[sp] = fr;
+          stack_t[sp] = ft;
+          sp++;
+        } else {
+          atomicOr(err, 1u);
+        }
+        if (!(have && nt >= t_best)) { cur = nr; continue; }
+      } else if (h0) {
+        if (!(have && ta >= t_best)) { cur = c0; continue; }
+      } else if (h1) {
+        if (!(have && tb >= t_best)) { cur = c1; continue; }
+      }
+    } else {
+      const uint32_t code = ~(uint32_t)cur;
+      const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
+      for (uint32_t i = start; i < end; i++) {
+        const float4 p0 = __ldg(prims + 3 * i + 0);
+        const float4 p1 = __ldg(prims + 3 * i + 1);
+        const float4 p2 = __ldg(prims + 3 * i + 2);
+        float t;
+        if (ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) {
+          if (!have || t < t_best) {
+            have = true;
+            t_best = t;
+            prim_best = (int)i;
+          }
+        }
+      }
+    }
+    bool found = false;
+    while (sp > 0) {
+      sp--;
+      if (have && stack_t[sp] >= t_best) continue;
+      cur = stack_ref[sp];
+      found = true;
+      break;
+    }
+    if (!found) break;
+  }
+  return have;
+}
+
+}  // namespace omg

@@ -1,0 +1,170 @@
+// Device-side layout shared by the host runtime (api.cpp, scene.cpp) and the
+// kernels (trace.cu, dome.cu, lbvh.cu, reverb.cu).
+//
+// HBM layout of one scene (all 16-byte aligned, read through the read-only
+// path):
+//   nodes   : BVH2 with both child boxes in the parent, 64 B per node
+//             n0 = (c0.lo.x, c0.lo.y, c0.lo.z, c0.hi.x)
+//             n1 = (c0.hi.y, c0.hi.z, c1.lo.x, c1.lo.y)
+//             n2 = (c1.lo.z, c1.hi.x, c1.hi.y, c1.hi.z)
+//             n3 = (c0 ref, c1 ref, -, -) as int bits
+//             ref >= 0: internal node index; ref < 0: leaf ~((start << 3) | (count - 1))
+//   prims   : 48 B per tessellated primitive, in leaf order
+//             p0 = (a.xyz, material id)  p1 = (e1.xyz, original tri id)  p2 = (e2.xyz, surface id)
+//   normals : 16 B per ORIGINAL triangle: normalize(e1 x e2) of the authored triangle
+//             (mesh.rs:458-461), .w = material id
+//   mats    : 80 B per material, with the branch weights precomputed (bit-identical
+//             to computing them per bounce: same f32 operations, same order)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/omg_cuda.h"
+
+namespace omg {
+
+constexpr int MAXB = OMG_MAX_BANDS;
+constexpr int STACK_DEPTH = 64;           // mesh.rs:492 (64-entry traversal stack)
+
+// tracer.rs:148-182 per material: p = clamp(max_b T_b^2, 0.02, 0.5) when
+// > 1e-5 else 0; transmitted weight T_b^2 / p; reflected weight
+// max(1 - a_b - T_b^2, 0) / (1 - p).
+struct alignas(16) DMat {
+  float p;
+  float scattering;
+  float wt[MAXB];
+  float wr[MAXB];
+  float absorption[MAXB];      // dome escape: tp *= 1 - absorption (dome.rs:365-367)
+  float t2[MAXB];              // dome through: tp *= T^2 (dome.rs:398-402)
+  float pad[2];
+};
+static_assert(sizeof(DMat) == 144, "DMat layout");
+
+struct DScene {
+  const float4* nodes;
+  const float4* prims;
+  const float4* normals;
+  const DMat* mats;
+  const uint16_t* tri_surface;   // authored surface id per original tri (segment_hits merge)
+  int32_t root;                  // root ref (internal 0, or a leaf ref)
+  uint32_t n_nodes;
+  uint32_t n_prims;
+  uint32_t n_bands;
+};
+
+// Panel overlay (scene.rs:90-137): box and an index into the batch's material table.
+struct alignas(16) DPanel {
+  float mn[3];
+  uint32_t mat;
+  float mx[3];
+  uint32_t pad;
+};
+
+// One job of a launch. Values that the reference computes per ray from
+// constants are precomputed here with the same f32 operations.
+struct alignas(16) DJob {
+  uint32_t geom;          // OMG_GEOM_BOX / OMG_GEOM_MESH
+  uint32_t scene;         // index into the scene table
+  uint32_t n_rays;
+  uint32_t seed;
+  float src[3];
+  float per_ray;          // 1 / n_rays (tracer.rs:90)
+  float lis[3];
+  float floor_e;          // energy_floor * per_ray (tracer.rs:163)
+  float box[3];
+  uint32_t box_mat;       // first of 6 wall materials in the batch material table
+  float e0[MAXB];         // per_ray * source_energy[b] (tracer.rs:95)
+  uint32_t nb;
+  uint32_t n_bins;
+  uint32_t max_bounces;
+  uint32_t dir_band;
+  float bin_dt;
+  float max_time;
+  float rr;               // receiver radius
+  float wall_eps;
+  float c;                // speed of sound
+  uint32_t panel_off;
+  uint32_t n_panels;
+  uint32_t ray_base;      // first global ray id of this job
+  uint64_t acc_off;       // float offset of this job's accumulators
+  uint64_t out_off;       // float offset of this job's output (bins then dirs)
+};
+
+// Per-launch header in device memory (scratch: cleared before every launch).
+struct alignas(16) DLaunch {
+  uint32_t ray_counter;   // persistent-queue head
+  uint32_t error;         // OMG_E_OVERFLOW etc. set by kernels
+  uint32_t pad[2];
+};
+
+// Accumulator block of one job (all float, compensated pairs):
+//   bins_s[n_bins*nb], bins_c[n_bins*nb], dirs_s[n_bins*3], dirs_c[n_bins*3]
+inline uint64_t acc_floats(uint32_t n_bins, uint32_t nb) { return 2ull * n_bins * (nb + 3); }
+inline uint64_t out_floats(uint32_t n_bins, uint32_t nb) { return 1ull * n_bins * (nb + 3); }
+
+// Launch shapes of the tracer kernel (autotuned).
+struct LaunchShape {
+  uint32_t block_threads = 128;
+  uint32_t blocks_per_sm = 4;
+  uint32_t refill_min = 32;     // rays fetched per warp refill (multiple of 32 not required)
+};
+
+// ----------------------------------------------------------- kernel launchers
+// trace.cu
+cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
+                         const DScene* scenes, const DMat* job_mats, const DPanel* panels, float* acc,
+                         DLaunch* hdr, uint32_t* job_segments, const LaunchShape& shape, int n_sms,
+                         cudaStream_t s);
+cudaError_t launch_finalize(const DJob* jobs, uint32_t n_jobs, const float* acc, float* out, uint64_t total_out,
+                            cudaStream_t s);
+cudaError_t launch_raycast(const DScene* scene, const float* o, const float* d, uint32_t n, float* t,
+                           uint32_t* tri, DLaunch* hdr, cudaStream_t s);
+// reverb.cu: one echogram per job at out + out_off (bins part), n_bins x nb
+struct DReverbJob {
+  uint64_t bins_off;
+  uint32_t n_bins;
+  uint32_t nb;
+  float bin_dt;
+  uint32_t pad;
+};
+cudaError_t launch_reverb(const DReverbJob* rj, uint32_t n_jobs, uint32_t max_bins, const float* bins,
+                          omg_reverb* out, const uint32_t* job_segments, cudaStream_t s);
+// lbvh.cu: build the node array for prims already in device memory; reorders
+// prims into leaf order (prims_out) and returns the root ref.
+cudaError_t lbvh_build(const float4* prims_in, uint32_t n_prims, float4* prims_out, float4* nodes_out,
+                       int32_t* root_ref, void* scratch, size_t scratch_bytes, cudaStream_t s);
+size_t lbvh_scratch_bytes(uint32_t n_prims);
+
+// dome.cu
+struct DDomePanel {
+  int32_t axis;
+  float plane, lat0, lat1, z0, z1;
+  int32_t glass;
+  float t2[MAXB];         // trans^2 per band
+};
+struct DDomeLaunch {
+  const DScene* scene;
+  const float4* fan;      // n_fan directions (xyz, bin index in w)
+  uint32_t n_fan;
+  uint32_t n_rays;
+  uint32_t max_events;
+  uint32_t nb;
+  const DDomePanel* panels;   // glass first, then leaves
+  uint32_t n_glass;
+  uint32_t n_panels;
+  const float* eyes;          // n_eyes x 3
+  uint32_t n_eyes;
+  float* ray_tp;              // n_eyes x n_rays x nb
+  uint8_t* ray_escape;        // n_eyes x n_rays
+  float* ema;                 // n_eyes x 9 x nb (device state)
+  uint32_t* primed;           // n_eyes
+  float* raw;                 // n_eyes x 9 x nb
+  float* out_dir;             // n_eyes x 9 x 3
+  float* out_energy;          // n_eyes x 9 x nb
+  DLaunch* hdr;
+  uint32_t* events;           // escape events + through calls (2 counters)
+};
+cudaError_t launch_dome(const DDomeLaunch& L, cudaStream_t s);
+cudaError_t build_dome_fan(float4* fan, uint32_t n_fan, cudaStream_t s);
+
+}  // namespace omg

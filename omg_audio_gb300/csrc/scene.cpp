@@ -1,0 +1,384 @@
+// Host-side scene preparation: mesh builder with vertex dedup, tessellation of
+// oversized triangles, the reference's binned-SAH BVH, and flattening into the
+// device layout (child-box BVH2, 48-byte primitives, per-triangle normals).
+//
+// Compiled with -ffp-contract=off: every f32 result here (midpoints, edges,
+// boxes, normals) rounds exactly as the reference's Rust code does, so the
+// SAH tree and the primitive list are bit-identical to mesh.rs's.
+#include "scene.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+namespace omg {
+
+// ------------------------------------------------------------ mesh builder
+// mesh.rs:70-165
+uint32_t MeshBuilder::material(const omg_material& m) {
+  materials.push_back(m);
+  return (uint32_t)(materials.size() - 1);
+}
+
+uint32_t MeshBuilder::begin_surface() {
+  next_surface++;
+  return (uint32_t)(uint16_t)(next_surface - 1);
+}
+
+uint32_t MeshBuilder::vertex(const float p[3]) {
+  // mesh.rs:108-114: quantise to 0.1 mm, f32 product, round half away from zero
+  auto q = [](float v) { return (int64_t)std::round(v * 1e4f); };
+  Key k{q(p[0]), q(p[1]), q(p[2])};
+  auto it = lookup.find(k);
+  if (it != lookup.end()) return it->second;
+  uint32_t id = (uint32_t)(positions.size() / 3);
+  positions.push_back(p[0]);
+  positions.push_back(p[1]);
+  positions.push_back(p[2]);
+  lookup.emplace(k, id);
+  return id;
+}
+
+void MeshBuilder::tri(const float a[3], const float b[3], const float c[3], uint32_t m) {
+  uint32_t ia = vertex(a), ib = vertex(b), ic = vertex(c);
+  indices.push_back(ia);
+  indices.push_back(ib);
+  indices.push_back(ic);
+  tri_material.push_back((uint16_t)m);
+  tri_surface.push_back(next_surface > 0 ? (uint16_t)(next_surface - 1) : (uint16_t)0);
+  tri_max_edge.push_back(cur_max_edge > 0.0f ? cur_max_edge : kMaxPrimEdge);
+}
+
+void MeshBuilder::quad(const float a[3], const float b[3], const float c[3], const float d[3], uint32_t m) {
+  tri(a, b, c, m);
+  tri(a, c, d, m);
+}
+
+void MeshBuilder::abox(const float mn[3], const float mx[3], uint32_t m) {
+  const float ax = mn[0], ay = mn[1], az = mn[2], bx = mx[0], by = mx[1], bz = mx[2];
+  auto Q = [&](float p0, float p1, float p2, float q0, float q1, float q2, float r0, float r1, float r2, float s0,
+               float s1, float s2) {
+    const float A[3] = {p0, p1, p2}, B[3] = {q0, q1, q2}, Cc[3] = {r0, r1, r2}, D[3] = {s0, s1, s2};
+    quad(A, B, Cc, D, m);
+  };
+  Q(ax, ay, az, ax, by, az, ax, by, bz, ax, ay, bz);
+  Q(bx, ay, az, bx, ay, bz, bx, by, bz, bx, by, az);
+  Q(ax, ay, az, ax, ay, bz, bx, ay, bz, bx, ay, az);
+  Q(ax, by, az, bx, by, az, bx, by, bz, ax, by, bz);
+  Q(ax, ay, az, bx, ay, az, bx, by, az, ax, by, az);
+  Q(ax, ay, bz, ax, by, bz, bx, by, bz, bx, ay, bz);
+}
+
+// --------------------------------------------------------------- vec math
+namespace {
+struct F3 {
+  float x, y, z;
+};
+inline F3 add(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline F3 sub(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline F3 mul(F3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline float len(F3 a) { return std::sqrt(dot(a, a)); }
+inline F3 cross(F3 a, F3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline F3 vmin(F3 a, F3 b) { return {std::fmin(a.x, b.x), std::fmin(a.y, b.y), std::fmin(a.z, b.z)}; }
+inline F3 vmax(F3 a, F3 b) { return {std::fmax(a.x, b.x), std::fmax(a.y, b.y), std::fmax(a.z, b.z)}; }
+inline float get(F3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+inline F3 normalize(F3 a) {  // vec3.rs:19-26
+  float l = len(a);
+  if (l > 1e-12f) return mul(a, 1.0f / l);
+  return {1.0f, 0.0f, 0.0f};
+}
+
+struct Prim {
+  F3 a, e1, e2;
+  uint32_t tri;
+  uint16_t material;
+};
+
+struct RefNode {  // mesh.rs:52-58
+  F3 bmin, bmax;
+  uint32_t a, b;
+};
+
+constexpr uint32_t kLeafBit = 1u << 31;  // mesh.rs:17
+constexpr size_t kLeafSize = 4;          // mesh.rs:16
+
+inline void pbounds(const Prim& p, F3* lo, F3* hi) {
+  F3 a = p.a, b = add(p.a, p.e1), c = add(p.a, p.e2);
+  *lo = vmin(vmin(a, b), c);
+  *hi = vmax(vmax(a, b), c);
+}
+inline F3 pcentroid(const Prim& p) { return add(p.a, mul(add(p.e1, p.e2), 1.0f / 3.0f)); }
+inline float area(F3 lo, F3 hi) {
+  F3 e = vmax(sub(hi, lo), F3{0, 0, 0});
+  return 2.0f * (e.x * e.y + e.y * e.z + e.z * e.x);
+}
+inline uint64_t sat_u64(float v) {
+  if (!(v >= 0.0f)) return 0;
+  if (v >= 1.8446744073709552e19f) return UINT64_MAX;
+  return (uint64_t)v;
+}
+
+// mesh.rs:292-405
+uint32_t build_node(std::vector<RefNode>& nodes, std::vector<Prim>& prims, size_t start, size_t end) {
+  const int NBIN = 16;
+  const float FMAX = std::numeric_limits<float>::max();
+  F3 bmin{FMAX, FMAX, FMAX}, bmax{-FMAX, -FMAX, -FMAX}, cmin = bmin, cmax = bmax;
+  for (size_t i = start; i < end; i++) {
+    F3 lo, hi;
+    pbounds(prims[i], &lo, &hi);
+    bmin = vmin(bmin, lo);
+    bmax = vmax(bmax, hi);
+    F3 c = pcentroid(prims[i]);
+    cmin = vmin(cmin, c);
+    cmax = vmax(cmax, c);
+  }
+  uint32_t idx = (uint32_t)nodes.size();
+  nodes.push_back({bmin, bmax, 0, 0});
+  size_t count = end - start;
+  if (count <= kLeafSize) {
+    nodes[idx].a = kLeafBit | (uint32_t)start;
+    nodes[idx].b = (uint32_t)count;
+    return idx;
+  }
+  F3 cext = sub(cmax, cmin);
+  int axis = (cext.x >= cext.y && cext.x >= cext.z) ? 0 : (cext.y >= cext.z ? 1 : 2);
+  float cwidth = get(cext, axis);
+  size_t mid;
+  if (cwidth < 1e-6f) {
+    mid = start + count / 2;
+  } else {
+    const float cmin_a = get(cmin, axis);
+    auto bin_of = [&](const Prim& p) -> int {
+      float v = (get(pcentroid(p), axis) - cmin_a) / cwidth * (float)NBIN;
+      v = std::fmin(v, (float)NBIN - 1.0f);
+      return (int)sat_u64(v);
+    };
+    F3 blo[NBIN], bhi[NBIN];
+    uint32_t bn[NBIN];
+    for (int k = 0; k < NBIN; k++) {
+      blo[k] = {FMAX, FMAX, FMAX};
+      bhi[k] = {-FMAX, -FMAX, -FMAX};
+      bn[k] = 0;
+    }
+    for (size_t i = start; i < end; i++) {
+      int k = bin_of(prims[i]);
+      F3 lo, hi;
+      pbounds(prims[i], &lo, &hi);
+      blo[k] = vmin(blo[k], lo);
+      bhi[k] = vmax(bhi[k], hi);
+      bn[k] += 1;
+    }
+    float right_cost[NBIN] = {0};
+    F3 amin{FMAX, FMAX, FMAX}, amax{-FMAX, -FMAX, -FMAX};
+    uint32_t an = 0;
+    for (int k = NBIN - 1; k >= 1; k--) {
+      amin = vmin(amin, blo[k]);
+      amax = vmax(amax, bhi[k]);
+      an += bn[k];
+      right_cost[k - 1] = an > 0 ? area(amin, amax) * (float)an : 0.0f;
+    }
+    int best_cut = -1;
+    float best_cost = FMAX;
+    amin = {FMAX, FMAX, FMAX};
+    amax = {-FMAX, -FMAX, -FMAX};
+    an = 0;
+    for (int k = 0; k < NBIN - 1; k++) {
+      amin = vmin(amin, blo[k]);
+      amax = vmax(amax, bhi[k]);
+      an += bn[k];
+      if (an == 0 || an == (uint32_t)count) continue;
+      float cost = area(amin, amax) * (float)an + right_cost[k];
+      if (cost < best_cost) {
+        best_cost = cost;
+        best_cut = k;
+      }
+    }
+    if (best_cut < 0) {
+      mid = start + count / 2;
+    } else {
+      size_t i = 0, j = count;
+      while (i < j) {
+        if (bin_of(prims[start + i]) <= best_cut) {
+          i++;
+        } else {
+          j--;
+          std::swap(prims[start + i], prims[start + j]);
+        }
+      }
+      mid = start + i;
+    }
+  }
+  mid = std::min(std::max(mid, start + 1), end - 1);
+  uint32_t left = build_node(nodes, prims, start, mid);
+  uint32_t right = build_node(nodes, prims, mid, end);
+  nodes[idx].a = left;
+  nodes[idx].b = right;
+  return idx;
+}
+}  // namespace
+
+// mesh.rs:241-287 — tessellate (longest edge at its midpoint, LIFO work list).
+void tessellate(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
+                const float* tri_max_edge, std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri,
+                std::vector<uint16_t>& prim_mat) {
+  struct W {
+    F3 a, b, c;
+    uint32_t t;
+  };
+  auto vtx = [&](uint32_t i) { return F3{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}; };
+  std::vector<W> work;
+  work.reserve(n_tris);
+  for (uint32_t t = 0; t < n_tris; t++) work.push_back({vtx(idx[3 * t]), vtx(idx[3 * t + 1]), vtx(idx[3 * t + 2]), t});
+  prim_geo.clear();
+  prim_tri.clear();
+  prim_mat.clear();
+  while (!work.empty()) {
+    W w = work.back();
+    work.pop_back();
+    F3 a = w.a, b = w.b, c = w.c;
+    float lab = len(sub(b, a)), lbc = len(sub(c, b)), lca = len(sub(a, c));
+    float longest = std::fmax(std::fmax(lab, lbc), lca);
+    float lim = tri_max_edge ? tri_max_edge[w.t] : kMaxPrimEdge;
+    if (longest > lim) {
+      if (lab >= lbc && lab >= lca) {
+        F3 m = mul(add(a, b), 0.5f);
+        work.push_back({a, m, c, w.t});
+        work.push_back({m, b, c, w.t});
+      } else if (lbc >= lca) {
+        F3 m = mul(add(b, c), 0.5f);
+        work.push_back({a, b, m, w.t});
+        work.push_back({a, m, c, w.t});
+      } else {
+        F3 m = mul(add(c, a), 0.5f);
+        work.push_back({a, b, m, w.t});
+        work.push_back({m, b, c, w.t});
+      }
+      continue;
+    }
+    F3 e1 = sub(b, a), e2 = sub(c, a);
+    const float g[9] = {a.x, a.y, a.z, e1.x, e1.y, e1.z, e2.x, e2.y, e2.z};
+    prim_geo.insert(prim_geo.end(), g, g + 9);
+    prim_tri.push_back(w.t);
+    prim_mat.push_back(tri_mat[w.t]);
+  }
+}
+
+// Reference SAH tree over the tessellated prims (reorders them into leaf
+// order). ref_boxes/ref_ab receive the reference's node array.
+void build_sah(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, std::vector<uint16_t>& prim_mat,
+               std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab) {
+  size_t n = prim_tri.size();
+  std::vector<Prim> prims(n);
+  for (size_t i = 0; i < n; i++) {
+    const float* g = &prim_geo[9 * i];
+    prims[i] = {{g[0], g[1], g[2]}, {g[3], g[4], g[5]}, {g[6], g[7], g[8]}, prim_tri[i], prim_mat[i]};
+  }
+  std::vector<RefNode> nodes;
+  ref_boxes.clear();
+  ref_ab.clear();
+  if (n == 0) return;
+  nodes.reserve(2 * n / kLeafSize + 8);
+  build_node(nodes, prims, 0, n);
+  for (size_t i = 0; i < n; i++) {
+    const Prim& p = prims[i];
+    const float g[9] = {p.a.x, p.a.y, p.a.z, p.e1.x, p.e1.y, p.e1.z, p.e2.x, p.e2.y, p.e2.z};
+    std::memcpy(&prim_geo[9 * i], g, sizeof(g));
+    prim_tri[i] = p.tri;
+    prim_mat[i] = p.material;
+  }
+  ref_boxes.resize(nodes.size() * 6);
+  ref_ab.resize(nodes.size() * 2);
+  for (size_t i = 0; i < nodes.size(); i++) {
+    const RefNode& r = nodes[i];
+    float* o = &ref_boxes[6 * i];
+    o[0] = r.bmin.x; o[1] = r.bmin.y; o[2] = r.bmin.z;
+    o[3] = r.bmax.x; o[4] = r.bmax.y; o[5] = r.bmax.z;
+    ref_ab[2 * i] = r.a;
+    ref_ab[2 * i + 1] = r.b;
+  }
+}
+
+// Flatten the reference node array into the device BVH2: one device node per
+// internal reference node, holding both children's boxes; leaf children are
+// encoded in the parent's child ref.
+int32_t flatten_bvh2(const std::vector<float>& ref_boxes, const std::vector<uint32_t>& ref_ab,
+                     std::vector<float>& dev_nodes) {
+  size_t nref = ref_ab.size() / 2;
+  dev_nodes.clear();
+  if (nref == 0) return 0;
+  auto leaf_code = [&](uint32_t i) -> int32_t {
+    uint32_t start = ref_ab[2 * i] & ~kLeafBit, count = ref_ab[2 * i + 1];
+    return (int32_t)~((start << 3) | (count - 1));
+  };
+  if (ref_ab[0] & kLeafBit) return leaf_code(0);
+  std::vector<int32_t> dev_of(nref, -1);
+  int32_t next = 0;
+  // preorder numbering of internal nodes (root = 0)
+  std::vector<uint32_t> st{0};
+  std::vector<uint32_t> order;
+  while (!st.empty()) {
+    uint32_t i = st.back();
+    st.pop_back();
+    if (ref_ab[2 * i] & kLeafBit) continue;
+    dev_of[i] = next++;
+    order.push_back(i);
+    st.push_back(ref_ab[2 * i + 1]);
+    st.push_back(ref_ab[2 * i]);
+  }
+  dev_nodes.assign((size_t)next * 16, 0.0f);
+  for (uint32_t i : order) {
+    float* o = &dev_nodes[(size_t)dev_of[i] * 16];
+    uint32_t c0 = ref_ab[2 * i], c1 = ref_ab[2 * i + 1];
+    const float* b0 = &ref_boxes[6 * c0];
+    const float* b1 = &ref_boxes[6 * c1];
+    o[0] = b0[0]; o[1] = b0[1]; o[2] = b0[2]; o[3] = b0[3];
+    o[4] = b0[4]; o[5] = b0[5]; o[6] = b1[0]; o[7] = b1[1];
+    o[8] = b1[2]; o[9] = b1[3]; o[10] = b1[4]; o[11] = b1[5];
+    int32_t r0 = (ref_ab[2 * c0] & kLeafBit) ? leaf_code(c0) : dev_of[c0];
+    int32_t r1 = (ref_ab[2 * c1] & kLeafBit) ? leaf_code(c1) : dev_of[c1];
+    std::memcpy(&o[12], &r0, 4);
+    std::memcpy(&o[13], &r1, 4);
+  }
+  return 0;
+}
+
+// mesh.rs:458-461 per original triangle; .w carries the material id bits.
+void tri_normals(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
+                 std::vector<float>& out) {
+  out.resize((size_t)n_tris * 4);
+  for (uint32_t t = 0; t < n_tris; t++) {
+    F3 a{pos[3 * idx[3 * t]], pos[3 * idx[3 * t] + 1], pos[3 * idx[3 * t] + 2]};
+    F3 b{pos[3 * idx[3 * t + 1]], pos[3 * idx[3 * t + 1] + 1], pos[3 * idx[3 * t + 1] + 2]};
+    F3 c{pos[3 * idx[3 * t + 2]], pos[3 * idx[3 * t + 2] + 1], pos[3 * idx[3 * t + 2] + 2]};
+    F3 n = normalize(cross(sub(b, a), sub(c, a)));
+    out[4 * t] = n.x;
+    out[4 * t + 1] = n.y;
+    out[4 * t + 2] = n.z;
+    uint32_t m = tri_mat[t];
+    std::memcpy(&out[4 * t + 3], &m, 4);
+  }
+}
+
+// tracer.rs:148-182 precomputed per material with the job's band count.
+DMat make_dmat(const omg_material& m, uint32_t nb) {
+  DMat d;
+  std::memset(&d, 0, sizeof(d));
+  float p_t = 0.0f;
+  for (uint32_t b = 0; b < nb; b++) p_t = std::fmax(p_t, m.transmission[b] * m.transmission[b]);
+  float p = p_t > 1e-5f ? std::fmin(std::fmax(p_t, 0.02f), 0.5f) : 0.0f;
+  d.p = p;
+  d.scattering = m.scattering;
+  for (uint32_t b = 0; b < nb; b++) {
+    float t2 = m.transmission[b] * m.transmission[b];
+    d.wt[b] = p > 0.0f ? t2 / p : 0.0f;
+    float keep = std::fmax(1.0f - m.absorption[b] - t2, 0.0f);
+    d.wr[b] = keep / (1.0f - p);
+    d.absorption[b] = m.absorption[b];
+    d.t2[b] = t2;
+  }
+  return d;
+}
+
+}  // namespace omg

@@ -1,0 +1,57 @@
+// Host-side scene preparation (scene.cpp).
+#pragma once
+#include <cstdint>
+#include <unordered_map>
+#include <vector>
+
+#include "omg_internal.h"
+
+namespace omg {
+
+constexpr float kMaxPrimEdge = 4.0f;  // mesh.rs:41
+
+struct MeshBuilder {
+  struct Key {
+    int64_t x, y, z;
+    bool operator==(const Key& o) const { return x == o.x && y == o.y && z == o.z; }
+  };
+  struct KeyHash {
+    size_t operator()(const Key& k) const {
+      uint64_t h = (uint64_t)k.x * 0x9E3779B97F4A7C15ULL;
+      h ^= (uint64_t)k.y + 0x7F4A7C159E3779B9ULL + (h << 6) + (h >> 2);
+      h ^= (uint64_t)k.z + 0x94D049BB133111EBULL + (h << 6) + (h >> 2);
+      return (size_t)h;
+    }
+  };
+  std::vector<float> positions;
+  std::vector<uint32_t> indices;
+  std::vector<uint16_t> tri_material;
+  std::vector<omg_material> materials;
+  std::vector<uint16_t> tri_surface;
+  std::vector<float> tri_max_edge;
+  float cur_max_edge = 0.0f;
+  uint16_t next_surface = 0;
+  std::unordered_map<Key, uint32_t, KeyHash> lookup;
+
+  uint32_t material(const omg_material& m);
+  uint32_t begin_surface();
+  void coarse(float e) { cur_max_edge = e; }
+  uint32_t vertex(const float p[3]);
+  void tri(const float a[3], const float b[3], const float c[3], uint32_t m);
+  void quad(const float a[3], const float b[3], const float c[3], const float d[3], uint32_t m);
+  void abox(const float mn[3], const float mx[3], uint32_t m);
+};
+
+void tessellate(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
+                const float* tri_max_edge, std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri,
+                std::vector<uint16_t>& prim_mat);
+void build_sah(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, std::vector<uint16_t>& prim_mat,
+               std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab);
+// Returns the root ref; dev_nodes gets 16 floats per internal node.
+int32_t flatten_bvh2(const std::vector<float>& ref_boxes, const std::vector<uint32_t>& ref_ab,
+                     std::vector<float>& dev_nodes);
+void tri_normals(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
+                 std::vector<float>& out);
+DMat make_dmat(const omg_material& m, uint32_t nb);
+
+}  // namespace omg

@@ -1,0 +1,363 @@
+// Stochastic energy path tracer kernels for sm_103a.
+//
+// One persistent kernel traces every ray of every job of a launch: warps pull
+// rays from a global queue and refill idle lanes after each segment, so SIMD
+// lanes stay busy while rays end at different bounce counts. Each segment is
+// one iteration of the reference's bounce loop (tracer.rs:103-200): closest
+// hit, receiver test, then absorb / transmit / scatter.
+//
+// Arithmetic follows the reference's f32 operation order term by term and
+// this file is compiled with -fmad=false, so every f32 result rounds exactly
+// as the reference's (and the f32 oracle's) does. The only transcendental,
+// cos/sin of the Lambert azimuth, is evaluated in double and rounded once.
+#include "device_common.cuh"
+
+namespace omg {
+
+namespace {
+
+// Compensated accumulation: the atomic returns the old value, so the exact
+// rounding error of the add it performed is recovered with TwoSum (Knuth)
+// and accumulated in a second float. sum + comp carries ~2x the f32 precision.
+__device__ __forceinline__ void acc_add(float* s, float* c, float x) {
+  float old = atomicAdd(s, x);
+  float sum = old + x;
+  float bp = sum - old;
+  float err = (old - (sum - bp)) + (x - bp);
+  if (err != 0.0f) atomicAdd(c, err);
+}
+
+struct Hit {
+  float t;
+  float nx, ny, nz;
+  const DMat* m;
+};
+
+// scene.rs:39-88 — analytic shoebox.
+__device__ __forceinline__ bool box_hit(const DJob& J, const DMat* __restrict__ job_mats, float px, float py,
+                                        float pz, float dx, float dy, float dz, Hit& h) {
+  if (!(px > 0.0f && px < J.box[0] && py > 0.0f && py < J.box[1] && pz > 0.0f && pz < J.box[2])) return false;
+  float bt = FLT_MAX;
+  int bw = 0;
+  const float p[3] = {px, py, pz}, d[3] = {dx, dy, dz};
+#pragma unroll
+  for (int axis = 0; axis < 3; axis++) {
+    float di = d[axis];
+    if (di > 1e-9f) {
+      float t = (J.box[axis] - p[axis]) / di;
+      if (t < bt) { bt = t; bw = 2 * axis + 1; }
+    } else if (di < -1e-9f) {
+      float t = -p[axis] / di;
+      if (t < bt) { bt = t; bw = 2 * axis; }
+    }
+  }
+  if (!isfinite(bt) || bt <= 0.0f) return false;
+  h.t = bt;
+  h.nx = h.ny = h.nz = 0.0f;
+  float sgn = (bw % 2 == 0) ? 1.0f : -1.0f;
+  int ax = bw / 2;
+  if (ax == 0) h.nx = sgn; else if (ax == 1) h.ny = sgn; else h.nz = sgn;
+  h.m = job_mats + J.box_mat + bw;
+  return true;
+}
+
+// scene.rs:94-137 — panel slab ENTRY test, nearest of base and panels.
+__device__ __forceinline__ bool panels_hit(const DJob& J, const DPanel* __restrict__ panels,
+                                           const DMat* __restrict__ job_mats, float px, float py, float pz, float dx,
+                                           float dy, float dz, bool have, Hit& h) {
+  const float p[3] = {px, py, pz}, d[3] = {dx, dy, dz};
+  for (uint32_t i = 0; i < J.n_panels; i++) {
+    const DPanel& pn = panels[J.panel_off + i];
+    float t0 = 0.0f, t1 = FLT_MAX;
+    int axis = 3;
+    bool miss = false;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      if (miss) break;
+      float da = d[a], pa = p[a], lo = pn.mn[a], hi = pn.mx[a];
+      if (fabsf(da) < 1e-9f) {
+        if (pa < lo || pa > hi) { t0 = FLT_MAX; miss = true; }
+      } else {
+        float ta = (lo - pa) / da, tb = (hi - pa) / da;
+        if (ta > tb) { float tmp = ta; ta = tb; tb = tmp; }
+        if (ta > t0) { t0 = ta; axis = a; }
+        t1 = fminf(t1, tb);
+        if (t0 > t1) { t0 = FLT_MAX; miss = true; }
+      }
+    }
+    if (t0 > 1e-4f && t0 < FLT_MAX && axis < 3 && (!have || t0 < h.t)) {
+      h.t = t0;
+      h.nx = h.ny = h.nz = 0.0f;
+      float s = d[axis] > 0.0f ? -1.0f : 1.0f;
+      if (axis == 0) h.nx = s; else if (axis == 1) h.ny = s; else h.nz = s;
+      h.m = job_mats + pn.mat;
+      have = true;
+    }
+  }
+  return have;
+}
+
+__device__ __forceinline__ uint32_t find_job(const DJob* __restrict__ jobs, uint32_t n_jobs, uint32_t r) {
+  uint32_t lo = 0, hi = n_jobs;   // last job with ray_base <= r
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&jobs[mid].ray_base) <= r) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+template <int NB>
+__global__ void __launch_bounds__(256) trace_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
+                                                    uint32_t total_rays, const DScene* __restrict__ scenes,
+                                                    const DMat* __restrict__ job_mats,
+                                                    const DPanel* __restrict__ panels, float* __restrict__ acc,
+                                                    DLaunch* __restrict__ hdr, uint32_t* __restrict__ job_segments,
+                                                    uint32_t refill_min) {
+  const unsigned FULL = 0xffffffffu;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  bool active = false;
+  bool exhausted = false;
+  uint32_t ji = 0;
+  float px = 0, py = 0, pz = 0, dx = 0, dy = 0, dz = 0, dist = 0;
+  float e[NB];
+#pragma unroll
+  for (int b = 0; b < NB; b++) e[b] = 0.0f;
+  Pcg rng;
+  rng.s = 0;
+  uint32_t bounce = 0, segs = 0;
+
+  while (true) {
+    // ---- refill idle lanes from the global ray queue (warp-aggregated)
+    const unsigned idle = __ballot_sync(FULL, !active);
+    if (!exhausted && idle != 0u && (__popc(idle) >= (int)refill_min || idle == FULL)) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(&hdr->ray_counter, (uint32_t)__popc(idle));
+      base = __shfl_sync(FULL, base, 0);
+      if (base >= total_rays) exhausted = true;
+      if (!active) {
+        const uint32_t r = base + (uint32_t)__popc(idle & lt_mask);
+        if (r < total_rays) {
+          ji = find_job(jobs, n_jobs, r);
+          const DJob& J = jobs[ji];
+          rng.init(J.seed, r - J.ray_base);
+          unit_sphere(rng, dx, dy, dz);
+          px = J.src[0]; py = J.src[1]; pz = J.src[2];
+#pragma unroll
+          for (int b = 0; b < NB; b++) e[b] = J.e0[b];
+          dist = 0.0f;
+          bounce = 0;
+          segs = 0;
+          active = true;
+        }
+      }
+    }
+    if (__ballot_sync(FULL, active) == 0u) {
+      if (exhausted) break;
+      continue;
+    }
+    if (!active) continue;
+
+    // ---- one segment of the bounce loop (tracer.rs:103-200)
+    const DJob& J = jobs[ji];
+    const uint32_t nb = J.nb;
+    Hit h;
+    h.t = FLT_MAX;
+    h.m = nullptr;
+    bool have;
+    if (J.geom == OMG_GEOM_BOX) {
+      have = box_hit(J, job_mats, px, py, pz, dx, dy, dz, h);
+    } else {
+      const DScene S = scenes[J.scene];
+      int prim = 0;
+      float t;
+      have = mesh_closest(S, px, py, pz, dx, dy, dz, t, prim, &hdr->error);
+      if (have) {
+        const float4 p0 = __ldg(S.prims + 3 * prim + 0);
+        const float4 p1 = __ldg(S.prims + 3 * prim + 1);
+        const uint32_t tri = __float_as_uint(p1.w);
+        const float4 nn = __ldg(S.normals + tri);
+        float nx = nn.x, ny = nn.y, nz = nn.z;
+        if (nx * dx + ny * dy + nz * dz > 0.0f) { nx = nx * -1.0f; ny = ny * -1.0f; nz = nz * -1.0f; }
+        h.t = t;
+        h.nx = nx; h.ny = ny; h.nz = nz;
+        h.m = S.mats + __float_as_uint(p0.w);
+      }
+    }
+    if (J.n_panels) have = panels_hit(J, panels, job_mats, px, py, pz, dx, dy, dz, have, h);
+    segs++;
+    const float t_hit = have ? h.t : FLT_MAX;
+
+    // receiver sphere crossing along this segment (tracer.rs:110-128)
+    {
+      const float tlx = J.lis[0] - px, tly = J.lis[1] - py, tlz = J.lis[2] - pz;
+      const float s = tlx * dx + tly * dy + tlz * dz;
+      if (s > 0.0f && s < t_hit) {
+        const float cx = px + dx * s, cy = py + dy * s, cz = pz + dz * s;
+        const float ddx = cx - J.lis[0], ddy = cy - J.lis[1], ddz = cz - J.lis[2];
+        if (sqrtf(ddx * ddx + ddy * ddy + ddz * ddz) < J.rr) {
+          const float arrival = (dist + s) / J.c;
+          const float q = arrival / J.bin_dt;
+          if (q < (float)J.n_bins) {          // (q as usize) < NBINS, q >= 0
+            const uint32_t bin = (uint32_t)q;
+            float* A = acc + J.acc_off;
+            const uint32_t nbb = J.n_bins * nb;
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+              if ((uint32_t)b < nb) acc_add(A + bin * nb + b, A + nbb + bin * nb + b, e[b]);
+            float em = e[0];
+#pragma unroll
+            for (int b = 1; b < NB; b++)
+              if ((uint32_t)b == J.dir_band) em = e[b];
+            float* D = A + 2 * nbb;
+            const uint32_t nd = J.n_bins * 3;
+            acc_add(D + bin * 3 + 0, D + nd + bin * 3 + 0, -(dx * em));
+            acc_add(D + bin * 3 + 1, D + nd + bin * 3 + 1, -(dy * em));
+            acc_add(D + bin * 3 + 2, D + nd + bin * 3 + 2, -(dz * em));
+          }
+        }
+      }
+    }
+
+    bool done = !have;
+    if (!done) {
+      px = px + dx * t_hit;
+      py = py + dy * t_hit;
+      pz = pz + dz * t_hit;
+      dist = dist + t_hit;
+      if (dist / J.c > J.max_time) done = true;
+    }
+    if (!done) {
+      const DMat& M = *h.m;
+      const float p = M.p;
+      bool alive = false;
+      if (p > 0.0f && rng.f32() < p) {
+        // through-the-wall branch (tracer.rs:160-173)
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+          if ((uint32_t)b < nb) {
+            e[b] = e[b] * M.wt[b];
+            if (e[b] > J.floor_e) alive = true;
+          }
+        if (!alive) {
+          done = true;
+        } else {
+          const float step = 2.0f * J.wall_eps;
+          px = px + dx * step;
+          py = py + dy * step;
+          pz = pz + dz * step;
+        }
+      } else {
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+          if ((uint32_t)b < nb) {
+            e[b] = e[b] * M.wr[b];
+            if (e[b] > J.floor_e) alive = true;
+          }
+        if (!alive) {
+          done = true;
+        } else {
+          const float nx = h.nx, ny = h.ny, nz = h.nz;
+          if (rng.f32() < M.scattering) {
+            float ux, uy, uz;
+            unit_sphere(rng, ux, uy, uz);
+            float ax = nx + ux, ay = ny + uy, az = nz + uz;
+            normalize3(ax, ay, az);
+            if (ax * nx + ay * ny + az * nz < 1e-3f) { ax = nx; ay = ny; az = nz; }
+            dx = ax; dy = ay; dz = az;
+          } else {
+            const float k = 2.0f * (dx * nx + dy * ny + dz * nz);
+            dx = dx - nx * k;
+            dy = dy - ny * k;
+            dz = dz - nz * k;
+          }
+          px = px + nx * J.wall_eps;
+          py = py + ny * J.wall_eps;
+          pz = pz + nz * J.wall_eps;
+        }
+      }
+    }
+    bounce++;
+    if (!done && bounce >= J.max_bounces) done = true;
+    if (done) {
+      atomicAdd(job_segments + ji, segs);
+      active = false;
+    }
+  }
+}
+
+// out = sum + comp per float, bins then dirs, per job.
+__global__ void finalize_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs, const float* __restrict__ acc,
+                                float* __restrict__ out) {
+  const uint32_t j = blockIdx.y;
+  if (j >= n_jobs) return;
+  const DJob& J = jobs[j];
+  const uint32_t nbb = J.n_bins * J.nb, nd = J.n_bins * 3;
+  const float* A = acc + J.acc_off;
+  float* O = out + J.out_off;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nbb + nd; i += gridDim.x * blockDim.x) {
+    float v;
+    if (i < nbb) v = A[i] + A[nbb + i];
+    else v = A[2 * nbb + (i - nbb)] + A[2 * nbb + nd + (i - nbb)];
+    O[i] = v;
+  }
+}
+
+__global__ void raycast_kernel(const DScene* __restrict__ scene, const float* __restrict__ o,
+                               const float* __restrict__ d, uint32_t n, float* __restrict__ t_out,
+                               uint32_t* __restrict__ tri_out, DLaunch* hdr) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const DScene S = *scene;
+  float t;
+  int prim = 0;
+  bool have = mesh_closest(S, o[3 * i], o[3 * i + 1], o[3 * i + 2], d[3 * i], d[3 * i + 1], d[3 * i + 2], t, prim,
+                           &hdr->error);
+  if (have) {
+    t_out[i] = t;
+    tri_out[i] = __float_as_uint(__ldg(S.prims + 3 * prim + 1).w);
+  } else {
+    t_out[i] = -1.0f;
+    tri_out[i] = 0xFFFFFFFFu;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
+                         const DScene* scenes, const DMat* job_mats, const DPanel* panels, float* acc, DLaunch* hdr,
+                         uint32_t* job_segments, const LaunchShape& shape, int n_sms, cudaStream_t s) {
+  if (n_jobs == 0 || total_rays == 0) return cudaSuccess;
+  uint32_t threads = shape.block_threads;
+  uint64_t want = (uint64_t)n_sms * shape.blocks_per_sm;
+  uint64_t need = ((uint64_t)total_rays + threads - 1) / threads;
+  uint32_t blocks = (uint32_t)(want < need ? want : need);
+  if (blocks == 0) blocks = 1;
+  uint32_t refill = shape.refill_min == 0 ? 1 : (shape.refill_min > 32 ? 32 : shape.refill_min);
+  if (max_nb <= 3) {
+    trace_kernel<3><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, acc, hdr,
+                                               job_segments, refill);
+  } else {
+    trace_kernel<8><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, acc, hdr,
+                                               job_segments, refill);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const DJob* jobs, uint32_t n_jobs, const float* acc, float* out, uint64_t total_out,
+                            cudaStream_t s) {
+  if (n_jobs == 0) return cudaSuccess;
+  (void)total_out;
+  dim3 grid(8, n_jobs);
+  finalize_kernel<<<grid, 256, 0, s>>>(jobs, n_jobs, acc, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_raycast(const DScene* scene, const float* o, const float* d, uint32_t n, float* t, uint32_t* tri,
+                           DLaunch* hdr, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  raycast_kernel<<<(n + 127) / 128, 128, 0, s>>>(scene, o, d, n, t, tri, hdr);
+  return cudaGetLastError();
+}
+
+}  // namespace omg
