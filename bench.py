@@ -10,6 +10,9 @@ so L2 is flushed (a 256 MB write) before every timed step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+The near-tie rule (tie_mode 1: lowest surface id among hits within 1e-6
+relative t) is on, so the f32 result matches the FP64 oracle.
+
 Rank 0 prints one JSON line. `--impl reference` times the CPU restatement of
 the reference tracer (the oracle port; the reference itself is Rust and has
 no toolchain here) on the host cores, on the same metric.
@@ -111,7 +114,7 @@ def cpu_sample(case, n_pairs, threads, n_rays=N_RAYS, ray_end=None):
     [0, n_pairs): segments, seconds and the traversal counters."""
     from oracle import oracle as O
     mesh = oracle_mesh(case)
-    P = O.params(**CFG)
+    P = O.params(tie_mode=1, **CFG)
     pan = [(mn, mx, O.Material.make(m.absorption, m.scattering, m.transmission)) for (mn, mx, m) in case.panels]
     seg = nodes = prims = hits = 0
     t0 = time.perf_counter()
@@ -182,15 +185,17 @@ def run_ours(args):
     from omg_audio_gb300 import _lib
 
     case = build_case()
-    ctx = Context(TraceConfig(device=local, timeout_ms=60000, **CFG))
-    stream = torch.cuda.current_stream()
+    ctx = Context(TraceConfig(device=local, timeout_ms=60000, tie_mode=1, **CFG))
+    # a dedicated stream: the library launches on it and the events are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     mb = MeshBuilder()
     case.recorder.replay(mb)
     bvh = _lib.BVH_LBVH if args.bvh == "lbvh" else _lib.BVH_SAH
     scene = ctx.upload_builder(mb, 3, bvh)
     jobs = [Job(src, lis, N_RAYS, seed=1000 + p, scene=scene, panel_offset=0, n_panels=len(case.panels))
-            for p, (src, lis) in enumerate(case.pairs)]
+            for p, (src, lis) in enumerate(case.pairs[:args.pairs])]
     batch = ctx.batch(jobs, case.panels)
     tune = batch.autotune(reps=1) if args.autotune else None
     dome = DomeProbe(ctx, scene, case.glass, n_fan=DOME_RAYS)
@@ -210,6 +215,12 @@ def run_ours(args):
         step()
         dome.sample(case.listeners, n_rays=DOME_RAYS)
     torch.cuda.synchronize()
+    if args.profile:
+        # small case for a profiler: the launches only, nothing timed or printed
+        for _ in range(args.steps):
+            step()
+        torch.cuda.synchronize()
+        return 0
     if ws > 1:
         dist.barrier()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
@@ -299,7 +310,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--bvh", choices=["sah", "lbvh"], default="sah")
-    ap.add_argument("--ref-pairs", type=int, default=4)
+    ap.add_argument("--ref-pairs", type=int, default=64)
+    ap.add_argument("--pairs", type=int, default=N_PAIRS, help="pairs traced per step (default: the workload's 64)")
+    ap.add_argument("--profile", action="store_true", help="launches only (a small case under a profiler)")
     ap.add_argument("--autotune", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -70,6 +70,10 @@ typedef struct omg_params {
     uint32_t dir_band;
     int32_t device;              /* CUDA device ordinal */
     uint32_t timeout_ms;         /* bound on every wait (0 = 10000) */
+    uint32_t tie_mode;           /* closest hit among near-ties (relative t-gap < 1e-6):
+                                    0 = the first one found in the reference's traversal
+                                    order (mesh.rs:505, strict <); 1 = the lowest authored
+                                    surface id, then triangle id (precision-independent) */
 } omg_params;
 
 /* LateBackend::trace job (late.rs:28-40): analytic shoebox [0,size]^3, walls in

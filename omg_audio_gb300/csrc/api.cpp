@@ -41,16 +41,13 @@ bool valid_material(const omg_material& m, uint32_t nb) {
 
 bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
 
+// The device scene table has a fixed capacity for the context's lifetime:
+// captured graphs hold its address, so it is never reallocated.
 int32_t sync_scene_table(omg_ctx* ctx) {
-  uint32_t need = ctx->next_scene + 1;
-  if (need > ctx->scene_cap) {
-    uint32_t cap = std::max<uint32_t>(16, need * 2);
-    DevBuf<DScene> nt;
-    CK(nt.alloc(cap));
-    CK(cudaMemset(nt.p, 0, cap * sizeof(DScene)));
-    std::swap(ctx->d_scenes.p, nt.p);
-    std::swap(ctx->d_scenes.n, nt.n);
-    ctx->scene_cap = cap;
+  if (ctx->scene_cap == 0) {
+    CK(ctx->d_scenes.alloc(kMaxScenes));
+    CK(cudaMemset(ctx->d_scenes.p, 0, kMaxScenes * sizeof(DScene)));
+    ctx->scene_cap = kMaxScenes;
   }
   std::vector<DScene> table(ctx->scene_cap);
   std::memset(table.data(), 0, table.size() * sizeof(DScene));
@@ -234,7 +231,7 @@ int32_t record_launch(omg_ctx* ctx, BatchRec& B, cudaStream_t s, int parts = 3) 
     CK(cudaMemsetAsync(B.d_acc.p, 0, B.n_acc * sizeof(float), s));
     CK(cudaMemsetAsync(B.d_seg.p, 0, B.n_jobs * sizeof(uint32_t), s));
     CK(launch_trace(B.d_jobs.p, B.n_jobs, B.total_rays, B.max_nb, ctx->d_scenes.p, B.d_job_mats.p, B.d_panels.p,
-                    B.d_acc.p, B.d_hdr.p, B.d_seg.p, B.shape, ctx->n_sms, s));
+                    B.d_acc.p, B.d_hdr.p, B.d_seg.p, B.shape, ctx->n_sms, ctx->prm.tie_mode != 0, s));
   }
   if (parts & 2) {
     CK(launch_finalize(B.d_jobs.p, B.n_jobs, B.d_acc.p, B.d_out.p, B.n_out, s));
@@ -404,6 +401,7 @@ void omg_params_default(omg_params* p) {
   p->dir_band = 1;
   p->device = 0;
   p->timeout_ms = 10000;
+  p->tie_mode = 0;
 }
 
 int32_t omg_abi_version(void) { return OMG_ABI_VERSION; }

@@ -120,7 +120,9 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
       }
     }
   }
-  uint32_t id = ctx->next_scene++;
+  uint32_t id = 1;  // lowest free slot of the fixed table
+  while (id < kMaxScenes && ctx->scenes.count(id)) id++;
+  if (id >= kMaxScenes) return OMG_E_INVALID;
   ctx->scenes[id] = std::move(S);
   int32_t rc = sync_scene_table(ctx);
   if (rc) {
@@ -243,7 +245,8 @@ int32_t omg_raycast(omg_ctx* ctx, uint32_t id, const float* o, const float* d, u
   CK(cudaMemsetAsync(ctx->q_hdr.p, 0, sizeof(DLaunch), s));
   CK(cudaMemcpyAsync(ctx->q_o.p, o, 12ull * n, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(ctx->q_d.p, d, 12ull * n, cudaMemcpyHostToDevice, s));
-  CK(launch_raycast(ctx->d_scenes.p + id, ctx->q_o.p, ctx->q_d.p, n, ctx->q_t.p, ctx->q_tri.p, ctx->q_hdr.p, s));
+  CK(launch_raycast(ctx->d_scenes.p + id, ctx->q_o.p, ctx->q_d.p, n, ctx->q_t.p, ctx->q_tri.p, ctx->q_hdr.p,
+                    ctx->prm.tie_mode != 0, s));
   CK(cudaMemcpyAsync(t, ctx->q_t.p, 4ull * n, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(tri, ctx->q_tri.p, 4ull * n, cudaMemcpyDeviceToHost, s));
   DLaunch h;

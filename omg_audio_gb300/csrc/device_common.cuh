@@ -113,14 +113,26 @@ __device__ __forceinline__ bool ray_tri(const float4& p0, const float4& p1, cons
 // mesh.rs:484-541 — ordered closest-hit traversal over the child-box BVH2.
 // Visit order, culling (t_enter >= best) and the strict `<` on hits are the
 // reference's, so over the reference tree the same triangle wins every tie.
-__device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy, float oz, float dx, float dy, float dz,
-                             float& t_best, int& prim_best, uint32_t* err) {
+//
+// TIE = true resolves near-ties deterministically instead: a hit within a
+// relative t-gap of 1e-6 of the best replaces it only when its authored
+// surface id (then its original triangle id) is lower. Coplanar copies of a
+// shared wall, authored once per room with different materials, then resolve
+// the same way at any precision (the rule segment_hits applies to crossings,
+// mesh.rs:583-602). Nodes are culled only beyond best * (1 + 1e-6).
+constexpr float kTieRel = 1e-6f;
+
+template <bool TIE>
+__device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy, float oz, float dx, float dy,
+                                             float dz, float& t_best, int& prim_best, uint32_t* err) {
   if (S.n_prims == 0) return false;
   const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
   const float4* __restrict__ nodes = S.nodes;
   const float4* __restrict__ prims = S.prims;
   bool have = false;
   t_best = FLT_MAX;
+  float t_cull = FLT_MAX;            // TIE: best * (1 + 1e-6); else best
+  uint32_t s_best = 0, tri_best = 0;
   int stack_ref[STACK_DEPTH];
   float stack_t[STACK_DEPTH];
   int sp = 0;
@@ -131,7 +143,7 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
       const float4 n1 = __ldg(nodes + 4 * cur + 1);
       const float4 n2 = __ldg(nodes + 4 * cur + 2);
       const float4 n3 = __ldg(nodes + 4 * cur + 3);
-      const float tmax = have ? t_best : FLT_MAX;
+      const float tmax = have ? t_cull : FLT_MAX;
       float ta, tb;
       const bool h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ox, oy, oz, ix, iy, iz, tmax, ta);
       const bool h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ox, oy, oz, ix, iy, iz, tmax, tb);
@@ -148,11 +160,11 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
         } else {
           atomicOr(err, 1u);
         }
-        if (!(have && nt >= t_best)) { cur = nr; continue; }
+        if (!(have && (TIE ? nt > t_cull : nt >= t_best))) { cur = nr; continue; }
       } else if (h0) {
-        if (!(have && ta >= t_best)) { cur = c0; continue; }
+        if (!(have && (TIE ? ta > t_cull : ta >= t_best))) { cur = c0; continue; }
       } else if (h1) {
-        if (!(have && tb >= t_best)) { cur = c1; continue; }
+        if (!(have && (TIE ? tb > t_cull : tb >= t_best))) { cur = c1; continue; }
       }
     } else {
       const uint32_t code = ~(uint32_t)cur;
@@ -163,10 +175,28 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
         const float4 p2 = __ldg(prims + 3 * i + 2);
         float t;
         if (ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) {
-          if (!have || t < t_best) {
+          bool take;
+          if (!TIE) {
+            take = !have || t < t_best;
+          } else if (!have || t < t_best * (1.0f - kTieRel)) {
+            take = true;
+          } else if (t <= t_cull) {
+            const uint32_t s = __float_as_uint(p2.w), tr = __float_as_uint(p1.w);
+            take = s < s_best || (s == s_best && tr < tri_best);
+          } else {
+            take = false;
+          }
+          if (take) {
             have = true;
             t_best = t;
             prim_best = (int)i;
+            if (TIE) {
+              t_cull = t * (1.0f + kTieRel);
+              s_best = __float_as_uint(p2.w);
+              tri_best = __float_as_uint(p1.w);
+            } else {
+              t_cull = t;
+            }
           }
         }
       }
@@ -174,7 +204,7 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
     bool found = false;
     while (sp > 0) {
       sp--;
-      if (have && stack_t[sp] >= t_best) continue;
+      if (have && (TIE ? stack_t[sp] > t_cull : stack_t[sp] >= t_best)) continue;
       cur = stack_ref[sp];
       found = true;
       break;

@@ -42,7 +42,7 @@ __device__ bool trace_escape(const DScene& S, const DDomeLaunch& L, float px, fl
     events++;
     float tm = FLT_MAX;
     int prim = 0;
-    const bool mh = mesh_closest(S, px, py, pz, dx, dy, dz, tm, prim, &L.hdr->error);
+    const bool mh = mesh_closest<false>(S, px, py, pz, dx, dy, dz, tm, prim, &L.hdr->error);
     const float t_mesh = mh ? tm : FLT_MAX;
     float t_pan = t_mesh;
     int pan = -1;

@@ -194,11 +194,16 @@ __global__ void gather_kernel(const float4* __restrict__ in, const unsigned long
 __global__ void refit_kernel(const float4* __restrict__ prims, int n, const int* __restrict__ left,
                              const int* __restrict__ right, const int* __restrict__ parent_int,
                              const int* __restrict__ parent_leaf, float* __restrict__ boxes,
-                             unsigned int* __restrict__ flags) {
+                             unsigned int* __restrict__ flags, unsigned int* __restrict__ err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int p = parent_leaf[i];
-  while (p >= 0) {
+  // keys are 62 bits wide, so no path to the root is longer than 64 nodes
+  for (int guard = 0; p >= 0; guard++) {
+    if (guard >= 128) {
+      atomicOr(err, 1u);
+      return;
+    }
     __threadfence();
     if (atomicAdd(&flags[p], 1u) == 0u) return;
     __threadfence();
@@ -303,7 +308,7 @@ cudaError_t lbvh_build(const float4* prims_in, uint32_t n, float4* prims_out, fl
   p += (size_t)n * 24;
   unsigned int* flags = (unsigned int*)p;
 
-  const uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+  const uint32_t init[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u};  // bounds + error word
   cudaError_t e = cudaMemcpyAsync(cb, init, sizeof(init), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return e;
   bounds_kernel<<<std::min<uint32_t>((n + 255) / 256, 1024), 256, 0, s>>>(prims_in, n, cb);
@@ -325,7 +330,8 @@ cudaError_t lbvh_build(const float4* prims_in, uint32_t n, float4* prims_out, fl
                                                          range_hi);
   e = cudaMemsetAsync(flags, 0, (size_t)n * 4, s);
   if (e != cudaSuccess) return e;
-  refit_kernel<<<(n + 255) / 256, 256, 0, s>>>(prims_out, (int)n, left, right, parent_int, parent_leaf, boxes, flags);
+  refit_kernel<<<(n + 255) / 256, 256, 0, s>>>(prims_out, (int)n, left, right, parent_int, parent_leaf, boxes, flags,
+                                                 cb + 6);
   write_nodes_kernel<<<(n - 1 + 255) / 256, 256, 0, s>>>(prims_out, (int)n, left, right, range_lo, range_hi, boxes,
                                                           nodes_out);
   // root: internal node 0, or a leaf when the whole tree fits one leaf
@@ -334,7 +340,12 @@ cudaError_t lbvh_build(const float4* prims_in, uint32_t n, float4* prims_out, fl
   if (e != cudaSuccess) return e;
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return cudaStreamSynchronize(s);
+  uint32_t herr = 0;
+  e = cudaMemcpyAsync(&herr, cb + 6, 4, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  return herr ? cudaErrorInvalidValue : cudaSuccess;
 }
 
 }  // namespace omg

@@ -113,12 +113,12 @@ struct LaunchShape {
 // trace.cu
 cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
                          const DScene* scenes, const DMat* job_mats, const DPanel* panels, float* acc,
-                         DLaunch* hdr, uint32_t* job_segments, const LaunchShape& shape, int n_sms,
+                         DLaunch* hdr, uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie,
                          cudaStream_t s);
 cudaError_t launch_finalize(const DJob* jobs, uint32_t n_jobs, const float* acc, float* out, uint64_t total_out,
                             cudaStream_t s);
 cudaError_t launch_raycast(const DScene* scene, const float* o, const float* d, uint32_t n, float* t,
-                           uint32_t* tri, DLaunch* hdr, cudaStream_t s);
+                           uint32_t* tri, DLaunch* hdr, bool tie, cudaStream_t s);
 // reverb.cu: one echogram per job at out + out_off (bins part), n_bins x nb
 struct DReverbJob {
   uint64_t bins_off;

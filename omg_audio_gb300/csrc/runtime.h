@@ -152,6 +152,7 @@ int32_t fail(omg_ctx* ctx, cudaError_t e, const char* where);
 uint32_t timeout_of(const omg_ctx* ctx);
 int32_t wait_event(omg_ctx* ctx, cudaEvent_t ev, uint32_t timeout_ms);
 int32_t sync_scene_table(omg_ctx* ctx);
+constexpr uint32_t kMaxScenes = 4096;     // scene ids 1 .. kMaxScenes-1
 bool valid_material(const omg_material& m, uint32_t nb);
 bool finite3(const float* v);
 

@@ -106,7 +106,7 @@ __device__ __forceinline__ uint32_t find_job(const DJob* __restrict__ jobs, uint
   return lo;
 }
 
-template <int NB>
+template <int NB, bool TIE>
 __global__ void __launch_bounds__(256) trace_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
                                                     uint32_t total_rays, const DScene* __restrict__ scenes,
                                                     const DMat* __restrict__ job_mats,
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const DJob* __restrict__ job
       const DScene S = scenes[J.scene];
       int prim = 0;
       float t;
-      have = mesh_closest(S, px, py, pz, dx, dy, dz, t, prim, &hdr->error);
+      have = mesh_closest<TIE>(S, px, py, pz, dx, dy, dz, t, prim, &hdr->error);
       if (have) {
         const float4 p0 = __ldg(S.prims + 3 * prim + 0);
         const float4 p1 = __ldg(S.prims + 3 * prim + 1);
@@ -303,6 +303,7 @@ __global__ void finalize_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs, 
   }
 }
 
+template <bool TIE>
 __global__ void raycast_kernel(const DScene* __restrict__ scene, const float* __restrict__ o,
                                const float* __restrict__ d, uint32_t n, float* __restrict__ t_out,
                                uint32_t* __restrict__ tri_out, DLaunch* hdr) {
@@ -311,8 +312,8 @@ __global__ void raycast_kernel(const DScene* __restrict__ scene, const float* __
   const DScene S = *scene;
   float t;
   int prim = 0;
-  bool have = mesh_closest(S, o[3 * i], o[3 * i + 1], o[3 * i + 2], d[3 * i], d[3 * i + 1], d[3 * i + 2], t, prim,
-                           &hdr->error);
+  bool have = mesh_closest<TIE>(S, o[3 * i], o[3 * i + 1], o[3 * i + 2], d[3 * i], d[3 * i + 1], d[3 * i + 2], t,
+                                prim, &hdr->error);
   if (have) {
     t_out[i] = t;
     tri_out[i] = __float_as_uint(__ldg(S.prims + 3 * prim + 1).w);
@@ -326,7 +327,7 @@ __global__ void raycast_kernel(const DScene* __restrict__ scene, const float* __
 
 cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
                          const DScene* scenes, const DMat* job_mats, const DPanel* panels, float* acc, DLaunch* hdr,
-                         uint32_t* job_segments, const LaunchShape& shape, int n_sms, cudaStream_t s) {
+                         uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie, cudaStream_t s) {
   if (n_jobs == 0 || total_rays == 0) return cudaSuccess;
   uint32_t threads = shape.block_threads;
   uint64_t want = (uint64_t)n_sms * shape.blocks_per_sm;
@@ -334,13 +335,17 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
   uint32_t blocks = (uint32_t)(want < need ? want : need);
   if (blocks == 0) blocks = 1;
   uint32_t refill = shape.refill_min == 0 ? 1 : (shape.refill_min > 32 ? 32 : shape.refill_min);
+#define OMG_TRACE_LAUNCH(NB, TIE)                                                                        \
+  trace_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, acc, hdr, \
+                                                   job_segments, refill)
   if (max_nb <= 3) {
-    trace_kernel<3><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, acc, hdr,
-                                               job_segments, refill);
+    if (tie) OMG_TRACE_LAUNCH(3, true);
+    else OMG_TRACE_LAUNCH(3, false);
   } else {
-    trace_kernel<8><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, acc, hdr,
-                                               job_segments, refill);
+    if (tie) OMG_TRACE_LAUNCH(8, true);
+    else OMG_TRACE_LAUNCH(8, false);
   }
+#undef OMG_TRACE_LAUNCH
   return cudaGetLastError();
 }
 
@@ -354,9 +359,10 @@ cudaError_t launch_finalize(const DJob* jobs, uint32_t n_jobs, const float* acc,
 }
 
 cudaError_t launch_raycast(const DScene* scene, const float* o, const float* d, uint32_t n, float* t, uint32_t* tri,
-                           DLaunch* hdr, cudaStream_t s) {
+                           DLaunch* hdr, bool tie, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  raycast_kernel<<<(n + 127) / 128, 128, 0, s>>>(scene, o, d, n, t, tri, hdr);
+  if (tie) raycast_kernel<true><<<(n + 127) / 128, 128, 0, s>>>(scene, o, d, n, t, tri, hdr);
+  else raycast_kernel<false><<<(n + 127) / 128, 128, 0, s>>>(scene, o, d, n, t, tri, hdr);
   return cudaGetLastError();
 }
 

@@ -41,11 +41,12 @@ class TraceConfig:
     dir_band: int = 1
     device: int = 0
     timeout_ms: int = 20000
+    tie_mode: int = 0          # 0: reference first-found; 1: lowest surface id among near-ties
 
     def to_c(self) -> _lib.omg_params:
         p = _lib.omg_params()
         for k in ("n_bands", "n_bins", "bin_dt", "max_time", "max_bounces", "energy_floor", "receiver_radius",
-                  "wall_eps", "speed_of_sound", "dir_band", "device", "timeout_ms"):
+                  "wall_eps", "speed_of_sound", "dir_band", "device", "timeout_ms", "tie_mode"):
             setattr(p, k, getattr(self, k))
         return p
 

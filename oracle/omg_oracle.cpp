@@ -94,6 +94,17 @@ void run_trace(HitFn hitfn, const TraceParams& P, const float* src, const float*
   }
 }
 
+// A mesh whose raycast_hit applies the context's tie rule.
+template <class R>
+struct TieMesh {
+  const Mesh<R>* m;
+  bool tie;
+  bool raycast_hit(const V3<R>& p, const V3<R>& d, GeomHit<R>* h, TraversalStats* st = nullptr,
+                   uint32_t* tri = nullptr) const {
+    return m->raycast_hit(p, d, h, st, tri, tie);
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -174,7 +185,8 @@ int orc_mesh_export_bvh(void* hv, float* node_boxes /*n*6*/, uint32_t* node_ab /
   return 0;
 }
 
-// Closest hit per query (mesh.rs:484-541; brute != 0 scans every triangle).
+// Closest hit per query (mesh.rs:484-541). flags bit 0: scan every triangle;
+// bit 1: the near-tie rule (lowest surface id).
 // t = -1 and tri = 0xFFFFFFFF on a miss. stats: node reads, prim tests.
 int orc_mesh_raycast(void* hv, const float* o, const float* d, uint32_t n, int brute, double* t_out, uint32_t* tri_out,
                      uint64_t* stats) {
@@ -186,12 +198,12 @@ int orc_mesh_raycast(void* hv, const float* o, const float* d, uint32_t n, int b
     if (h->real == 0) {
       float tf; uint32_t tr;
       V3<float> oo = from_f<float>(o + 3 * i), dd = from_f<float>(d + 3 * i);
-      hit = brute ? h->mf.raycast_brute(oo, dd, &tf, &tr) : h->mf.raycast(oo, dd, &tf, &tr, &st);
+      hit = (brute & 1) ? h->mf.raycast_brute(oo, dd, &tf, &tr) : h->mf.raycast(oo, dd, &tf, &tr, &st, (brute & 2) != 0);
       if (hit) { t = tf; tri = tr; }
     } else {
       double td; uint32_t tr;
       V3<double> oo = from_f<double>(o + 3 * i), dd = from_f<double>(d + 3 * i);
-      hit = brute ? h->md.raycast_brute(oo, dd, &td, &tr) : h->md.raycast(oo, dd, &td, &tr, &st);
+      hit = (brute & 1) ? h->md.raycast_brute(oo, dd, &td, &tr) : h->md.raycast(oo, dd, &td, &tr, &st, (brute & 2) != 0);
       if (hit) { t = td; tri = tr; }
     }
     t_out[i] = t;
@@ -258,8 +270,9 @@ int orc_trace_mesh(int real, void* hv, const BoxPanelC* panels, uint32_t n_panel
     auto pn = panels_of<float>(panels, n_panels);
     const Mesh<float>& m = h->mf;
     auto fn = [&](const V3<float>& p, const V3<float>& d, GeomHit<float>* g, uint32_t* tri, TraversalStats* st) {
-      if (pn.empty()) return m.raycast_hit(p, d, g, st, tri);
-      return with_panels_hit<float>(m, pn, p, d, g, st);
+      TieMesh<float> tm{&m, P->tie_mode != 0};
+      if (pn.empty()) return tm.raycast_hit(p, d, g, st, tri);
+      return with_panels_hit<float>(tm, pn, p, d, g, st);
     };
     if (rng_kind & ACC64)
       run_trace<float, double>(fn, *P, src, lis, n_rays, energy, rng_kind & 0xF, seed, ray_begin, ray_end, n_threads, bins, dirs, stats);
@@ -269,8 +282,9 @@ int orc_trace_mesh(int real, void* hv, const BoxPanelC* panels, uint32_t n_panel
     auto pn = panels_of<double>(panels, n_panels);
     const Mesh<double>& m = h->md;
     auto fn = [&](const V3<double>& p, const V3<double>& d, GeomHit<double>* g, uint32_t* tri, TraversalStats* st) {
-      if (pn.empty()) return m.raycast_hit(p, d, g, st, tri);
-      return with_panels_hit<double>(m, pn, p, d, g, st);
+      TieMesh<double> tm{&m, P->tie_mode != 0};
+      if (pn.empty()) return tm.raycast_hit(p, d, g, st, tri);
+      return with_panels_hit<double>(tm, pn, p, d, g, st);
     };
     run_trace<double, double>(fn, *P, src, lis, n_rays, energy, rng_kind & 0xF, seed, ray_begin, ray_end, n_threads, bins, dirs, stats);
   }
@@ -399,4 +413,18 @@ void orc_xorshift_draws(uint64_t seed, uint32_t n, uint64_t* out) {
 }
 
 int orc_abi_version() { return 1; }
+}
+
+extern "C" {
+// dome.rs:121-258 into an oracle MeshBuilder; writes up to glass_cap panes.
+// Returns the pane count. wall_max_edge = 0 keeps the reference's default limit.
+uint32_t orc_world_build(void* mbv, const RoomC* rooms, uint32_t n_rooms, const DoorC* doors, uint32_t n_doors,
+                         float town0, float town1, float wall_max_edge, uint32_t nb, DomePanel* glass,
+                         uint32_t glass_cap) {
+  std::vector<RoomC> r(rooms, rooms + n_rooms);
+  std::vector<DoorC> d(doors, doors + n_doors);
+  auto g = build_world_mesh(*(MeshBuilder*)mbv, r, d, town0, town1, wall_max_edge, (int)nb);
+  for (size_t i = 0; i < g.size() && i < glass_cap; i++) glass[i] = g[i];
+  return (uint32_t)g.size();
+}
 }

@@ -487,12 +487,19 @@ struct Mesh {
   // mesh.rs:484-541 — ORDERED closest-hit traversal, 64-entry stack of
   // (node, t_enter), near child on top, strict `<` (first found wins ties).
   // Returns the ORIGINAL triangle id.
-  bool raycast(const V3<R>& o, const V3<R>& d, R* tout, uint32_t* triout, TraversalStats* st = nullptr) const {
+  //
+  // tie = true: a hit within a relative t-gap of 1e-6 of the best replaces it
+  // only with a lower authored surface id (then original triangle id), and
+  // nodes are culled only beyond best * (1 + 1e-6) — the precision-independent
+  // near-tie rule (the one segment_hits applies to crossings, mesh.rs:583-602).
+  bool raycast(const V3<R>& o, const V3<R>& d, R* tout, uint32_t* triout, TraversalStats* st = nullptr,
+               bool tie = false) const {
     if (nodes.empty()) return false;
     V3<R> inv_d(R(1) / d.x, R(1) / d.y, R(1) / d.z);
+    const R rel = R(1e-6f);
     bool have = false;
-    R bt = 0;
-    uint32_t btri = 0;
+    R bt = 0, bcull = 0;
+    uint32_t btri = 0, bsurf = 0;
     uint32_t sn[64];
     R stt[64];
     size_t sp = 1;
@@ -501,7 +508,7 @@ struct Mesh {
       sp--;
       uint32_t ni = sn[sp];
       R t_enter = stt[sp];
-      if (have && t_enter >= bt) continue;
+      if (have && (tie ? t_enter > bcull : t_enter >= bt)) continue;
       const BvhNode<R>& node = nodes[ni];
       if (st) st->node_reads++;
       if (node.a & LEAF_BIT) {
@@ -511,11 +518,28 @@ struct Mesh {
           if (st) st->prim_tests++;
           R t;
           if (ray_tri_packed(pt.a, pt.e1, pt.e2, o, d, &t)) {
-            if (!have || t < bt) { have = true; bt = t; btri = pt.tri; }
+            bool take;
+            if (!tie) {
+              take = !have || t < bt;
+            } else if (!have || t < bt * (R(1) - rel)) {
+              take = true;
+            } else if (t <= bcull) {
+              uint32_t s = tri_surface[pt.tri];
+              take = s < bsurf || (s == bsurf && pt.tri < btri);
+            } else {
+              take = false;
+            }
+            if (take) {
+              have = true;
+              bt = t;
+              btri = pt.tri;
+              bsurf = tri_surface[pt.tri];
+              bcull = tie ? t * (R(1) + rel) : t;
+            }
           }
         }
       } else {
-        R tmax = have ? bt : R(std::numeric_limits<float>::max());
+        R tmax = have ? bcull : R(std::numeric_limits<float>::max());
         const BvhNode<R>& l = nodes[node.a];
         const BvhNode<R>& r = nodes[node.b];
         if (st) st->node_reads += 2;
@@ -614,9 +638,10 @@ struct Mesh {
   }
 
   // mesh.rs:607-620 — normal of the ORIGINAL triangle, flipped against d.
-  bool raycast_hit(const V3<R>& p, const V3<R>& d, GeomHit<R>* h, TraversalStats* st = nullptr, uint32_t* tri_out = nullptr) const {
+  bool raycast_hit(const V3<R>& p, const V3<R>& d, GeomHit<R>* h, TraversalStats* st = nullptr, uint32_t* tri_out = nullptr,
+                   bool tie = false) const {
     R t; uint32_t tri;
-    if (!raycast(p, d, &t, &tri, st)) return false;
+    if (!raycast(p, d, &t, &tri, st, tie)) return false;
     V3<R> n = tri_normal(tri);
     if (n.dot(d) > R(0)) n = n * R(-1);
     h->t = t;
@@ -687,6 +712,7 @@ struct TraceParams {
   float wall_eps = 1e-3f;       // tracer.rs:16
   float speed_of_sound = 343.0f;// lib.rs:18
   uint32_t dir_band = 1;        // tracer.rs:123-125 (mid band)
+  uint32_t tie_mode = 0;        // 0: reference first-found; 1: lowest surface id among near-ties
 };
 
 struct TraceStats {
@@ -1030,6 +1056,173 @@ void dome_sample(const Mesh<R>& mesh, const std::vector<DomePanel>& glass, const
     out_dir[k * 3 + 1] = (float)d.y;
     out_dir[k * 3 + 2] = (float)d.z;
   }
+}
+
+}  // namespace orc
+
+namespace orc {
+
+// ----------------------------------------------------------- world build
+// crates/omg-scene/src/dome.rs:79-119 — rectangle minus holes as sub-rectangles.
+struct Rect { float u0, u1, v0, v1; };
+
+inline std::vector<Rect> subrects(Rect r, const std::vector<Rect>& holes) {
+  std::vector<float> cuts{r.u0, r.u1};
+  for (const Rect& h : holes) {
+    cuts.push_back(std::fmin(std::fmax(h.u0, r.u0), r.u1));
+    cuts.push_back(std::fmin(std::fmax(h.u1, r.u0), r.u1));
+  }
+  std::stable_sort(cuts.begin(), cuts.end());
+  std::vector<float> ded;
+  for (float c : cuts) {
+    if (!ded.empty() && std::fabs(c - ded.back()) < 1e-4f) continue;  // Vec::dedup_by keeps the first
+    ded.push_back(c);
+  }
+  std::vector<Rect> out;
+  for (size_t k = 0; k + 1 < ded.size(); k++) {
+    float u0 = ded[k], u1 = ded[k + 1];
+    if (u1 - u0 < 1e-3f) continue;
+    float um = 0.5f * (u0 + u1);
+    std::vector<std::pair<float, float>> vh;
+    for (const Rect& h : holes) {
+      if (h.u0 <= um && um <= h.u1) {
+        float a = std::fmax(h.v0, r.v0), b = std::fmin(h.v1, r.v1);
+        if (b > a) vh.push_back({a, b});
+      }
+    }
+    std::stable_sort(vh.begin(), vh.end(), [](const std::pair<float, float>& x, const std::pair<float, float>& y) {
+      return x.first < y.first;
+    });
+    float v = r.v0;
+    for (auto& h : vh) {
+      if (h.first - v > 1e-3f) out.push_back({u0, u1, v, h.first});
+      v = std::fmax(v, h.second);
+    }
+    if (r.v1 - v > 1e-3f) out.push_back({u0, u1, v, r.v1});
+  }
+  return out;
+}
+
+struct RoomC {       // walkthrough.rs:29-42
+  float min[2], max[2];
+  float height, barrier_height, floor_z, wall_thickness;
+  int outdoor;
+  Material walls[6];
+};
+
+struct DoorC {       // walkthrough.rs:228-249 (+ pane transmission)
+  int rooms[2];
+  float pos[2];
+  int axis;
+  float half, height, zc;
+  int glass;
+  float openness;
+  int heavy;
+  float pane_trans[MAXB];
+};
+
+// material.rs:59-62 in f32
+inline Material with_thickness(const Material& m, float thickness, int nb) {
+  Material o = m;
+  float k = std::fmin(0.15f / std::fmax(thickness, 0.02f), 2.0f);
+  for (int b = 0; b < nb; b++) o.transmission[b] = std::fmin(m.transmission[b] * k, 0.9f);
+  return o;
+}
+
+// dome.rs:121-258 — the world mesh: ground (coarse outside the town band),
+// every room's walls with true holes, ceiling slabs with stairwell holes.
+// Returns the glass panes as dome panels.
+inline std::vector<DomePanel> build_world_mesh(MeshBuilder& b, const std::vector<RoomC>& rooms,
+                                               const std::vector<DoorC>& doors, float town0, float town1,
+                                               float wall_max_edge, int nb) {
+  std::vector<DomePanel> glass;
+  const RoomC* outdoor = nullptr;
+  for (const RoomC& r : rooms) if (r.outdoor) { outdoor = &r; break; }
+  if (!outdoor) return glass;
+  uint16_t ground = b.material(outdoor->walls[4]);
+  b.begin_surface();
+  std::vector<Rect> shafts;
+  for (const DoorC& d : doors)
+    if (d.zc < 0.0f) shafts.push_back({d.pos[0] - 1.5f, d.pos[0] + 0.8f, d.pos[1] - d.half, d.pos[1] + d.half});
+  for (const Rect& s : subrects({outdoor->min[0], outdoor->max[0], outdoor->min[1], outdoor->max[1]}, shafts)) {
+    struct Band { float y0, y1, coarse; };
+    std::vector<Band> bands;
+    float n0 = std::fmax(s.v0, town0), n1 = std::fmin(s.v1, town1);
+    if (s.v0 < town0) bands.push_back({s.v0, std::fmin(s.v1, town0), 64.0f});
+    if (n1 > n0) bands.push_back({n0, n1, 0.0f});
+    if (s.v1 > town1) bands.push_back({std::fmax(s.v0, town1), s.v1, 64.0f});
+    for (const Band& bd : bands) {
+      b.coarse(bd.coarse == 0.0f ? wall_max_edge : bd.coarse);
+      float A[3] = {s.u0, bd.y0, 0.0f}, B[3] = {s.u1, bd.y0, 0.0f}, Cc[3] = {s.u1, bd.y1, 0.0f},
+            D[3] = {s.u0, bd.y1, 0.0f};
+      b.quad(A, B, Cc, D, ground);
+    }
+    b.coarse(wall_max_edge);
+  }
+  for (size_t ri = 0; ri < rooms.size(); ri++) {
+    const RoomC& r = rooms[ri];
+    if (r.outdoor) continue;
+    float z0 = r.floor_z, z1 = r.floor_z + r.height;
+    const RoomC* above = nullptr;
+    for (const RoomC& n : rooms) {
+      if (!n.outdoor && n.floor_z >= z1 - 0.05f && n.floor_z <= z1 + 0.8f && std::fabs(n.min[0] - r.min[0]) < 2.0f &&
+          std::fabs(n.min[1] - r.min[1]) < 2.0f) {
+        above = &n;
+        break;
+      }
+    }
+    float wall_top = above ? above->floor_z : std::fmax(r.barrier_height, z1);
+    struct Side { int wi; float plane, lo, hi; int axis; };
+    const Side sides[4] = {{0, r.min[0], r.min[1], r.max[1], 0}, {1, r.max[0], r.min[1], r.max[1], 0},
+                           {2, r.min[1], r.min[0], r.max[0], 1}, {3, r.max[1], r.min[0], r.max[0], 1}};
+    for (const Side& sd : sides) {
+      uint16_t mat = b.material(with_thickness(r.walls[sd.wi], r.wall_thickness, nb));
+      b.begin_surface();
+      std::vector<Rect> holes;
+      for (const DoorC& d : doors) {
+        if (d.axis != sd.axis || (d.rooms[0] != (int)ri && d.rooms[1] != (int)ri)) continue;
+        float dp = sd.axis == 0 ? d.pos[0] : d.pos[1];
+        float dl = sd.axis == 0 ? d.pos[1] : d.pos[0];
+        if (std::fabs(dp - sd.plane) > 0.1f) continue;
+        holes.push_back({dl - d.half, dl + d.half, d.zc - 0.5f * d.height, d.zc + 0.5f * d.height});
+        if (d.glass) {
+          DomePanel p;
+          std::memset(&p, 0, sizeof(p));
+          p.axis = sd.axis;
+          p.plane = sd.plane;
+          p.lat0 = dl - d.half;
+          p.lat1 = dl + d.half;
+          p.z0 = d.zc - 0.5f * d.height;
+          p.z1 = d.zc + 0.5f * d.height;
+          p.glass = 1;
+          for (int k = 0; k < nb; k++) p.trans[k] = d.pane_trans[k];
+          glass.push_back(p);
+        }
+      }
+      for (const Rect& s : subrects({sd.lo, sd.hi, z0, wall_top}, holes)) {
+        auto P = [&](float u, float v, float* o) {
+          if (sd.axis == 0) { o[0] = sd.plane; o[1] = u; o[2] = v; }
+          else { o[0] = u; o[1] = sd.plane; o[2] = v; }
+        };
+        float A[3], B[3], Cc[3], D[3];
+        P(s.u0, s.v0, A); P(s.u1, s.v0, B); P(s.u1, s.v1, Cc); P(s.u0, s.v1, D);
+        b.quad(A, B, Cc, D, mat);
+      }
+    }
+    uint16_t mat = b.material(with_thickness(r.walls[5], r.wall_thickness, nb));
+    b.begin_surface();
+    std::vector<Rect> holes;
+    for (const DoorC& d : doors) {
+      bool vertical = std::fabs(d.zc - z1) < 0.6f;
+      if (vertical && (d.rooms[0] == (int)ri || d.rooms[1] == (int)ri) && !d.glass)
+        holes.push_back({d.pos[0] - d.half, d.pos[0] + d.half, d.pos[1] - d.half, d.pos[1] + d.half});
+    }
+    for (const Rect& s : subrects({r.min[0], r.max[0], r.min[1], r.max[1]}, holes)) {
+      float A[3] = {s.u0, s.v0, z1}, B[3] = {s.u1, s.v0, z1}, Cc[3] = {s.u1, s.v1, z1}, D[3] = {s.u0, s.v1, z1};
+      b.quad(A, B, Cc, D, mat);
+    }
+  }
+  return glass;
 }
 
 }  // namespace orc

@@ -62,7 +62,7 @@ class TraceParams(C.Structure):
     _fields_ = [("n_bands", C.c_uint32), ("n_bins", C.c_uint32), ("bin_dt", C.c_float),
                 ("max_time", C.c_float), ("max_bounces", C.c_uint32), ("energy_floor", C.c_float),
                 ("receiver_radius", C.c_float), ("wall_eps", C.c_float), ("speed_of_sound", C.c_float),
-                ("dir_band", C.c_uint32)]
+                ("dir_band", C.c_uint32), ("tie_mode", C.c_uint32)]
 
 
 class DomePanel(C.Structure):
@@ -71,10 +71,10 @@ class DomePanel(C.Structure):
 
 
 def params(n_bands=3, n_bins=300, bin_dt=0.010, max_time=3.0, max_bounces=64, energy_floor=1e-7,
-           receiver_radius=0.5, wall_eps=1e-3, speed_of_sound=343.0, dir_band=1) -> TraceParams:
+           receiver_radius=0.5, wall_eps=1e-3, speed_of_sound=343.0, dir_band=1, tie_mode=0) -> TraceParams:
     """Defaults are the reference constants (tracer.rs:12-16, 103, 163; lib.rs:18-22)."""
     return TraceParams(n_bands, n_bins, bin_dt, max_time, max_bounces, energy_floor, receiver_radius,
-                       wall_eps, speed_of_sound, dir_band)
+                       wall_eps, speed_of_sound, dir_band, tie_mode)
 
 
 _lib = None
@@ -220,14 +220,14 @@ class Mesh:
         assert rc == 0
         return dict(node_boxes=nb, node_ab=nab, prim_geo=pg, prim_tri=pt, prim_mat=pm)
 
-    def raycast(self, o: np.ndarray, d: np.ndarray, brute: bool = False):
+    def raycast(self, o: np.ndarray, d: np.ndarray, brute: bool = False, tie: bool = False):
         o = np.ascontiguousarray(o, np.float32).reshape(-1, 3)
         d = np.ascontiguousarray(d, np.float32).reshape(-1, 3)
         n = len(o)
         t = np.zeros(n, np.float64)
         tri = np.zeros(n, np.uint32)
         st = np.zeros(2, np.uint64)
-        lib().orc_mesh_raycast(self.h, _p(o), _p(d), n, int(brute), _p(t), _p(tri), _p(st))
+        lib().orc_mesh_raycast(self.h, _p(o), _p(d), n, int(brute) | (2 if tie else 0), _p(t), _p(tri), _p(st))
         return t, tri, dict(node_reads=int(st[0]), prim_tests=int(st[1]))
 
     def segment_hits(self, a, b, cap: int = 256):

@@ -44,3 +44,13 @@ def ctx_c1(built_lib):
     c = Context(TraceConfig(n_bins=2000, bin_dt=0.001, max_time=2.0, max_bounces=200, energy_floor=1e-6))
     yield c
     c.close()
+
+
+@pytest.fixture(scope="session")
+def ctx_tie(built_lib):
+    """Config-1 constants with the precision-independent near-tie rule."""
+    from omg_audio_gb300 import Context, TraceConfig
+    c = Context(TraceConfig(n_bins=2000, bin_dt=0.001, max_time=2.0, max_bounces=200, energy_floor=1e-6,
+                            tie_mode=1))
+    yield c
+    c.close()

@@ -1,0 +1,60 @@
+"""The ambient dome on the GPU against the oracle (dome.rs:293-478).
+
+The fan is deterministic: per listener and bin, the GPU's energies (before
+the EMA) agree with the FP64 oracle within 1e-4 relative on bins holding
+>= 1e-6 of the listener's total; per-ray escape flags agree with the f32
+oracle exactly. Tolerance: 1e-4 relative per bin (the deterministic-fan bar).
+"""
+import numpy as np
+import pytest
+
+from omg_audio_gb300 import DomeProbe, MeshBuilder
+from omg_audio_gb300 import workloads as W
+from omg_audio_gb300.world import door_panels
+
+from test_oracle_golden import omat
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_probe(O, case, real, n_fan):
+    mb = O.MeshBuilder()
+    case.recorder.replay(mb, lambda m: omat(O, m))
+    mesh = mb.build(real)
+    return mesh, O.DomeProbe(mesh, [g.as_dict() for g in case.glass], n_fan=n_fan, nb=3)
+
+
+@pytest.mark.parametrize("n_fan", [384, 512])
+def test_dome_matches_fp64_oracle(ctx, oracle, n_fan):
+    O = oracle
+    case = W.multiroom(seed=2)
+    mb = MeshBuilder()
+    case.recorder.replay(mb)
+    scene = ctx.upload_builder(mb)
+    probe = DomeProbe(ctx, scene, case.glass, n_fan=n_fan)
+    eyes = case.listeners[:16]
+    # two closed doors (leaves) and the open rest
+    doors = [d for d in case.doors if not d.glass]
+    doors[0].openness, doors[3].openness = 0.0, 0.4
+    leaves = door_panels(doors)
+    g = probe.sample(eyes, leaves, n_rays=n_fan)
+    worst = 0.0
+    for e, eye in enumerate(eyes):
+        mesh64, p64 = _oracle_probe(O, case, "f64", n_fan)
+        r64 = p64.sample(eye, [l.as_dict() for l in leaves], n_rays=n_fan)
+        mesh32, p32 = _oracle_probe(O, case, "f32", n_fan)
+        r32 = p32.sample(eye, [l.as_dict() for l in leaves], n_rays=n_fan)
+        assert np.array_equal(g["escape"][e], r32["escape"])
+        raw64 = r64["raw"]
+        tot = raw64.sum()
+        m = raw64 >= 1e-6 * max(tot, 1e-300)
+        if m.any():
+            worst = max(worst, float(np.max(np.abs(g["raw"][e][m] - raw64[m]) / raw64[m])))
+        # first call primes the EMA with alpha 1: the output equals the raw bins
+        assert np.allclose(g["energy"][e], g["raw"][e], rtol=0, atol=0)
+    assert worst <= 1e-4, worst
+    # the second sample applies the 0.35 EMA per listener
+    g2 = probe.sample(eyes, leaves, n_rays=n_fan)
+    assert np.allclose(g2["energy"], g["energy"], rtol=1e-6)
+    probe.destroy()
+    scene.release()
