@@ -313,7 +313,8 @@ def main():
     ap.add_argument("--ref-pairs", type=int, default=64)
     ap.add_argument("--pairs", type=int, default=N_PAIRS, help="pairs traced per step (default: the workload's 64)")
     ap.add_argument("--profile", action="store_true", help="launches only (a small case under a profiler)")
-    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip the launch-shape autotuner (it runs once, before the warm-up)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

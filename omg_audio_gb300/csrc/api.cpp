@@ -284,6 +284,7 @@ int32_t build_graphs(omg_ctx* ctx, BatchRec& B) {
 
 int32_t prepare_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
                       uint32_t n_panels) {
+  B.shape = ctx->shape;
   int32_t rc = fill_batch(ctx, B, jobs, n_jobs, panels, n_panels);
   if (rc) return rc;
   if ((rc = alloc_batch(ctx, B))) return rc;
@@ -295,7 +296,7 @@ int32_t prepare_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n
 
 int32_t check_kernel_flags(omg_ctx* ctx, const BatchRec& B) {
   if (B.h_hdr.p->error) {
-    ctx->last_error = "traversal stack overflow in the trace kernel";
+    ctx->last_error = "trace kernel: traversal stack or walk budget exceeded";
     return OMG_E_OVERFLOW;
   }
   return OMG_OK;
@@ -671,6 +672,7 @@ done:
   B.shape = rc == OMG_OK ? best_shape : keep;
   if (rc) return rc;
   if ((rc = build_graphs(ctx, B))) return rc;
+  ctx->shape = best_shape;
   best->block_threads = best_shape.block_threads;
   best->blocks_per_sm = best_shape.blocks_per_sm;
   best->refill_min = best_shape.refill_min;

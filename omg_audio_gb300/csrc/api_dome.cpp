@@ -170,6 +170,7 @@ int32_t omg_dome_sample(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint
   L.out_energy = D.energy.p;
   L.hdr = D.hdr.p;
   L.events = D.events.p;
+  L.tie = ctx->prm.tie_mode;
   CK(launch_dome(L, s));
   std::vector<float> energy(9ull * nb * n_eyes), dir(27ull * n_eyes);
   CK(cudaMemcpyAsync(energy.data(), D.energy.p, energy.size() * 4, cudaMemcpyDeviceToHost, s));

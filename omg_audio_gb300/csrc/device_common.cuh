@@ -123,9 +123,56 @@ __device__ __forceinline__ bool ray_tri(const float4& p0, const float4& p1, cons
 constexpr float kTieRel = 1e-6f;
 
 template <bool TIE>
+__device__ __forceinline__ bool leaf_test(const float4* __restrict__ prims, int leaf, float ox, float oy, float oz,
+                                          float dx, float dy, float dz, bool& have, float& t_best, float& t_cull,
+                                          int& prim_best, uint32_t& s_best, uint32_t& tri_best) {
+  const uint32_t code = ~(uint32_t)leaf;
+  const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
+  for (uint32_t i = start; i < end; i++) {
+    const float4 p0 = __ldg(prims + 3 * i + 0);
+    const float4 p1 = __ldg(prims + 3 * i + 1);
+    const float4 p2 = __ldg(prims + 3 * i + 2);
+    float t;
+    if (ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) {
+      bool take;
+      if (!TIE) {
+        take = !have || t < t_best;
+      } else if (!have || t < t_best * (1.0f - kTieRel)) {
+        take = true;
+      } else if (t <= t_cull) {
+        const uint32_t s = __float_as_uint(p2.w), tr = __float_as_uint(p1.w);
+        take = s < s_best || (s == s_best && tr < tri_best);
+      } else {
+        take = false;
+      }
+      if (take) {
+        have = true;
+        t_best = t;
+        prim_best = (int)i;
+        if (TIE) {
+          t_cull = t * (1.0f + kTieRel);
+          s_best = __float_as_uint(p2.w);
+          tri_best = __float_as_uint(p1.w);
+        } else {
+          t_cull = t;
+        }
+      }
+    }
+  }
+  return have;
+}
+
+// While-while traversal (Aila & Laine 2009). With TIE the traversal is
+// speculative: a lane that reaches a leaf postpones it and keeps descending
+// until every active lane of the warp holds a leaf, so triangle tests run
+// together; the nearest hit is the same (only culling is later), and the
+// tie rule makes the winner independent of the visit order. Without TIE a
+// leaf is tested as soon as it is reached: the reference's exact order.
+template <bool TIE>
 __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy, float oz, float dx, float dy,
                                              float dz, float& t_best, int& prim_best, uint32_t* err) {
   if (S.n_prims == 0) return false;
+  constexpr int kDone = 0x7FFFFFFF;  // never a node index (< 2^28)
   const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
   const float4* __restrict__ nodes = S.nodes;
   const float4* __restrict__ prims = S.prims;
@@ -137,8 +184,26 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
   float stack_t[STACK_DEPTH];
   int sp = 0;
   int cur = S.root;
-  while (true) {
-    if (cur >= 0) {
+  int leaf = 0;                      // postponed leaf (< 0), or 0
+  // every node and leaf is visited at most once per ray: a walk longer than
+  // this bound means a corrupt tree; stop and flag it rather than spin
+  uint32_t budget = 2u * S.n_nodes + S.n_prims + 64u;
+  // next stacked entry that is not culled, or kDone
+  auto pop = [&]() -> int {
+    while (sp > 0) {
+      sp--;
+      if (have && (TIE ? stack_t[sp] > t_cull : stack_t[sp] >= t_best)) continue;
+      return stack_ref[sp];
+    }
+    return kDone;
+  };
+  while (cur != kDone || leaf < 0) {
+    // ---- internal nodes
+    while (cur >= 0 && cur != kDone) {
+      if (budget-- == 0u) {
+        atomicOr(err, 4u);
+        return have;
+      }
       const float4 n0 = __ldg(nodes + 4 * cur + 0);
       const float4 n1 = __ldg(nodes + 4 * cur + 1);
       const float4 n2 = __ldg(nodes + 4 * cur + 2);
@@ -160,56 +225,49 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
         } else {
           atomicOr(err, 1u);
         }
-        if (!(have && (TIE ? nt > t_cull : nt >= t_best))) { cur = nr; continue; }
+        cur = (have && (TIE ? nt > t_cull : nt >= t_best)) ? pop() : nr;
       } else if (h0) {
-        if (!(have && (TIE ? ta > t_cull : ta >= t_best))) { cur = c0; continue; }
+        cur = (have && (TIE ? ta > t_cull : ta >= t_best)) ? pop() : c0;
       } else if (h1) {
-        if (!(have && (TIE ? tb > t_cull : tb >= t_best))) { cur = c1; continue; }
+        cur = (have && (TIE ? tb > t_cull : tb >= t_best)) ? pop() : c1;
+      } else {
+        cur = pop();
       }
+      if (TIE) {
+        if (cur < 0 && leaf == 0) {  // postpone the leaf, keep descending
+          leaf = cur;
+          cur = pop();
+        }
+        if (__all_sync(__activemask(), leaf < 0 || cur == kDone)) break;
+      }
+    }
+    // ---- leaves (the postponed one, then any leaf the stack yields next)
+    if (!TIE) {
+      if (cur == kDone) break;
+      if (budget-- == 0u) {
+        atomicOr(err, 4u);
+        return have;
+      }
+      leaf_test<TIE>(prims, cur, ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best);
+      cur = pop();
     } else {
-      const uint32_t code = ~(uint32_t)cur;
-      const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
-      for (uint32_t i = start; i < end; i++) {
-        const float4 p0 = __ldg(prims + 3 * i + 0);
-        const float4 p1 = __ldg(prims + 3 * i + 1);
-        const float4 p2 = __ldg(prims + 3 * i + 2);
-        float t;
-        if (ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) {
-          bool take;
-          if (!TIE) {
-            take = !have || t < t_best;
-          } else if (!have || t < t_best * (1.0f - kTieRel)) {
-            take = true;
-          } else if (t <= t_cull) {
-            const uint32_t s = __float_as_uint(p2.w), tr = __float_as_uint(p1.w);
-            take = s < s_best || (s == s_best && tr < tri_best);
-          } else {
-            take = false;
-          }
-          if (take) {
-            have = true;
-            t_best = t;
-            prim_best = (int)i;
-            if (TIE) {
-              t_cull = t * (1.0f + kTieRel);
-              s_best = __float_as_uint(p2.w);
-              tri_best = __float_as_uint(p1.w);
-            } else {
-              t_cull = t;
-            }
-          }
+      if (leaf == 0 && cur < 0) {  // a leaf reached outside the node loop (e.g. a leaf root)
+        leaf = cur;
+        cur = pop();
+      }
+      while (leaf < 0) {
+        if (budget-- == 0u) {
+          atomicOr(err, 4u);
+          return have;
+        }
+        leaf_test<TIE>(prims, leaf, ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best);
+        leaf = 0;
+        if (cur < 0) {
+          leaf = cur;
+          cur = pop();
         }
       }
     }
-    bool found = false;
-    while (sp > 0) {
-      sp--;
-      if (have && (TIE ? stack_t[sp] > t_cull : stack_t[sp] >= t_best)) continue;
-      cur = stack_ref[sp];
-      found = true;
-      break;
-    }
-    if (!found) break;
   }
   return have;
 }

@@ -33,6 +33,7 @@ __device__ __forceinline__ bool panel_hit(const DDomePanel& p, float ox, float o
 }
 
 // dome.rs:328-382. Returns true (escaped) with the throughput in tp.
+template <bool TIE>
 __device__ bool trace_escape(const DScene& S, const DDomeLaunch& L, float px, float py, float pz, float dx, float dy,
                              float dz, float tp[MAXB], uint32_t& events) {
   const uint32_t nb = L.nb;
@@ -42,7 +43,7 @@ __device__ bool trace_escape(const DScene& S, const DDomeLaunch& L, float px, fl
     events++;
     float tm = FLT_MAX;
     int prim = 0;
-    const bool mh = mesh_closest<false>(S, px, py, pz, dx, dy, dz, tm, prim, &L.hdr->error);
+    const bool mh = mesh_closest<TIE>(S, px, py, pz, dx, dy, dz, tm, prim, &L.hdr->error);
     const float t_mesh = mh ? tm : FLT_MAX;
     float t_pan = t_mesh;
     int pan = -1;
@@ -222,6 +223,7 @@ __device__ void trace_through(const DScene& S, const DDomeLaunch& L, float ex, f
   }
 }
 
+template <bool TIE>
 __global__ void dome_rays_kernel(DDomeLaunch L) {
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= L.n_eyes * L.n_rays) return;
@@ -232,7 +234,7 @@ __global__ void dome_rays_kernel(DDomeLaunch L) {
   const float ex = L.eyes[3 * eye], ey = L.eyes[3 * eye + 1], ez = L.eyes[3 * eye + 2];
   float bp[MAXB], tp[MAXB];
   uint32_t events = 0, through = 0;
-  const bool esc = trace_escape(S, L, ex, ey, ez, f.x, f.y, f.z, bp, events);
+  const bool esc = trace_escape<TIE>(S, L, ex, ey, ez, f.x, f.y, f.z, bp, events);
   if (esc && bp[0] > 0.5f) {
 #pragma unroll
     for (int b = 0; b < MAXB; b++) tp[b] = bp[b];
@@ -340,7 +342,8 @@ cudaError_t build_dome_fan(float4* fan, uint32_t n, cudaStream_t s) {
 cudaError_t launch_dome(const DDomeLaunch& L, cudaStream_t s) {
   const uint64_t total = (uint64_t)L.n_eyes * L.n_rays;
   if (total == 0) return cudaSuccess;
-  dome_rays_kernel<<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);
+  if (L.tie) dome_rays_kernel<true><<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);
+  else dome_rays_kernel<false><<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);
   dome_bins_kernel<<<L.n_eyes, 32, 0, s>>>(L, 0.35f);
   return cudaGetLastError();
 }

@@ -93,7 +93,7 @@ struct alignas(16) DJob {
 // Per-launch header in device memory (scratch: cleared before every launch).
 struct alignas(16) DLaunch {
   uint32_t ray_counter;   // persistent-queue head
-  uint32_t error;         // OMG_E_OVERFLOW etc. set by kernels
+  uint32_t error;         // kernel flags: 1 stack overflow, 2 crossing list overflow, 4 walk budget
   uint32_t pad[2];
 };
 
@@ -106,7 +106,7 @@ inline uint64_t out_floats(uint32_t n_bins, uint32_t nb) { return 1ull * n_bins 
 struct LaunchShape {
   uint32_t block_threads = 128;
   uint32_t blocks_per_sm = 4;
-  uint32_t refill_min = 32;     // rays fetched per warp refill (multiple of 32 not required)
+  uint32_t refill_min = 1;      // a warp refetches rays once this many lanes are idle
 };
 
 // ----------------------------------------------------------- kernel launchers
@@ -163,6 +163,7 @@ struct DDomeLaunch {
   float* out_energy;          // n_eyes x 9 x nb
   DLaunch* hdr;
   uint32_t* events;           // escape events + through calls (2 counters)
+  uint32_t tie;               // near-tie rule of the escape raycasts (omg_params.tie_mode)
 };
 cudaError_t launch_dome(const DDomeLaunch& L, cudaStream_t s);
 cudaError_t build_dome_fan(float4* fan, uint32_t n_fan, cudaStream_t s);

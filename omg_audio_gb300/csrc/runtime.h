@@ -143,6 +143,7 @@ struct omg_ctx {
   omg::DevBuf<omg::DReverbJob> r_jobs;
   omg::DevBuf<omg_reverb> r_out;
   uint64_t last_h2d = 0, last_d2h = 0;     // copy volume of the last one-shot trace
+  omg::LaunchShape shape;                  // launch shape for new batches (the autotuner's last pick)
 };
 
 

@@ -359,10 +359,12 @@ struct DomeHandle {
   std::vector<V3<double>> fan_d;
   std::vector<float> ema;
   int primed = 0;
+  bool tie = false;
 };
 
-void* orc_dome_new(void* meshv, const DomePanel* glass, uint32_t n_glass, uint32_t n_fan, uint32_t nb) {
+void* orc_dome_new(void* meshv, const DomePanel* glass, uint32_t n_glass, uint32_t n_fan, uint32_t nb, int tie) {
   DomeHandle* d = new DomeHandle();
+  d->tie = tie != 0;
   d->mesh = (MeshHandle*)meshv;
   d->glass.assign(glass, glass + n_glass);
   if (d->mesh->real == 0) d->fan_f = dome_fan<float>(n_fan);
@@ -383,11 +385,11 @@ int orc_dome_sample(void* dv, const float* eye, const DomePanel* leaves, uint32_
   if (d->mesh->real == 0) {
     if (n_rays > d->fan_f.size()) return -1;
     dome_sample<float>(d->mesh->mf, d->glass, lv, d->fan_f, from_f<float>(eye), n_rays, max_events, nb, ema_alpha,
-                       d->ema.data(), &d->primed, out_dir, out_energy, raw_energy, escape_flags, ray_tp, &st);
+                       d->ema.data(), &d->primed, out_dir, out_energy, raw_energy, escape_flags, ray_tp, &st, d->tie);
   } else {
     if (n_rays > d->fan_d.size()) return -1;
     dome_sample<double>(d->mesh->md, d->glass, lv, d->fan_d, from_f<double>(eye), n_rays, max_events, nb, ema_alpha,
-                        d->ema.data(), &d->primed, out_dir, out_energy, raw_energy, escape_flags, ray_tp, &st);
+                        d->ema.data(), &d->primed, out_dir, out_energy, raw_energy, escape_flags, ray_tp, &st, d->tie);
   }
   if (stats) {
     stats[0] = st.escape_events; stats[1] = st.through_calls;

@@ -942,13 +942,14 @@ struct DomeStats {
 // dome.rs:328-382 — specular escape, <= max_events, horizon 80 m.
 template <class R>
 bool dome_trace_escape(const Mesh<R>& mesh, const std::vector<DomePanel>& glass, const std::vector<DomePanel>& leaves,
-                       V3<R> pos, V3<R> dir, uint32_t max_events, uint32_t nb, R* tp, DomeStats* st) {
+                       V3<R> pos, V3<R> dir, uint32_t max_events, uint32_t nb, R* tp, DomeStats* st,
+                       bool tie = false) {
   const R HORIZON = R(80);
   for (uint32_t b = 0; b < nb; b++) tp[b] = R(1);
   for (uint32_t ev = 0; ev < max_events; ev++) {
     if (st) st->escape_events++;
     R tm; uint32_t tri;
-    bool mh = mesh.raycast(pos, dir, &tm, &tri, st ? &st->trav : nullptr);
+    bool mh = mesh.raycast(pos, dir, &tm, &tri, st ? &st->trav : nullptr, tie);
     R t_mesh = mh ? tm : R(std::numeric_limits<float>::max());
     R t_pan = t_mesh;
     const DomePanel* pan = nullptr;
@@ -1008,7 +1009,7 @@ void dome_sample(const Mesh<R>& mesh, const std::vector<DomePanel>& glass, const
                  const std::vector<V3<R>>& fan, const V3<R>& eye, uint32_t n_rays, uint32_t max_events, uint32_t nb,
                  float ema_alpha, float* ema_state /*9*nb*/, int* primed, float* out_dir /*9*3*/,
                  float* out_energy /*9*nb*/, double* raw_energy /*9*nb, before the EMA*/, uint8_t* escape_flags,
-                 float* ray_tp /*n_rays*nb*/, DomeStats* st) {
+                 float* ray_tp /*n_rays*nb*/, DomeStats* st, bool tie = false) {
   const float PI = 3.14159265358979323846f;
   const float TAU = 6.28318530717958647692f;
   uint32_t N = (uint32_t)fan.size();
@@ -1020,7 +1021,7 @@ void dome_sample(const Mesh<R>& mesh, const std::vector<DomePanel>& glass, const
     uint32_t i = (uint32_t)((uint64_t)j * N / n_rays);
     V3<R> d0 = fan[i];
     R bp[MAXB], tp[MAXB];
-    bool esc = dome_trace_escape<R>(mesh, glass, leaves, eye, d0, max_events, nb, bp, st);
+    bool esc = dome_trace_escape<R>(mesh, glass, leaves, eye, d0, max_events, nb, bp, st, tie);
     if (escape_flags) escape_flags[j] = esc ? 1 : 0;
     if (esc && bp[0] > R(0.5)) {
       for (uint32_t b = 0; b < nb; b++) tp[b] = bp[b];

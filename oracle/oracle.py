@@ -116,7 +116,7 @@ def lib():
         L.orc_trace_mesh_log.restype = U32
         L.orc_estimate_reverb.argtypes = [P, U32, U32, F, I, P, P, P]
         L.orc_late_direction.argtypes = [P, P, U32, U32, U32, F, F, I, P, P]
-        L.orc_dome_new.argtypes = [P, P, U32, U32, U32]
+        L.orc_dome_new.argtypes = [P, P, U32, U32, U32, I]
         L.orc_dome_new.restype = P
         L.orc_dome_free.argtypes = [P]
         L.orc_dome_sample.argtypes = [P, P, P, U32, U32, U32, U32, F, P, P, P, P, P, P]
@@ -349,12 +349,13 @@ def dome_panels(panels):
 class DomeProbe:
     """crates/omg-scene/src/dome.rs:293-478 over a prebuilt world mesh."""
 
-    def __init__(self, mesh: Mesh, glass=(), n_fan=384, nb=3):
+    def __init__(self, mesh: Mesh, glass=(), n_fan=384, nb=3, tie=False):
         arr, n = dome_panels(list(glass))
         self._glass = arr
         self.mesh = mesh
         self.nb = nb
-        self.h = lib().orc_dome_new(mesh.h, C.cast(arr, C.c_void_p) if arr is not None else None, n, n_fan, nb)
+        self.h = lib().orc_dome_new(mesh.h, C.cast(arr, C.c_void_p) if arr is not None else None, n, n_fan, nb,
+                                    int(tie))
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -394,4 +395,56 @@ def pcg_draws(seed: int, ray: int, n: int) -> np.ndarray:
 def xorshift_draws(seed: int, n: int) -> np.ndarray:
     out = np.zeros(n, np.uint64)
     lib().orc_xorshift_draws(seed, n, _p(out))
+    return out
+
+
+# ------------------------------------------------------------- world build
+class RoomC(C.Structure):
+    """walkthrough.rs:29-42."""
+    _fields_ = [("min", C.c_float * 2), ("max", C.c_float * 2), ("height", C.c_float),
+                ("barrier_height", C.c_float), ("floor_z", C.c_float), ("wall_thickness", C.c_float),
+                ("outdoor", C.c_int), ("walls", Material * 6)]
+
+
+class DoorC(C.Structure):
+    """walkthrough.rs:228-249 with the pane's amplitude transmission."""
+    _fields_ = [("rooms", C.c_int * 2), ("pos", C.c_float * 2), ("axis", C.c_int), ("half", C.c_float),
+                ("height", C.c_float), ("zc", C.c_float), ("glass", C.c_int), ("openness", C.c_float),
+                ("heavy", C.c_int), ("pane_trans", C.c_float * MAXB)]
+
+
+def world_build(mb: MeshBuilder, rooms, doors, town=(-40.0, 120.0), wall_max_edge=0.0, nb=3):
+    """dome.rs:121-258 into an oracle MeshBuilder. rooms/doors: dicts with the
+    walkthrough fields; room walls are oracle Materials; door 'pane_trans' is
+    the pane's amplitude transmission. Returns the glass panes as dicts."""
+    L = lib()
+    L.orc_world_build.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_float, C.c_float,
+                                  C.c_float, C.c_uint32, C.c_void_p, C.c_uint32]
+    L.orc_world_build.restype = C.c_uint32
+    ra = (RoomC * len(rooms))()
+    for i, r in enumerate(rooms):
+        ra[i].min[0], ra[i].min[1] = r["min"]
+        ra[i].max[0], ra[i].max[1] = r["max"]
+        ra[i].height, ra[i].barrier_height = r["height"], r["barrier_height"]
+        ra[i].floor_z, ra[i].wall_thickness = r["floor_z"], r["wall_thickness"]
+        ra[i].outdoor = int(r["outdoor"])
+        for w in range(6):
+            ra[i].walls[w] = r["walls"][w]
+    da = (DoorC * max(1, len(doors)))()
+    for i, d in enumerate(doors):
+        da[i].rooms[0], da[i].rooms[1] = d["rooms"]
+        da[i].pos[0], da[i].pos[1] = d["pos"]
+        da[i].axis, da[i].half, da[i].height, da[i].zc = d["axis"], d["half"], d["height"], d["zc"]
+        da[i].glass, da[i].openness, da[i].heavy = int(d["glass"]), d["openness"], int(d["heavy"])
+        for b, v in enumerate(d.get("pane_trans", ())):
+            da[i].pane_trans[b] = v
+    cap = 256
+    ga = (DomePanel * cap)()
+    n = L.orc_world_build(mb.h, C.cast(ra, C.c_void_p), len(rooms), C.cast(da, C.c_void_p), len(doors), town[0],
+                          town[1], wall_max_edge, nb, C.cast(ga, C.c_void_p), cap)
+    out = []
+    for i in range(min(n, cap)):
+        g = ga[i]
+        out.append(dict(axis=g.axis, plane=g.plane, lat=(g.lat0, g.lat1), z=(g.z0, g.z1), glass=bool(g.glass),
+                        trans=tuple(g.trans[:nb])))
     return out
