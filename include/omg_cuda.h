@@ -265,7 +265,8 @@ int32_t omg_poll(omg_ctx* ctx, uint32_t ticket, float* bins, float* dirs, omg_re
 typedef struct omg_tune_result {
     uint32_t block_threads;
     uint32_t blocks_per_sm;
-    uint32_t refill_min;
+    uint32_t refill_min;         /* a warp refills from the ray queue once this many lanes idle */
+    uint32_t walk_steps;         /* traversal steps per lane per loop iteration (0 = whole walk) */
     float ms;
 } omg_tune_result;
 int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t batch_id, uint32_t reps, omg_tune_result* best);

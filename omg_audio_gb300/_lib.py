@@ -69,7 +69,7 @@ class omg_dome_bin(C.Structure):
 
 class omg_tune_result(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("refill_min", C.c_uint32),
-                ("ms", C.c_float)]
+                ("walk_steps", C.c_uint32), ("ms", C.c_float)]
 
 
 P, U32, U64, I32, F = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int32, C.c_float

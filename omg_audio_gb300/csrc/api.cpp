@@ -635,8 +635,9 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
   BatchRec& B = *it->second;
   if (reps == 0) reps = 3;
   const uint32_t threads[] = {64, 128, 256};
-  const uint32_t per_sm[] = {2, 4, 8, 16};
-  const uint32_t refill[] = {1, 8, 16};
+  const uint32_t per_sm[] = {2, 4, 8};
+  const uint32_t refill[] = {1, 8};
+  const uint32_t walks[] = {8, 32, 0};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -646,11 +647,13 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
   int32_t rc = OMG_OK;
   for (uint32_t th : threads)
     for (uint32_t ps : per_sm)
-      for (uint32_t rf : refill) {
+      for (uint32_t rf : refill)
+        for (uint32_t wk : walks) {
         if (th * ps > 2048) continue;
         B.shape.block_threads = th;
         B.shape.blocks_per_sm = ps;
         B.shape.refill_min = rf;
+        B.shape.walk_steps = wk;
         // warm-up, then timed repetitions on the context stream
         if ((rc = record_launch(ctx, B, ctx->stream))) goto done;
         if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { rc = OMG_E_DEVICE; goto done; }
@@ -676,6 +679,7 @@ done:
   best->block_threads = best_shape.block_threads;
   best->blocks_per_sm = best_shape.blocks_per_sm;
   best->refill_min = best_shape.refill_min;
+  best->walk_steps = best_shape.walk_steps;
   best->ms = best_ms;
   return OMG_OK;
 }

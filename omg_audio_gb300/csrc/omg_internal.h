@@ -107,6 +107,7 @@ struct LaunchShape {
   uint32_t block_threads = 128;
   uint32_t blocks_per_sm = 4;
   uint32_t refill_min = 1;      // a warp refetches rays once this many lanes are idle
+  uint32_t walk_steps = 16;     // traversal steps per lane per loop iteration (0 = a whole walk)
 };
 
 // ----------------------------------------------------------- kernel launchers

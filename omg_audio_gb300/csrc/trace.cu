@@ -106,17 +106,187 @@ __device__ __forceinline__ uint32_t find_job(const DJob* __restrict__ jobs, uint
   return lo;
 }
 
+// Per-lane closest-hit walk that can stop after a step budget and resume
+// (mesh.rs:484-541 semantics; TIE as in mesh_closest).
+struct Walk {
+  int cur;
+  int leaf;          // postponed leaf (TIE), or 0
+  int sp;
+  bool have;
+  float t_best, t_cull;
+  uint32_t s_best, tri_best;
+  int prim_best;
+  float ix, iy, iz;
+  uint32_t budget;
+  int stack_ref[STACK_DEPTH];
+  float stack_t[STACK_DEPTH];
+};
+
+constexpr int kDone = 0x7FFFFFFF;  // never a node index (< 2^28)
+
+template <bool TIE>
+__device__ __forceinline__ int walk_pop(Walk& w) {
+  while (w.sp > 0) {
+    w.sp--;
+    if (w.have && (TIE ? w.stack_t[w.sp] > w.t_cull : w.stack_t[w.sp] >= w.t_best)) continue;
+    return w.stack_ref[w.sp];
+  }
+  return kDone;
+}
+
+__device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float dx, float dy, float dz) {
+  w.cur = S.n_prims ? S.root : kDone;
+  w.leaf = 0;
+  w.sp = 0;
+  w.have = false;
+  w.t_best = FLT_MAX;
+  w.t_cull = FLT_MAX;
+  w.s_best = 0;
+  w.tri_best = 0;
+  w.prim_best = 0;
+  w.ix = 1.0f / dx;
+  w.iy = 1.0f / dy;
+  w.iz = 1.0f / dz;
+  w.budget = 2u * S.n_nodes + S.n_prims + 64u;
+}
+
+// Up to `steps` node visits / leaf tests; returns true when the walk is done.
+template <bool TIE>
+__device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, float oy, float oz, float dx,
+                                           float dy, float dz, int steps, uint32_t* err) {
+  const float4* __restrict__ nodes = S.nodes;
+  const float4* __restrict__ prims = S.prims;
+  if (!TIE) {
+    // the reference's order: each node or leaf as it is reached
+    while (steps-- > 0 && w.cur != kDone) {
+      if (w.budget-- == 0u) {
+        atomicOr(err, 4u);
+        w.cur = kDone;
+        break;
+      }
+      if (w.cur >= 0) {
+        const float4 n0 = __ldg(nodes + 4 * w.cur + 0);
+        const float4 n1 = __ldg(nodes + 4 * w.cur + 1);
+        const float4 n2 = __ldg(nodes + 4 * w.cur + 2);
+        const float4 n3 = __ldg(nodes + 4 * w.cur + 3);
+        const float tmax = w.have ? w.t_cull : FLT_MAX;
+        float ta, tb;
+        const bool h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ox, oy, oz, w.ix, w.iy, w.iz, tmax, ta);
+        const bool h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ox, oy, oz, w.ix, w.iy, w.iz, tmax, tb);
+        const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+        if (h0 && h1) {
+          int nr, fr;
+          float nt, ft;
+          if (ta <= tb) { nr = c0; nt = ta; fr = c1; ft = tb; }
+          else { nr = c1; nt = tb; fr = c0; ft = ta; }
+          if (w.sp < STACK_DEPTH) {
+            w.stack_ref[w.sp] = fr;
+            w.stack_t[w.sp] = ft;
+            w.sp++;
+          } else {
+            atomicOr(err, 1u);
+          }
+          w.cur = (w.have && nt >= w.t_best) ? walk_pop<TIE>(w) : nr;
+        } else if (h0) {
+          w.cur = (w.have && ta >= w.t_best) ? walk_pop<TIE>(w) : c0;
+        } else if (h1) {
+          w.cur = (w.have && tb >= w.t_best) ? walk_pop<TIE>(w) : c1;
+        } else {
+          w.cur = walk_pop<TIE>(w);
+        }
+      } else {
+        leaf_test<TIE>(prims, w.cur, ox, oy, oz, dx, dy, dz, w.have, w.t_best, w.t_cull, w.prim_best, w.s_best,
+                       w.tri_best);
+        w.cur = walk_pop<TIE>(w);
+      }
+    }
+    return w.cur == kDone;
+  }
+  // speculative while-while: descend, postponing one leaf, until every lane of
+  // the warp holds a leaf; then test leaves
+  while (steps > 0 && w.cur >= 0 && w.cur != kDone) {
+    steps--;
+    if (w.budget-- == 0u) {
+      atomicOr(err, 4u);
+      w.cur = kDone;
+      w.leaf = 0;
+      return true;
+    }
+    const float4 n0 = __ldg(nodes + 4 * w.cur + 0);
+    const float4 n1 = __ldg(nodes + 4 * w.cur + 1);
+    const float4 n2 = __ldg(nodes + 4 * w.cur + 2);
+    const float4 n3 = __ldg(nodes + 4 * w.cur + 3);
+    const float tmax = w.have ? w.t_cull : FLT_MAX;
+    float ta, tb;
+    const bool h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ox, oy, oz, w.ix, w.iy, w.iz, tmax, ta);
+    const bool h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ox, oy, oz, w.ix, w.iy, w.iz, tmax, tb);
+    const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+    if (h0 && h1) {
+      int nr, fr;
+      float nt, ft;
+      if (ta <= tb) { nr = c0; nt = ta; fr = c1; ft = tb; }
+      else { nr = c1; nt = tb; fr = c0; ft = ta; }
+      if (w.sp < STACK_DEPTH) {
+        w.stack_ref[w.sp] = fr;
+        w.stack_t[w.sp] = ft;
+        w.sp++;
+      } else {
+        atomicOr(err, 1u);
+      }
+      w.cur = (w.have && nt > w.t_cull) ? walk_pop<TIE>(w) : nr;
+    } else if (h0) {
+      w.cur = (w.have && ta > w.t_cull) ? walk_pop<TIE>(w) : c0;
+    } else if (h1) {
+      w.cur = (w.have && tb > w.t_cull) ? walk_pop<TIE>(w) : c1;
+    } else {
+      w.cur = walk_pop<TIE>(w);
+    }
+    if (w.cur < 0 && w.leaf == 0) {
+      w.leaf = w.cur;
+      w.cur = walk_pop<TIE>(w);
+    }
+    if (__all_sync(__activemask(), w.leaf < 0 || w.cur == kDone)) break;
+  }
+  if (w.leaf == 0 && w.cur < 0) {
+    w.leaf = w.cur;
+    w.cur = walk_pop<TIE>(w);
+  }
+  while (w.leaf < 0 && steps > 0) {
+    steps--;
+    if (w.budget-- == 0u) {
+      atomicOr(err, 4u);
+      w.cur = kDone;
+      w.leaf = 0;
+      return true;
+    }
+    leaf_test<TIE>(prims, w.leaf, ox, oy, oz, dx, dy, dz, w.have, w.t_best, w.t_cull, w.prim_best, w.s_best,
+                   w.tri_best);
+    w.leaf = 0;
+    if (w.cur < 0) {
+      w.leaf = w.cur;
+      w.cur = walk_pop<TIE>(w);
+    }
+  }
+  return w.cur == kDone && w.leaf == 0;
+}
+
+// The tracer. Each lane runs a small state machine so that a lane whose
+// closest-hit walk ends shades its segment and starts the next one at once,
+// while the other lanes of its warp keep walking: per loop iteration a lane
+// takes at most `walk_steps` traversal steps, then shades if its walk is done.
+// Idle lanes refill from the global ray queue.
 template <int NB, bool TIE>
 __global__ void __launch_bounds__(256) trace_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
                                                     uint32_t total_rays, const DScene* __restrict__ scenes,
                                                     const DMat* __restrict__ job_mats,
                                                     const DPanel* __restrict__ panels, float* __restrict__ acc,
                                                     DLaunch* __restrict__ hdr, uint32_t* __restrict__ job_segments,
-                                                    uint32_t refill_min) {
+                                                    uint32_t refill_min, int walk_budget) {
   const unsigned FULL = 0xffffffffu;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  bool active = false;
+  enum { IDLE = 0, WALK = 1, SHADE = 2 };
+  int phase = IDLE;
   bool exhausted = false;
   uint32_t ji = 0;
   float px = 0, py = 0, pz = 0, dx = 0, dy = 0, dz = 0, dist = 0;
@@ -126,16 +296,33 @@ __global__ void __launch_bounds__(256) trace_kernel(const DJob* __restrict__ job
   Pcg rng;
   rng.s = 0;
   uint32_t bounce = 0, segs = 0;
+  Walk w;
+  Hit h;
+  bool have = false;
+  uint32_t* err = &hdr->error;
+
+  // begin one segment from (p, d): the box hit directly, or a mesh walk
+  auto begin_segment = [&](const DJob& J) {
+    if (J.geom == OMG_GEOM_BOX) {
+      h.t = FLT_MAX;
+      h.m = nullptr;
+      have = box_hit(J, job_mats, px, py, pz, dx, dy, dz, h);
+      phase = SHADE;
+    } else {
+      walk_begin(w, scenes[J.scene], dx, dy, dz);
+      phase = WALK;
+    }
+  };
 
   while (true) {
     // ---- refill idle lanes from the global ray queue (warp-aggregated)
-    const unsigned idle = __ballot_sync(FULL, !active);
+    const unsigned idle = __ballot_sync(FULL, phase == IDLE);
     if (!exhausted && idle != 0u && (__popc(idle) >= (int)refill_min || idle == FULL)) {
       uint32_t base = 0;
       if (lane == 0) base = atomicAdd(&hdr->ray_counter, (uint32_t)__popc(idle));
       base = __shfl_sync(FULL, base, 0);
       if (base >= total_rays) exhausted = true;
-      if (!active) {
+      if (phase == IDLE) {
         const uint32_t r = base + (uint32_t)__popc(idle & lt_mask);
         if (r < total_rays) {
           ji = find_job(jobs, n_jobs, r);
@@ -148,42 +335,41 @@ __global__ void __launch_bounds__(256) trace_kernel(const DJob* __restrict__ job
           dist = 0.0f;
           bounce = 0;
           segs = 0;
-          active = true;
+          begin_segment(J);
         }
       }
     }
-    if (__ballot_sync(FULL, active) == 0u) {
+    if (__ballot_sync(FULL, phase != IDLE) == 0u) {
       if (exhausted) break;
       continue;
     }
-    if (!active) continue;
+
+    // ---- closest-hit walk, at most walk_budget steps this iteration
+    if (phase == WALK) {
+      const DJob& J = jobs[ji];
+      const DScene& S = scenes[J.scene];
+      if (walk_steps<TIE>(w, S, px, py, pz, dx, dy, dz, walk_budget, err)) {
+        have = w.have;
+        h.t = FLT_MAX;
+        h.m = nullptr;
+        if (have) {
+          const float4 p0 = __ldg(S.prims + 3 * w.prim_best + 0);
+          const float4 p1 = __ldg(S.prims + 3 * w.prim_best + 1);
+          const float4 nn = __ldg(S.normals + __float_as_uint(p1.w));
+          float nx = nn.x, ny = nn.y, nz = nn.z;
+          if (nx * dx + ny * dy + nz * dz > 0.0f) { nx = nx * -1.0f; ny = ny * -1.0f; nz = nz * -1.0f; }
+          h.t = w.t_best;
+          h.nx = nx; h.ny = ny; h.nz = nz;
+          h.m = S.mats + __float_as_uint(p0.w);
+        }
+        phase = SHADE;
+      }
+    }
+    if (phase != SHADE) continue;
 
     // ---- one segment of the bounce loop (tracer.rs:103-200)
     const DJob& J = jobs[ji];
     const uint32_t nb = J.nb;
-    Hit h;
-    h.t = FLT_MAX;
-    h.m = nullptr;
-    bool have;
-    if (J.geom == OMG_GEOM_BOX) {
-      have = box_hit(J, job_mats, px, py, pz, dx, dy, dz, h);
-    } else {
-      const DScene S = scenes[J.scene];
-      int prim = 0;
-      float t;
-      have = mesh_closest<TIE>(S, px, py, pz, dx, dy, dz, t, prim, &hdr->error);
-      if (have) {
-        const float4 p0 = __ldg(S.prims + 3 * prim + 0);
-        const float4 p1 = __ldg(S.prims + 3 * prim + 1);
-        const uint32_t tri = __float_as_uint(p1.w);
-        const float4 nn = __ldg(S.normals + tri);
-        float nx = nn.x, ny = nn.y, nz = nn.z;
-        if (nx * dx + ny * dy + nz * dz > 0.0f) { nx = nx * -1.0f; ny = ny * -1.0f; nz = nz * -1.0f; }
-        h.t = t;
-        h.nx = nx; h.ny = ny; h.nz = nz;
-        h.m = S.mats + __float_as_uint(p0.w);
-      }
-    }
     if (J.n_panels) have = panels_hit(J, panels, job_mats, px, py, pz, dx, dy, dz, have, h);
     segs++;
     const float t_hit = have ? h.t : FLT_MAX;
@@ -281,7 +467,9 @@ __global__ void __launch_bounds__(256) trace_kernel(const DJob* __restrict__ job
     if (!done && bounce >= J.max_bounces) done = true;
     if (done) {
       atomicAdd(job_segments + ji, segs);
-      active = false;
+      phase = IDLE;
+    } else {
+      begin_segment(J);
     }
   }
 }
@@ -335,9 +523,10 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
   uint32_t blocks = (uint32_t)(want < need ? want : need);
   if (blocks == 0) blocks = 1;
   uint32_t refill = shape.refill_min == 0 ? 1 : (shape.refill_min > 32 ? 32 : shape.refill_min);
+  const int steps = shape.walk_steps == 0 ? 1000000 : (int)shape.walk_steps;
 #define OMG_TRACE_LAUNCH(NB, TIE)                                                                        \
   trace_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, acc, hdr, \
-                                                   job_segments, refill)
+                                                   job_segments, refill, steps)
   if (max_nb <= 3) {
     if (tie) OMG_TRACE_LAUNCH(3, true);
     else OMG_TRACE_LAUNCH(3, false);

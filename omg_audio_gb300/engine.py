@@ -369,7 +369,8 @@ class Batch:
     def autotune(self, reps: int = 2):
         r = _lib.omg_tune_result()
         self.ctx._check(lib().omg_batch_autotune(self.ctx.h, self.id, reps, C.byref(r)), "omg_batch_autotune")
-        return dict(block_threads=r.block_threads, blocks_per_sm=r.blocks_per_sm, refill_min=r.refill_min, ms=r.ms)
+        return dict(block_threads=r.block_threads, blocks_per_sm=r.blocks_per_sm, refill_min=r.refill_min,
+                    walk_steps=r.walk_steps, ms=r.ms)
 
     def destroy(self):
         if self.id:

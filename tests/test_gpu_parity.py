@@ -126,12 +126,16 @@ def test_closest_hit_tri_ids(ctx, ctx_tie, oracle, bvh, tie):
     hit_g = tri_gpu != 0xFFFFFFFF
     assert np.array_equal(hit_g, tri32 != 0xFFFFFFFF)
     same_t = t_gpu[hit_g] == t32[hit_g].astype(np.float32)
-    if tie == 0:
-        assert same_t.all()  # the same arithmetic over the same primitives
-        if bvh == _lib.BVH_SAH:
-            assert np.array_equal(tri_gpu, tri32)  # the reference tree: every tie breaks the same way
+    if tie == 0 and bvh == _lib.BVH_SAH:
+        assert same_t.all()  # the same arithmetic over the same primitives and the same tree
+        assert np.array_equal(tri_gpu, tri32)  # every tie breaks the same way
     else:
-        assert np.mean(tri_gpu == tri32) > 0.999
+        # another tree (or the tie rule) may settle a near-tie on the other
+        # coplanar triangle: its t differs by the near-tie bound at most
+        rel = np.abs(t_gpu[hit_g] - t32[hit_g]) / np.maximum(t32[hit_g], 1e-9)
+        assert np.all(rel < 1e-6), rel.max()
+        if tie:
+            assert np.mean(tri_gpu == tri32) > 0.999
     t64, tri64, _ = om64.raycast(o, d, tie=bool(tie))
     hit_r = tri64 != 0xFFFFFFFF
     pos, idx = _mesh_arrays(case.recorder)
