@@ -45,7 +45,7 @@ __device__ __forceinline__ void unit_sphere(Pcg& g, float& x, float& y, float& z
 __device__ __forceinline__ void normalize3(float& x, float& y, float& z) {
   float l = sqrtf(x * x + y * y + z * z);
   if (l > 1e-12f) {
-    float inv = 1.0f / l;
+    float inv = __frcp_rn(l);  // IEEE 1/l, as 1.0f / l
     x = x * inv;
     y = y * inv;
     z = z * inv;
@@ -93,7 +93,7 @@ __device__ __forceinline__ bool ray_tri(const float4& p0, const float4& p1, cons
   float pz = dx * e2y - dy * e2x;
   float det = e1x * px + e1y * py + e1z * pz;
   if (fabsf(det) < 1e-9f) return false;
-  float inv = 1.0f / det;
+  float inv = __frcp_rn(det);  // IEEE 1/det, as 1.0f / det
   float sx = ox - p0.x, sy = oy - p0.y, sz = oz - p0.z;
   float u = (sx * px + sy * py + sz * pz) * inv;
   if (!(u >= -1e-6f && u <= ONE_EPS)) return false;
@@ -173,7 +173,7 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
                                              float dz, float& t_best, int& prim_best, uint32_t* err) {
   if (S.n_prims == 0) return false;
   constexpr int kDone = 0x7FFFFFFF;  // never a node index (< 2^28)
-  const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+  const float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
   const float4* __restrict__ nodes = S.nodes;
   const float4* __restrict__ prims = S.prims;
   bool have = false;

@@ -109,11 +109,11 @@ __device__ uint32_t segment_hits(const DScene& S, float ax, float ay, float az, 
   float dx = bx - ax, dy = by - ay, dz = bz - az;
   const float len = sqrtf(dx * dx + dy * dy + dz * dz);
   if (len < 1e-6f) return 0;
-  const float il = 1.0f / len;
+  const float il = __frcp_rn(len);
   dx = dx * il;
   dy = dy * il;
   dz = dz * il;
-  const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+  const float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
   uint32_t n = 0;
   bool overflow = false;
   int stack[STACK_DEPTH];

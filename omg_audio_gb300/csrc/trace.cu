@@ -62,12 +62,33 @@ __device__ __forceinline__ bool box_hit(const DJob& J, const DMat* __restrict__ 
 }
 
 // scene.rs:94-137 — panel slab ENTRY test, nearest of base and panels.
+// Before the exact test (the reference's divisions, unchanged) a panel is
+// skipped when its box, grown by 1 cm, cannot meet the segment's bounding
+// box: an entry point at t0 in (1e-4, best t) lies on the panel's box and on
+// the segment, so both boxes would contain it (to within rounding, far below
+// 1 cm at room coordinates). Without a base hit the segment is unbounded and
+// every panel is tested.
 __device__ __forceinline__ bool panels_hit(const DJob& J, const DPanel* __restrict__ panels,
                                            const DMat* __restrict__ job_mats, float px, float py, float pz, float dx,
                                            float dy, float dz, bool have, Hit& h) {
   const float p[3] = {px, py, pz}, d[3] = {dx, dy, dz};
+  float slo[3], shi[3];
+  const bool bounded = have;
+  if (bounded) {
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const float q = p[a] + d[a] * h.t;
+      slo[a] = fminf(p[a], q) - 0.01f;
+      shi[a] = fmaxf(p[a], q) + 0.01f;
+    }
+  }
   for (uint32_t i = 0; i < J.n_panels; i++) {
     const DPanel& pn = panels[J.panel_off + i];
+    if (bounded && have) {
+      if (pn.mx[0] < slo[0] || pn.mn[0] > shi[0] || pn.mx[1] < slo[1] || pn.mn[1] > shi[1] || pn.mx[2] < slo[2] ||
+          pn.mn[2] > shi[2])
+        continue;
+    }
     float t0 = 0.0f, t1 = FLT_MAX;
     int axis = 3;
     bool miss = false;
@@ -92,6 +113,14 @@ __device__ __forceinline__ bool panels_hit(const DJob& J, const DPanel* __restri
       if (axis == 0) h.nx = s; else if (axis == 1) h.ny = s; else h.nz = s;
       h.m = job_mats + pn.mat;
       have = true;
+      if (bounded) {  // the segment only shrinks: tighten its box
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+          const float q = p[a] + d[a] * h.t;
+          slo[a] = fminf(p[a], q) - 0.01f;
+          shi[a] = fmaxf(p[a], q) + 0.01f;
+        }
+      }
     }
   }
   return have;
@@ -108,6 +137,8 @@ __device__ __forceinline__ uint32_t find_job(const DJob* __restrict__ jobs, uint
 
 // Per-lane closest-hit walk that can stop after a step budget and resume
 // (mesh.rs:484-541 semantics; TIE as in mesh_closest).
+// The walk's scalars stay in registers (the struct has no arrays, so it is
+// split into registers once inlined); the two stacks live beside it.
 struct Walk {
   int cur;
   int leaf;          // postponed leaf (TIE), or 0
@@ -118,8 +149,8 @@ struct Walk {
   int prim_best;
   float ix, iy, iz;
   uint32_t budget;
-  int stack_ref[STACK_DEPTH];
-  float stack_t[STACK_DEPTH];
+  int* stack_ref;
+  float* stack_t;
 };
 
 constexpr int kDone = 0x7FFFFFFF;  // never a node index (< 2^28)
@@ -144,9 +175,9 @@ __device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float dx, f
   w.s_best = 0;
   w.tri_best = 0;
   w.prim_best = 0;
-  w.ix = 1.0f / dx;
-  w.iy = 1.0f / dy;
-  w.iz = 1.0f / dz;
+  w.ix = __frcp_rn(dx);
+  w.iy = __frcp_rn(dy);
+  w.iz = __frcp_rn(dz);
   w.budget = 2u * S.n_nodes + S.n_prims + 64u;
 }
 
@@ -296,7 +327,11 @@ __global__ void __launch_bounds__(256) trace_kernel(const DJob* __restrict__ job
   Pcg rng;
   rng.s = 0;
   uint32_t bounce = 0, segs = 0;
+  int walk_stack_ref[STACK_DEPTH];
+  float walk_stack_t[STACK_DEPTH];
   Walk w;
+  w.stack_ref = walk_stack_ref;
+  w.stack_t = walk_stack_t;
   Hit h;
   bool have = false;
   uint32_t* err = &hdr->error;
