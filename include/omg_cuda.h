@@ -302,6 +302,27 @@ int32_t omg_dome_sample(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint
  * trace_through calls (dome.rs:390-422), summed over listeners. */
 int32_t omg_dome_segments(omg_ctx* ctx, uint32_t probe_id, uint64_t* escape_events, uint64_t* through_calls);
 
+/* ---------------------------------------------------------------- no-alloc */
+/* No counterpart in the reference: an addition of this library.
+ * omg_trace_box for callers that must not allocate device memory: an audio
+ * render callback or other real-time thread (an allocation can block for an
+ * unbounded time), or code running while another component owns the device
+ * allocator. The caller passes the job, the constants and its own DEVICE
+ * output buffers bins_dev[n_bins*n_bands] and dirs_dev[n_bins*3]; the work is
+ * queued on cuda_stream (NULL = the legacy default stream) and the call
+ * returns without waiting. The scratch memory lives in one fixed device array
+ * per GPU (kept until the process exits), so:
+ *  - n_bins * (n_bands + 3) must not exceed OMG_NOALLOC_MAX_CELLS, else
+ *    OMG_E_INVALID (about 352 KB of device memory per GPU);
+ *  - calls that overlap on the GPU race on that array: order them on one
+ *    stream;
+ *  - the first call on a device looks up the array's address (once per
+ *    device); make it before any stream capture.
+ * It allocates nothing: no cudaMalloc, no cudaFree, no allocating library call. */
+#define OMG_NOALLOC_MAX_CELLS 45056   /* 4096 bins x (8 bands + 3) */
+int32_t omg_trace_box_noalloc(const omg_box_job* job, const omg_params* params, float* bins_dev, float* dirs_dev,
+                              void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -121,7 +121,10 @@ SIGNATURES = {
     "omg_dome_destroy": (I32, [P, U32]),
     "omg_dome_sample": (I32, [P, U32, P, U32, P, U32, U32, U32, P, P, P, P]),
     "omg_dome_segments": (I32, [P, U32, PU64, PU64]),
+    "omg_trace_box_noalloc": (I32, [C.POINTER(omg_box_job), C.POINTER(omg_params), P, P, P]),
 }
+
+NOALLOC_MAX_CELLS = 45056
 
 _lib = None
 
