@@ -89,6 +89,63 @@ uint64_t batch_signature(const omg_job* jobs, uint32_t n, uint32_t n_panels, con
   return h;
 }
 
+// Sort a job's panels along a Morton curve of their centres and group them by
+// 4 behind union boxes (the trace kernel skips a group whose box misses the
+// segment). Panel order only matters for exact ties, which the kernel settles
+// by the original index.
+void group_panels(std::vector<DPanel>& jp, uint32_t base, std::vector<DPanelGroup>& groups, uint32_t& group_off,
+                  uint32_t& n_groups) {
+  group_off = (uint32_t)groups.size();
+  n_groups = 0;
+  if (jp.empty()) return;
+  float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+  for (const DPanel& p : jp)
+    for (int c = 0; c < 3; c++) {
+      lo[c] = std::min(lo[c], 0.5f * (p.mn[c] + p.mx[c]));
+      hi[c] = std::max(hi[c], 0.5f * (p.mn[c] + p.mx[c]));
+    }
+  auto spread = [](uint32_t v) {
+    uint64_t x = v & 0x1FFFFF;
+    x = (x | x << 32) & 0x1F00000000FFFFull;
+    x = (x | x << 16) & 0x1F0000FF0000FFull;
+    x = (x | x << 8) & 0x100F00F00F00F00Full;
+    x = (x | x << 4) & 0x10C30C30C30C30C3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+  };
+  std::vector<std::pair<uint64_t, uint32_t>> key(jp.size());
+  for (size_t i = 0; i < jp.size(); i++) {
+    uint32_t q[3];
+    for (int c = 0; c < 3; c++) {
+      float e = hi[c] - lo[c];
+      float u = e > 0 ? (0.5f * (jp[i].mn[c] + jp[i].mx[c]) - lo[c]) / e : 0.0f;
+      q[c] = (uint32_t)std::min(std::max(u * 1048575.0f, 0.0f), 1048575.0f);
+    }
+    key[i] = {(spread(q[0]) << 2) | (spread(q[1]) << 1) | spread(q[2]), (uint32_t)i};
+  }
+  std::stable_sort(key.begin(), key.end());
+  std::vector<DPanel> sorted(jp.size());
+  for (size_t i = 0; i < jp.size(); i++) sorted[i] = jp[key[i].second];
+  jp.swap(sorted);
+  for (size_t g = 0; g < jp.size(); g += 4) {
+    DPanelGroup G;
+    std::memset(&G, 0, sizeof(G));
+    G.first = base + (uint32_t)g;
+    G.count = (uint32_t)std::min<size_t>(4, jp.size() - g);
+    for (int c = 0; c < 3; c++) {
+      G.mn[c] = jp[g].mn[c];
+      G.mx[c] = jp[g].mx[c];
+    }
+    for (uint32_t k = 1; k < G.count; k++)
+      for (int c = 0; c < 3; c++) {
+        G.mn[c] = std::min(G.mn[c], jp[g + k].mn[c]);
+        G.mx[c] = std::max(G.mx[c], jp[g + k].mx[c]);
+      }
+    groups.push_back(G);
+    n_groups++;
+  }
+}
+
 // Fill the host-side job arrays of a batch (no device work).
 int32_t fill_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
                    uint32_t n_panels) {
@@ -97,6 +154,7 @@ int32_t fill_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jo
   B.jobs.assign(n_jobs, DJob{});
   B.job_mats.clear();
   B.panels.clear();
+  B.groups.clear();
   B.rjobs.assign(n_jobs, DReverbJob{});
   uint64_t acc = 0, out = 0, rays = 0;
   B.max_nb = 0;
@@ -152,6 +210,7 @@ int32_t fill_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jo
     }
     d.panel_off = (uint32_t)B.panels.size();
     d.n_panels = j.n_panels;
+    std::vector<DPanel> jp;
     for (uint32_t k = 0; k < j.n_panels; k++) {
       const omg_panel& p = panels[j.panel_offset + k];
       if (!finite3(p.mn) || !finite3(p.mx) || !valid_material(p.material, nb)) return OMG_E_INVALID;
@@ -162,9 +221,12 @@ int32_t fill_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jo
         dp.mx[c] = p.mx[c];
       }
       dp.mat = (uint32_t)B.job_mats.size();
+      dp.orig = k;
       B.job_mats.push_back(make_dmat(p.material, nb));
-      B.panels.push_back(dp);
+      jp.push_back(dp);
     }
+    group_panels(jp, (uint32_t)B.panels.size(), B.groups, d.group_off, d.n_groups);
+    B.panels.insert(B.panels.end(), jp.begin(), jp.end());
     d.ray_base = (uint32_t)rays;
     rays += j.n_rays;
     if (rays > 0xFFFFFFFFull) return OMG_E_INVALID;
@@ -192,6 +254,7 @@ int32_t alloc_batch(omg_ctx* ctx, BatchRec& B) {
   CK(B.d_jobs.alloc(B.n_jobs));
   CK(B.d_job_mats.alloc(B.job_mats.size()));
   CK(B.d_panels.alloc(B.panels.size()));
+  CK(B.d_groups.alloc(B.groups.size()));
   CK(B.d_acc.alloc(B.n_acc));
   CK(B.d_out.alloc(B.n_out));
   CK(B.d_hdr.alloc(1));
@@ -217,6 +280,9 @@ int32_t upload_batch(omg_ctx* ctx, BatchRec& B) {
   if (!B.panels.empty())
     CK(cudaMemcpyAsync(B.d_panels.p, B.panels.data(), B.panels.size() * sizeof(DPanel), cudaMemcpyHostToDevice,
                        ctx->stream));
+  if (!B.groups.empty())
+    CK(cudaMemcpyAsync(B.d_groups.p, B.groups.data(), B.groups.size() * sizeof(DPanelGroup), cudaMemcpyHostToDevice,
+                       ctx->stream));
   CK(cudaMemcpyAsync(B.d_rjobs.p, B.rjobs.data(), B.n_jobs * sizeof(DReverbJob), cudaMemcpyHostToDevice,
                      ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -231,7 +297,7 @@ int32_t record_launch(omg_ctx* ctx, BatchRec& B, cudaStream_t s, int parts = 3) 
     CK(cudaMemsetAsync(B.d_acc.p, 0, B.n_acc * sizeof(float), s));
     CK(cudaMemsetAsync(B.d_seg.p, 0, B.n_jobs * sizeof(uint32_t), s));
     CK(launch_trace(B.d_jobs.p, B.n_jobs, B.total_rays, B.max_nb, ctx->d_scenes.p, B.d_job_mats.p, B.d_panels.p,
-                    B.d_acc.p, B.d_hdr.p, B.d_seg.p, B.shape, ctx->n_sms, ctx->prm.tie_mode != 0, s));
+                    B.d_groups.p, B.d_acc.p, B.d_hdr.p, B.d_seg.p, B.shape, ctx->n_sms, ctx->prm.tie_mode != 0, s));
   }
   if (parts & 2) {
     CK(launch_finalize(B.d_jobs.p, B.n_jobs, B.d_acc.p, B.d_out.p, B.n_out, s));
@@ -349,6 +415,7 @@ int32_t one_shot(omg_ctx* ctx, const omg_job* jobs, uint32_t n_jobs, const omg_p
     BatchRec& B = *ctx->cached;
     std::vector<DMat> old_mats = B.job_mats;
     std::vector<DPanel> old_panels = B.panels;
+    std::vector<DPanelGroup> old_groups = B.groups;
     int32_t rc = fill_batch(ctx, B, jobs, n_jobs, panels, n_panels);
     if (rc) return rc;
     // materials and panels change rarely: re-upload only when they differ
@@ -361,9 +428,12 @@ int32_t one_shot(omg_ctx* ctx, const omg_job* jobs, uint32_t n_jobs, const omg_p
     if (!mats_same && !B.job_mats.empty())
       CK(cudaMemcpyAsync(B.d_job_mats.p, B.job_mats.data(), B.job_mats.size() * sizeof(DMat),
                          cudaMemcpyHostToDevice, ctx->stream));
-    if (!pan_same && !B.panels.empty())
+    if (!pan_same && !B.panels.empty()) {
       CK(cudaMemcpyAsync(B.d_panels.p, B.panels.data(), B.panels.size() * sizeof(DPanel), cudaMemcpyHostToDevice,
                          ctx->stream));
+      CK(cudaMemcpyAsync(B.d_groups.p, B.groups.data(), B.groups.size() * sizeof(DPanelGroup),
+                         cudaMemcpyHostToDevice, ctx->stream));
+    }
   }
   return run_io(ctx, *ctx->cached, bins, dirs, reverb);
 }

@@ -157,7 +157,7 @@ extern "C" int32_t omg_trace_box_noalloc(const omg_box_job* job, const omg_param
   noalloc_setup_kernel<<<64, 256, 0, s>>>(scratch, d, walls, acc);
   LaunchShape shape;
   cudaError_t e = launch_trace(reinterpret_cast<const DJob*>(scratch + kJobOff), 1, job->n_rays, nb, nullptr,
-                               reinterpret_cast<const DMat*>(scratch + kMatOff), nullptr, scratch,
+                               reinterpret_cast<const DMat*>(scratch + kMatOff), nullptr, nullptr, scratch,
                                reinterpret_cast<DLaunch*>(scratch + kHdrOff),
                                reinterpret_cast<uint32_t*>(scratch + kSegOff), shape, n_sms, prm->tie_mode != 0, s);
   if (e != cudaSuccess) {

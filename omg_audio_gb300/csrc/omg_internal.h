@@ -52,12 +52,21 @@ struct DScene {
   uint32_t n_bands;
 };
 
-// Panel overlay (scene.rs:90-137): box and an index into the batch's material table.
+// Panel overlay (scene.rs:90-137): box, an index into the batch's material
+// table, and the panel's index in the caller's order (exact-tie rule).
 struct alignas(16) DPanel {
   float mn[3];
   uint32_t mat;
   float mx[3];
-  uint32_t pad;
+  uint32_t orig;
+};
+
+// Up to 4 spatially close panels of one job behind their union box.
+struct alignas(16) DPanelGroup {
+  float mn[3];
+  uint32_t first;   // into the batch's panel array
+  float mx[3];
+  uint32_t count;
 };
 
 // One job of a launch. Values that the reference computes per ray from
@@ -85,6 +94,8 @@ struct alignas(16) DJob {
   float c;                // speed of sound
   uint32_t panel_off;
   uint32_t n_panels;
+  uint32_t group_off;     // panel groups of this job
+  uint32_t n_groups;
   uint32_t ray_base;      // first global ray id of this job
   uint64_t acc_off;       // float offset of this job's accumulators
   uint64_t out_off;       // float offset of this job's output (bins then dirs)
@@ -107,13 +118,14 @@ struct LaunchShape {
   uint32_t block_threads = 128;
   uint32_t blocks_per_sm = 4;
   uint32_t refill_min = 1;      // a warp refetches rays once this many lanes are idle
-  uint32_t walk_steps = 16;     // traversal steps per lane per loop iteration (0 = a whole walk)
+  uint32_t walk_steps = 0;      // traversal steps per lane per loop iteration (0 = a whole walk)
 };
 
 // ----------------------------------------------------------- kernel launchers
 // trace.cu
 cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
-                         const DScene* scenes, const DMat* job_mats, const DPanel* panels, float* acc,
+                         const DScene* scenes, const DMat* job_mats, const DPanel* panels,
+                         const DPanelGroup* groups, float* acc,
                          DLaunch* hdr, uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie,
                          cudaStream_t s);
 cudaError_t launch_finalize(const DJob* jobs, uint32_t n_jobs, const float* acc, float* out, uint64_t total_out,

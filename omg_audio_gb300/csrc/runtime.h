@@ -1,5 +1,6 @@
 // Shared runtime types of the C ABI (api.cpp, api_scene.cpp, api_dome.cpp).
 #pragma once
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -79,10 +80,12 @@ struct BatchRec {
   std::vector<DJob> jobs;
   std::vector<DMat> job_mats;
   std::vector<DPanel> panels;
+  std::vector<DPanelGroup> groups;
   std::vector<DReverbJob> rjobs;
   DevBuf<DJob> d_jobs;
   DevBuf<DMat> d_job_mats;
   DevBuf<DPanel> d_panels;
+  DevBuf<DPanelGroup> d_groups;
   DevBuf<float> d_acc, d_out;
   DevBuf<DLaunch> d_hdr;
   DevBuf<uint32_t> d_seg;

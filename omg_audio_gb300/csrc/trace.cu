@@ -62,18 +62,21 @@ __device__ __forceinline__ bool box_hit(const DJob& J, const DMat* __restrict__ 
 }
 
 // scene.rs:94-137 — panel slab ENTRY test, nearest of base and panels.
-// Before the exact test (the reference's divisions, unchanged) a panel is
-// skipped when its box, grown by 1 cm, cannot meet the segment's bounding
-// box: an entry point at t0 in (1e-4, best t) lies on the panel's box and on
-// the segment, so both boxes would contain it (to within rounding, far below
-// 1 cm at room coordinates). Without a base hit the segment is unbounded and
-// every panel is tested.
+// Panels are tested group by group: a group (and then a panel) is skipped when
+// its box cannot meet the segment's bounding box grown by 1 cm. An entry point
+// at t0 in (1e-4, best t) lies on the panel's box and on the segment, so both
+// boxes contain it (to within rounding, far below 1 cm at room coordinates).
+// Without a base hit the segment is unbounded and every panel is tested. The
+// reference scans panels in order with a strict `<`, so among equal entry
+// distances the first panel wins: here, the lowest original index.
 __device__ __forceinline__ bool panels_hit(const DJob& J, const DPanel* __restrict__ panels,
+                                           const DPanelGroup* __restrict__ groups,
                                            const DMat* __restrict__ job_mats, float px, float py, float pz, float dx,
                                            float dy, float dz, bool have, Hit& h) {
   const float p[3] = {px, py, pz}, d[3] = {dx, dy, dz};
   float slo[3], shi[3];
   const bool bounded = have;
+  uint32_t best_orig = 0xFFFFFFFFu;  // the current best is the base hit
   if (bounded) {
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -82,43 +85,49 @@ __device__ __forceinline__ bool panels_hit(const DJob& J, const DPanel* __restri
       shi[a] = fmaxf(p[a], q) + 0.01f;
     }
   }
-  for (uint32_t i = 0; i < J.n_panels; i++) {
-    const DPanel& pn = panels[J.panel_off + i];
-    if (bounded && have) {
-      if (pn.mx[0] < slo[0] || pn.mn[0] > shi[0] || pn.mx[1] < slo[1] || pn.mn[1] > shi[1] || pn.mx[2] < slo[2] ||
-          pn.mn[2] > shi[2])
+  for (uint32_t g = 0; g < J.n_groups; g++) {
+    const DPanelGroup& G = groups[J.group_off + g];
+    if (bounded && (G.mx[0] < slo[0] || G.mn[0] > shi[0] || G.mx[1] < slo[1] || G.mn[1] > shi[1] ||
+                    G.mx[2] < slo[2] || G.mn[2] > shi[2]))
+      continue;
+    for (uint32_t i = G.first; i < G.first + G.count; i++) {
+      const DPanel& pn = panels[i];
+      if (bounded && (pn.mx[0] < slo[0] || pn.mn[0] > shi[0] || pn.mx[1] < slo[1] || pn.mn[1] > shi[1] ||
+                      pn.mx[2] < slo[2] || pn.mn[2] > shi[2]))
         continue;
-    }
-    float t0 = 0.0f, t1 = FLT_MAX;
-    int axis = 3;
-    bool miss = false;
+      float t0 = 0.0f, t1 = FLT_MAX;
+      int axis = 3;
+      bool miss = false;
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-      if (miss) break;
-      float da = d[a], pa = p[a], lo = pn.mn[a], hi = pn.mx[a];
-      if (fabsf(da) < 1e-9f) {
-        if (pa < lo || pa > hi) { t0 = FLT_MAX; miss = true; }
-      } else {
-        float ta = (lo - pa) / da, tb = (hi - pa) / da;
-        if (ta > tb) { float tmp = ta; ta = tb; tb = tmp; }
-        if (ta > t0) { t0 = ta; axis = a; }
-        t1 = fminf(t1, tb);
-        if (t0 > t1) { t0 = FLT_MAX; miss = true; }
+      for (int a = 0; a < 3; a++) {
+        if (miss) break;
+        float da = d[a], pa = p[a], lo = pn.mn[a], hi = pn.mx[a];
+        if (fabsf(da) < 1e-9f) {
+          if (pa < lo || pa > hi) { t0 = FLT_MAX; miss = true; }
+        } else {
+          float ta = (lo - pa) / da, tb = (hi - pa) / da;
+          if (ta > tb) { float tmp = ta; ta = tb; tb = tmp; }
+          if (ta > t0) { t0 = ta; axis = a; }
+          t1 = fminf(t1, tb);
+          if (t0 > t1) { t0 = FLT_MAX; miss = true; }
+        }
       }
-    }
-    if (t0 > 1e-4f && t0 < FLT_MAX && axis < 3 && (!have || t0 < h.t)) {
-      h.t = t0;
-      h.nx = h.ny = h.nz = 0.0f;
-      float s = d[axis] > 0.0f ? -1.0f : 1.0f;
-      if (axis == 0) h.nx = s; else if (axis == 1) h.ny = s; else h.nz = s;
-      h.m = job_mats + pn.mat;
-      have = true;
-      if (bounded) {  // the segment only shrinks: tighten its box
+      const bool closer = !have || t0 < h.t || (t0 == h.t && best_orig != 0xFFFFFFFFu && pn.orig < best_orig);
+      if (t0 > 1e-4f && t0 < FLT_MAX && axis < 3 && closer) {
+        h.t = t0;
+        h.nx = h.ny = h.nz = 0.0f;
+        float s = d[axis] > 0.0f ? -1.0f : 1.0f;
+        if (axis == 0) h.nx = s; else if (axis == 1) h.ny = s; else h.nz = s;
+        h.m = job_mats + pn.mat;
+        have = true;
+        best_orig = pn.orig;
+        if (bounded) {  // the segment only shrinks: tighten its box
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-          const float q = p[a] + d[a] * h.t;
-          slo[a] = fminf(p[a], q) - 0.01f;
-          shi[a] = fmaxf(p[a], q) + 0.01f;
+          for (int a = 0; a < 3; a++) {
+            const float q = p[a] + d[a] * h.t;
+            slo[a] = fminf(p[a], q) - 0.01f;
+            shi[a] = fmaxf(p[a], q) + 0.01f;
+          }
         }
       }
     }
@@ -307,10 +316,11 @@ __device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, f
 // takes at most `walk_steps` traversal steps, then shades if its walk is done.
 // Idle lanes refill from the global ray queue.
 template <int NB, bool TIE>
-__global__ void __launch_bounds__(256) trace_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
-                                                    uint32_t total_rays, const DScene* __restrict__ scenes,
-                                                    const DMat* __restrict__ job_mats,
-                                                    const DPanel* __restrict__ panels, float* __restrict__ acc,
+__global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
+                                                       uint32_t total_rays, const DScene* __restrict__ scenes,
+                                                       const DMat* __restrict__ job_mats,
+                                                       const DPanel* __restrict__ panels,
+                                                       const DPanelGroup* __restrict__ groups, float* __restrict__ acc,
                                                     DLaunch* __restrict__ hdr, uint32_t* __restrict__ job_segments,
                                                     uint32_t refill_min, int walk_budget) {
   const unsigned FULL = 0xffffffffu;
@@ -405,7 +415,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const DJob* __restrict__ job
     // ---- one segment of the bounce loop (tracer.rs:103-200)
     const DJob& J = jobs[ji];
     const uint32_t nb = J.nb;
-    if (J.n_panels) have = panels_hit(J, panels, job_mats, px, py, pz, dx, dy, dz, have, h);
+    if (J.n_groups) have = panels_hit(J, panels, groups, job_mats, px, py, pz, dx, dy, dz, have, h);
     segs++;
     const float t_hit = have ? h.t : FLT_MAX;
 
@@ -549,7 +559,8 @@ __global__ void raycast_kernel(const DScene* __restrict__ scene, const float* __
 }  // namespace
 
 cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
-                         const DScene* scenes, const DMat* job_mats, const DPanel* panels, float* acc, DLaunch* hdr,
+                         const DScene* scenes, const DMat* job_mats, const DPanel* panels,
+                         const DPanelGroup* groups, float* acc, DLaunch* hdr,
                          uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie, cudaStream_t s) {
   if (n_jobs == 0 || total_rays == 0) return cudaSuccess;
   uint32_t threads = shape.block_threads;
@@ -560,7 +571,8 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
   uint32_t refill = shape.refill_min == 0 ? 1 : (shape.refill_min > 32 ? 32 : shape.refill_min);
   const int steps = shape.walk_steps == 0 ? 1000000 : (int)shape.walk_steps;
 #define OMG_TRACE_LAUNCH(NB, TIE)                                                                        \
-  trace_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, acc, hdr, \
+  trace_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, groups, \
+                                                   acc, hdr, \
                                                    job_segments, refill, steps)
   if (max_nb <= 3) {
     if (tie) OMG_TRACE_LAUNCH(3, true);

@@ -430,3 +430,7 @@ uint32_t orc_world_build(void* mbv, const RoomC* rooms, uint32_t n_rooms, const 
   return (uint32_t)g.size();
 }
 }
+
+extern "C" void orc_sincos_f32(const float* phi, uint32_t n, float* s, float* c) {
+  for (uint32_t i = 0; i < n; i++) sincos_f32(phi[i], &s[i], &c[i]);
+}

@@ -122,6 +122,32 @@ struct PcgRay {
   float next_f32() { return (float)(next_u32() >> 8u) / 16777216.0f; }
 };
 
+// sin and cos of an angle in [0, 2*pi] in f32 only, the same operations in the
+// same order as the CUDA kernel's: Cody-Waite reduction by pi/2 (three-part
+// constant, exact quadrant products) and Taylor polynomials on [-pi/4, pi/4]
+// with coefficients +-1/n!. Within 3 ulp of the true values.
+inline void sincos_f32(float phi, float* s, float* c) {
+  const float k = std::nearbyint(phi * 0.636619772367581343f);
+  const float r = ((phi - k * 1.5703125f) - k * 4.837512969970703125e-4f) - k * 7.54978995489188216e-8f;
+  const float r2 = r * r;
+  const float sp =
+      r + r * r2 * (-1.66666666666666667e-1f +
+                    r2 * (8.33333333333333333e-3f + r2 * (-1.98412698412698413e-4f + r2 * 2.75573192239858907e-6f)));
+  const float cp =
+      1.0f + r2 * (-0.5f + r2 * (4.16666666666666667e-2f +
+                                 r2 * (-1.38888888888888889e-3f +
+                                       r2 * (2.48015873015873016e-5f + r2 * -2.75573192239858907e-7f))));
+  const int q = ((int)k) & 3;
+  if (q == 0) { *s = sp; *c = cp; }
+  else if (q == 1) { *s = cp; *c = -sp; }
+  else if (q == 2) { *s = -sp; *c = -cp; }
+  else { *s = -cp; *c = sp; }
+}
+
+// the ray directions' sin/cos: f32 polynomial (as the GPU), exact in FP64
+inline void dir_sincos(float phi, float* s, float* c) { sincos_f32(phi, s, c); }
+inline void dir_sincos(double phi, double* s, double* c) { *s = std::sin(phi); *c = std::cos(phi); }
+
 // rng.rs:24-29 — z = 1-2u, phi = TAU*u. The draws are f32 in the reference;
 // the FP64 oracle takes the same f32 draws and continues in R.
 template <class R, class G>
@@ -133,7 +159,7 @@ inline V3<R> unit_sphere(G& g) {
   float u2 = g.next_f32();
   R phi = R(TAU) * R(u2);
   R s, c;
-  sincos_r<R>(phi, &s, &c);
+  dir_sincos(phi, &s, &c);
   return V3<R>(r * c, r * s, z);
 }
 

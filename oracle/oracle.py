@@ -448,3 +448,14 @@ def world_build(mb: MeshBuilder, rooms, doors, town=(-40.0, 120.0), wall_max_edg
         out.append(dict(axis=g.axis, plane=g.plane, lat=(g.lat0, g.lat1), z=(g.z0, g.z1), glass=bool(g.glass),
                         trans=tuple(g.trans[:nb])))
     return out
+
+
+def sincos_f32(phi: np.ndarray):
+    """The f32 sin/cos both the oracle and the kernel use for ray directions."""
+    phi = np.ascontiguousarray(phi, np.float32)
+    s = np.zeros_like(phi)
+    c = np.zeros_like(phi)
+    L = lib()
+    L.orc_sincos_f32.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+    L.orc_sincos_f32(_p(phi), len(phi), _p(s), _p(c))
+    return s, c

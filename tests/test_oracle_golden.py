@@ -247,3 +247,16 @@ def test_f32_and_f64_oracles_agree_on_the_stream(oracle):
     r64 = O.estimate_reverb(b64, 0.010, level_f32=False)[0]
     assert np.all(np.abs(r32 / r64 - 1) < 0.01)
     assert abs(s32["segments"] - s64["segments"]) < 0.001 * s64["segments"]
+
+
+def test_f32_sincos_error_bound(oracle):
+    """The f32 sin/cos both sides use for ray directions (Cody-Waite + Taylor)
+    stays within 3 ulp of the true values on [0, 2*pi]."""
+    phi = (np.float32(6.2831855) * np.arange(1 << 18, dtype=np.float64) / (1 << 18)).astype(np.float32)
+    s, c = oracle.sincos_f32(phi)
+    S, Cc = np.sin(phi.astype(np.float64)), np.cos(phi.astype(np.float64))
+    for got, want in ((s, S), (c, Cc)):
+        big = np.abs(want) > 1e-3
+        ulp = np.spacing(np.abs(want[big]).astype(np.float32)).astype(np.float64)
+        assert np.max(np.abs(got[big] - want[big]) / ulp) <= 3.0
+        assert np.max(np.abs(got - want)) < 2e-7
