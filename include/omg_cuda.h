@@ -260,16 +260,36 @@ int32_t omg_submit_world(omg_ctx* ctx, uint32_t scene_id, const omg_world_job* j
                          uint32_t n_panels, uint32_t* ticket);
 int32_t omg_poll(omg_ctx* ctx, uint32_t ticket, float* bins, float* dirs, omg_reverb* reverb);
 
-/* Autotuner: time launch shapes (threads per block x blocks per SM x rays
- * fetched per warp) on the batch and keep the fastest for it. */
+/* Launch shape of a batch's trace. Rays first run `wf_rounds` wavefront
+ * rounds (a traversal kernel and a shading kernel over a queue of live rays);
+ * once at most `wf_tail` rays are alive, or after the last round, the
+ * persistent kernel finishes them, in `epochs` launches: an epoch parks its
+ * rays between two segments once at most `park_pct` % of them remain, and the
+ * next epoch resumes them in full warps (the last one runs every ray to its
+ * end). wf_rounds = 0 and epochs = 0: one persistent launch. The result is
+ * the same for every shape.
+ * Autotuner: times the persistent kernel's shapes (threads per block x blocks
+ * per SM x refill threshold x walk steps x shading group), then epoch counts and park
+ * thresholds, then wavefront round counts and hand-over thresholds; keeps the
+ * fastest for the batch and as the context's default for later batches. */
 typedef struct omg_tune_result {
     uint32_t block_threads;
     uint32_t blocks_per_sm;
     uint32_t refill_min;         /* a warp refills from the ray queue once this many lanes idle */
     uint32_t walk_steps;         /* traversal steps per lane per loop iteration (0 = whole walk) */
-    float ms;
+    uint32_t shade_min;          /* lanes of a warp that shade together (1..32; 0 reads as 1) */
+    uint32_t wf_rounds;          /* wavefront rounds before the persistent kernel (0 = none) */
+    uint32_t wf_tail;            /* hand over to the persistent kernel at <= this many live rays */
+    uint32_t epochs;             /* persistent-kernel epochs, <= 32 (0 = one launch) */
+    uint32_t park_pct;           /* an epoch parks its rays once <= this % of them remain */
+    float ms;                    /* autotune: mean time of the clear + trace part */
 } omg_tune_result;
 int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t batch_id, uint32_t reps, omg_tune_result* best);
+/* Set a batch's shape by hand (block_threads a multiple of 32, <= 256;
+ * block_threads x blocks_per_sm <= 2048; refill_min in 1..32); it also
+ * becomes the context's default. get: the batch's current shape (ms = 0). */
+int32_t omg_batch_set_shape(omg_ctx* ctx, uint32_t batch_id, const omg_tune_result* shape);
+int32_t omg_batch_get_shape(omg_ctx* ctx, uint32_t batch_id, omg_tune_result* shape);
 
 /* ----------------------------------------------------------- mesh queries */
 /* Closest hit per ray (Mesh::raycast, mesh.rs:484-541): t (-1 on miss) and the

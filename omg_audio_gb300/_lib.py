@@ -69,7 +69,8 @@ class omg_dome_bin(C.Structure):
 
 class omg_tune_result(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("refill_min", C.c_uint32),
-                ("walk_steps", C.c_uint32), ("ms", C.c_float)]
+                ("walk_steps", C.c_uint32), ("shade_min", C.c_uint32), ("wf_rounds", C.c_uint32), ("wf_tail", C.c_uint32),
+                ("epochs", C.c_uint32), ("park_pct", C.c_uint32), ("ms", C.c_float)]
 
 
 P, U32, U64, I32, F = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int32, C.c_float
@@ -115,6 +116,8 @@ SIGNATURES = {
     "omg_submit_world": (I32, [P, U32, C.POINTER(omg_world_job), P, U32, PU32]),
     "omg_poll": (I32, [P, U32, P, P, P]),
     "omg_batch_autotune": (I32, [P, U32, U32, C.POINTER(omg_tune_result)]),
+    "omg_batch_set_shape": (I32, [P, U32, C.POINTER(omg_tune_result)]),
+    "omg_batch_get_shape": (I32, [P, U32, C.POINTER(omg_tune_result)]),
     "omg_raycast": (I32, [P, U32, P, P, U32, P, P]),
     "omg_estimate_reverb": (I32, [P, P, U32, U32, F, U32, P]),
     "omg_dome_create": (I32, [P, U32, P, U32, U32, U32, PU32]),

@@ -63,6 +63,9 @@ int32_t sync_scene_table(omg_ctx* ctx) {
     d.n_nodes = s.n_nodes;
     d.n_prims = s.n_prims;
     d.n_bands = s.n_bands;
+    d.nodes4 = s.n_nodes4 ? s.nodes4.p : nullptr;
+    d.root4 = s.root4;
+    d.n_nodes4 = s.n_nodes4;
   }
   CK(cudaMemcpy(ctx->d_scenes.p, table.data(), table.size() * sizeof(DScene), cudaMemcpyHostToDevice));
   return OMG_OK;
@@ -266,6 +269,18 @@ int32_t alloc_batch(omg_ctx* ctx, BatchRec& B) {
   CK(B.h_hdr.alloc(1));
   CK(B.h_seg.alloc(B.n_jobs));
   CK(B.h_jobs.alloc(B.n_jobs));
+  const size_t cap = B.total_rays;
+  CK(B.d_wf_pos.alloc(cap));
+  CK(B.d_wf_dir.alloc(cap));
+  CK(B.d_wf_e.alloc(B.max_nb > 4 ? 2 * cap : cap));
+  CK(B.d_wf_bounce.alloc(cap));
+  CK(B.d_wf_queue.alloc(2 * cap));
+  CK(B.d_wf_hit.alloc(cap));
+  CK(B.d_wf_ctl.alloc(1));
+  CK(B.d_ep_q.alloc(2 * cap));
+  CK(B.d_ep_ctl.alloc(kMaxEpochs + 1));
+  B.wf = WfState{B.d_wf_pos.p, B.d_wf_dir.p, B.d_wf_e.p, B.d_wf_bounce.p, B.d_wf_hit.p, B.d_wf_queue.p,
+                 B.d_wf_ctl.p, B.total_rays};
   if (!B.done) CK(cudaEventCreateWithFlags(&B.done, cudaEventDisableTiming));
   return OMG_OK;
 }
@@ -296,8 +311,10 @@ int32_t record_launch(omg_ctx* ctx, BatchRec& B, cudaStream_t s, int parts = 3) 
     CK(cudaMemsetAsync(B.d_hdr.p, 0, sizeof(DLaunch), s));
     CK(cudaMemsetAsync(B.d_acc.p, 0, B.n_acc * sizeof(float), s));
     CK(cudaMemsetAsync(B.d_seg.p, 0, B.n_jobs * sizeof(uint32_t), s));
-    CK(launch_trace(B.d_jobs.p, B.n_jobs, B.total_rays, B.max_nb, ctx->d_scenes.p, B.d_job_mats.p, B.d_panels.p,
-                    B.d_groups.p, B.d_acc.p, B.d_hdr.p, B.d_seg.p, B.shape, ctx->n_sms, ctx->prm.tie_mode != 0, s));
+    CK(cudaMemsetAsync(B.d_ep_ctl.p, 0, (kMaxEpochs + 1) * sizeof(EpochCtl), s));
+    CK(launch_wavefront(B.d_jobs.p, B.n_jobs, B.total_rays, B.max_nb, ctx->d_scenes.p, B.d_job_mats.p,
+                        B.d_panels.p, B.d_groups.p, B.d_acc.p, B.d_hdr.p, B.d_seg.p, B.wf, B.d_ep_q.p,
+                        B.d_ep_ctl.p, B.shape, ctx->n_sms, ctx->prm.tie_mode != 0, s));
   }
   if (parts & 2) {
     CK(launch_finalize(B.d_jobs.p, B.n_jobs, B.d_acc.p, B.d_out.p, B.n_out, s));
@@ -314,6 +331,27 @@ int32_t record_readback(omg_ctx* ctx, BatchRec& B, cudaStream_t s) {
   return OMG_OK;
 }
 
+// Record the batch's work into one executable graph on capture stream cs.
+int32_t capture_graph(omg_ctx* ctx, BatchRec& B, cudaStream_t cs, bool io, int parts, cudaGraphExec_t* out) {
+  cudaGraph_t g;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(ctx, e, "cudaStreamBeginCapture");
+  int32_t rc = OMG_OK;
+  if (io) {
+    e = cudaMemcpyAsync(B.d_jobs.p, B.h_jobs.p, B.n_jobs * sizeof(DJob), cudaMemcpyHostToDevice, cs);
+    if (e != cudaSuccess) rc = fail(ctx, e, "cudaMemcpyAsync jobs");
+  }
+  if (rc == OMG_OK) rc = record_launch(ctx, B, cs, parts);
+  if (rc == OMG_OK && io) rc = record_readback(ctx, B, cs);
+  e = cudaStreamEndCapture(cs, &g);
+  if (rc != OMG_OK) return rc;
+  if (e != cudaSuccess) return fail(ctx, e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(ctx, e, "cudaGraphInstantiate");
+  return OMG_OK;
+}
+
 int32_t build_graphs(omg_ctx* ctx, BatchRec& B) {
   for (cudaGraphExec_t* g : {&B.graph, &B.graph_io, &B.graph_a, &B.graph_b}) {
     if (*g) cudaGraphExecDestroy(*g);
@@ -321,29 +359,10 @@ int32_t build_graphs(omg_ctx* ctx, BatchRec& B) {
   }
   cudaStream_t cs;
   CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-  auto capture = [&](bool io, cudaGraphExec_t* out, int parts = 3) -> int32_t {
-    cudaGraph_t g;
-    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return fail(ctx, e, "cudaStreamBeginCapture");
-    int32_t rc = OMG_OK;
-    if (io) {
-      e = cudaMemcpyAsync(B.d_jobs.p, B.h_jobs.p, B.n_jobs * sizeof(DJob), cudaMemcpyHostToDevice, cs);
-      if (e != cudaSuccess) rc = fail(ctx, e, "cudaMemcpyAsync jobs");
-    }
-    if (rc == OMG_OK) rc = record_launch(ctx, B, cs, parts);
-    if (rc == OMG_OK && io) rc = record_readback(ctx, B, cs);
-    e = cudaStreamEndCapture(cs, &g);
-    if (rc != OMG_OK) return rc;
-    if (e != cudaSuccess) return fail(ctx, e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(out, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return fail(ctx, e, "cudaGraphInstantiate");
-    return OMG_OK;
-  };
-  int32_t rc = capture(false, &B.graph);
-  if (rc == OMG_OK) rc = capture(true, &B.graph_io);
-  if (rc == OMG_OK) rc = capture(false, &B.graph_a, 1);
-  if (rc == OMG_OK) rc = capture(false, &B.graph_b, 2);
+  int32_t rc = capture_graph(ctx, B, cs, false, 3, &B.graph);
+  if (rc == OMG_OK) rc = capture_graph(ctx, B, cs, true, 3, &B.graph_io);
+  if (rc == OMG_OK) rc = capture_graph(ctx, B, cs, false, 1, &B.graph_a);
+  if (rc == OMG_OK) rc = capture_graph(ctx, B, cs, false, 2, &B.graph_b);
   cudaStreamDestroy(cs);
   return rc;
 }
@@ -433,6 +452,11 @@ int32_t one_shot(omg_ctx* ctx, const omg_job* jobs, uint32_t n_jobs, const omg_p
                          ctx->stream));
       CK(cudaMemcpyAsync(B.d_groups.p, B.groups.data(), B.groups.size() * sizeof(DPanelGroup),
                          cudaMemcpyHostToDevice, ctx->stream));
+    }
+    // the context's launch shape changed since the graphs were recorded
+    if (std::memcmp(&B.shape, &ctx->shape, sizeof(LaunchShape)) != 0) {
+      B.shape = ctx->shape;
+      if ((rc = build_graphs(ctx, B))) return rc;
     }
   }
   return run_io(ctx, *ctx->cached, bins, dirs, reverb);
@@ -627,8 +651,13 @@ int32_t omg_batch_destroy(omg_ctx* ctx, uint32_t id) {
 
 int32_t omg_batch_kernel_count(omg_ctx* ctx, uint32_t id, uint32_t* n) {
   if (!ctx || !n) return OMG_E_INVALID;
-  if (ctx->batches.find(id) == ctx->batches.end()) return OMG_E_NOT_FOUND;
-  *n = 3;  // trace, finalize, reverb
+  auto it = ctx->batches.find(id);
+  if (it == ctx->batches.end()) return OMG_E_NOT_FOUND;
+  // finalize, reverb; the persistent kernel once per epoch; wavefront: init,
+  // 2 per round, hand-over
+  const LaunchShape& sh = it->second->shape;
+  const uint32_t epochs = sh.epochs == 0 ? 1u : std::min<uint32_t>(sh.epochs, kMaxEpochs);
+  *n = 2 + epochs + (sh.wf_iters ? 2 + 2 * sh.wf_iters : 0);
   return OMG_OK;
 }
 
@@ -698,6 +727,48 @@ int32_t omg_poll(omg_ctx* ctx, uint32_t ticket, float* bins, float* dirs, omg_re
 }
 
 // ---------------------------------------------------------------- autotuner
+namespace {
+
+// Mean time of the clear + trace part with the batch's current shape: the part
+// is recorded into a graph (as launches run it), launched once to warm up,
+// then `reps` times between two events on the context stream.
+int32_t time_trace(omg_ctx* ctx, BatchRec& B, uint32_t reps, cudaStream_t cs, cudaEvent_t e0, cudaEvent_t e1,
+                   float* ms) {
+  cudaGraphExec_t g = nullptr;
+  int32_t rc = capture_graph(ctx, B, cs, false, 1, &g);
+  if (rc) return rc;
+  cudaError_t e = cudaGraphLaunch(g, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->stream);
+  for (uint32_t r = 0; r < reps && e == cudaSuccess; r++) e = cudaGraphLaunch(g, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+  if (e != cudaSuccess) rc = fail(ctx, e, "autotune launch");
+  if (rc == OMG_OK) rc = wait_event(ctx, e1, timeout_of(ctx) * (reps + 1));
+  if (rc == OMG_OK) {
+    cudaEventElapsedTime(ms, e0, e1);
+    *ms /= (float)reps;
+  }
+  cudaGraphExecDestroy(g);
+  return rc;
+}
+
+void shape_to_result(const LaunchShape& sh, float ms, omg_tune_result* r) {
+  r->block_threads = sh.block_threads;
+  r->blocks_per_sm = sh.blocks_per_sm;
+  r->refill_min = sh.refill_min;
+  r->walk_steps = sh.walk_steps;
+  r->wf_rounds = sh.wf_iters;
+  r->wf_tail = sh.wf_tail;
+  r->epochs = sh.epochs;
+  r->park_pct = sh.park_pct;
+  r->shade_min = sh.shade_min;
+  r->ms = ms;
+}
+
+}  // namespace
+
+// Three stages: the persistent kernel's shape alone (one launch), then epoch
+// counts and park thresholds with that shape, then wavefront round counts and
+// hand-over thresholds in front of the best of those.
 int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_result* best) {
   if (!ctx || !best) return OMG_E_INVALID;
   auto it = ctx->batches.find(id);
@@ -708,49 +779,106 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
   const uint32_t per_sm[] = {2, 4, 8};
   const uint32_t refill[] = {1, 8};
   const uint32_t walks[] = {8, 32, 0};
+  const uint32_t shade_mins[] = {1, 12, 24, 32};
+  const uint32_t rounds[] = {16, 32, 48, 64, 96, 128, 192};
+  const uint32_t tails[] = {0, 2048, 8192, 32768};
+  const uint32_t epoch_counts[] = {4, 8, 12, 16, 24};
+  const uint32_t park_pcts[] = {25, 40, 55, 70};
   cudaEvent_t e0, e1;
+  cudaStream_t cs;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  LaunchShape keep = B.shape;
+  CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  const LaunchShape keep = B.shape;
   float best_ms = 1e30f;
   LaunchShape best_shape = keep;
   int32_t rc = OMG_OK;
+  auto try_shape = [&](const LaunchShape& sh) -> int32_t {
+    B.shape = sh;
+    float ms = 0.0f;
+    int32_t r = time_trace(ctx, B, reps, cs, e0, e1, &ms);
+    if (r == OMG_OK && ms < best_ms) {
+      best_ms = ms;
+      best_shape = sh;
+    }
+    return r;
+  };
   for (uint32_t th : threads)
     for (uint32_t ps : per_sm)
       for (uint32_t rf : refill)
-        for (uint32_t wk : walks) {
-        if (th * ps > 2048) continue;
-        B.shape.block_threads = th;
-        B.shape.blocks_per_sm = ps;
-        B.shape.refill_min = rf;
-        B.shape.walk_steps = wk;
-        // warm-up, then timed repetitions on the context stream
-        if ((rc = record_launch(ctx, B, ctx->stream))) goto done;
-        if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { rc = OMG_E_DEVICE; goto done; }
-        for (uint32_t r = 0; r < reps; r++)
-          if ((rc = record_launch(ctx, B, ctx->stream))) goto done;
-        if (cudaEventRecord(e1, ctx->stream) != cudaSuccess) { rc = OMG_E_DEVICE; goto done; }
-        if ((rc = wait_event(ctx, e1, timeout_of(ctx) * (reps + 1)))) goto done;
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        ms /= reps;
-        if (ms < best_ms) {
-          best_ms = ms;
-          best_shape = B.shape;
-        }
-      }
-done:
+        for (uint32_t wk : walks)
+          for (uint32_t sm : shade_mins) {
+            if (rc || th * ps > 2048) continue;
+            LaunchShape sh;
+            sh.block_threads = th;
+            sh.blocks_per_sm = ps;
+            sh.refill_min = rf;
+            sh.walk_steps = wk;
+            sh.shade_min = sm;
+            rc = try_shape(sh);
+          }
+  const LaunchShape persistent = best_shape;
+  for (uint32_t ne : epoch_counts)
+    for (uint32_t pp : park_pcts) {
+      if (rc) continue;
+      LaunchShape sh = persistent;
+      sh.epochs = ne;
+      sh.park_pct = pp;
+      rc = try_shape(sh);
+    }
+  const LaunchShape chained = best_shape;
+  for (uint32_t nr : rounds)
+    for (uint32_t tl : tails) {
+      if (rc) continue;
+      LaunchShape sh = chained;
+      sh.wf_iters = nr;
+      sh.wf_tail = tl;
+      rc = try_shape(sh);
+    }
+  cudaStreamDestroy(cs);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   B.shape = rc == OMG_OK ? best_shape : keep;
   if (rc) return rc;
   if ((rc = build_graphs(ctx, B))) return rc;
   ctx->shape = best_shape;
-  best->block_threads = best_shape.block_threads;
-  best->blocks_per_sm = best_shape.blocks_per_sm;
-  best->refill_min = best_shape.refill_min;
-  best->walk_steps = best_shape.walk_steps;
-  best->ms = best_ms;
+  shape_to_result(best_shape, best_ms, best);
+  return OMG_OK;
+}
+
+// Set the launch shape of a batch (and the default of later batches) by hand.
+int32_t omg_batch_set_shape(omg_ctx* ctx, uint32_t id, const omg_tune_result* shape) {
+  if (!ctx || !shape) return OMG_E_INVALID;
+  auto it = ctx->batches.find(id);
+  if (it == ctx->batches.end()) return OMG_E_NOT_FOUND;
+  if (shape->block_threads == 0 || shape->block_threads % 32 != 0 || shape->block_threads > 256 ||
+      shape->blocks_per_sm == 0 || shape->block_threads * shape->blocks_per_sm > 2048 || shape->refill_min == 0 ||
+      shape->refill_min > 32 || shape->wf_rounds > 4096 || shape->epochs > kMaxEpochs || shape->park_pct > 100 ||
+      shape->shade_min > 32)
+    return OMG_E_INVALID;
+  BatchRec& B = *it->second;
+  LaunchShape sh;
+  sh.block_threads = shape->block_threads;
+  sh.blocks_per_sm = shape->blocks_per_sm;
+  sh.refill_min = shape->refill_min;
+  sh.walk_steps = shape->walk_steps;
+  sh.wf_iters = shape->wf_rounds;
+  sh.wf_tail = shape->wf_tail;
+  sh.epochs = shape->epochs;
+  sh.park_pct = shape->park_pct;
+  sh.shade_min = shape->shade_min == 0 ? 1u : shape->shade_min;
+  B.shape = sh;
+  int32_t rc = build_graphs(ctx, B);
+  if (rc) return rc;
+  ctx->shape = sh;
+  return OMG_OK;
+}
+
+int32_t omg_batch_get_shape(omg_ctx* ctx, uint32_t id, omg_tune_result* shape) {
+  if (!ctx || !shape) return OMG_E_INVALID;
+  auto it = ctx->batches.find(id);
+  if (it == ctx->batches.end()) return OMG_E_NOT_FOUND;
+  shape_to_result(it->second->shape, 0.0f, shape);
   return OMG_OK;
 }
 

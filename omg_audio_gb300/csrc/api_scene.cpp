@@ -84,6 +84,16 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
     CK(S->nodes.alloc(S->n_nodes * 4));
     if (S->n_nodes)
       CK(cudaMemcpy(S->nodes.p, dev_nodes.data(), dev_nodes.size() * 4, cudaMemcpyHostToDevice));
+    std::vector<float> dev_nodes4;
+    uint32_t need = 0;
+    S->root4 = flatten_bvh4(S->ref_boxes, S->ref_ab, dev_nodes4, &need);
+    S->n_nodes4 = (uint32_t)(dev_nodes4.size() / 32);
+    // a tree whose walks could overflow the traversal stack keeps the binary walk
+    if (need >= (uint32_t)STACK_DEPTH) S->n_nodes4 = 0;
+    if (S->n_nodes4) {
+      CK(S->nodes4.alloc((size_t)S->n_nodes4 * 8));
+      CK(cudaMemcpy(S->nodes4.p, dev_nodes4.data(), dev_nodes4.size() * 4, cudaMemcpyHostToDevice));
+    }
   } else {
     // LBVH: upload the primitives in tessellation order, build on the device
     std::vector<uint16_t> psurf(S->n_prims);

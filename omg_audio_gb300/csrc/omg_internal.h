@@ -50,7 +50,15 @@ struct DScene {
   uint32_t n_nodes;
   uint32_t n_prims;
   uint32_t n_bands;
+  // The same tree collapsed to 4 children per node (host-built scenes only;
+  // null otherwise). 128 B per node, 8 float4:
+  //   lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] ref[4] (int bits) -
+  // refs as in `nodes`; an unused child slot has ref kEmpty4 and a zero box.
+  const float4* nodes4;
+  int32_t root4;
+  uint32_t n_nodes4;
 };
+constexpr int32_t kEmpty4 = 0x7FFFFFFE;
 
 // Panel overlay (scene.rs:90-137): box, an index into the batch's material
 // table, and the panel's index in the caller's order (exact-tie rule).
@@ -115,19 +123,77 @@ inline uint64_t out_floats(uint32_t n_bins, uint32_t nb) { return 1ull * n_bins 
 
 // Launch shapes of the tracer kernel (autotuned).
 struct LaunchShape {
-  uint32_t block_threads = 128;
+  uint32_t block_threads = 256;
   uint32_t blocks_per_sm = 4;
   uint32_t refill_min = 1;      // a warp refetches rays once this many lanes are idle
   uint32_t walk_steps = 0;      // traversal steps per lane per loop iteration (0 = a whole walk)
+  uint32_t shade_min = 32;      // lanes that shade together (or every waiting lane once none walks)
+  uint32_t wf_iters = 0;        // wavefront rounds before the persistent kernel takes over (0: none)
+  uint32_t wf_tail = 0;         // ... or as soon as at most this many rays are alive
+  uint32_t epochs = 0;          // persistent-kernel epochs (0: one launch that never parks)
+  uint32_t park_pct = 50;       // an epoch parks its rays once at most this % of them remain
+  uint32_t park_min = 4096;     // epochs of at most this many rays run to the end
+};
+
+// Wavefront state (wavefront.cu). One record per ray of the batch, indexed by
+// the ray's global id, holds everything the bounce loop carries from one
+// segment to the next; two queues hold the ids of the live rays.
+struct alignas(16) WfCtl {
+  uint32_t count[2];     // queue lengths
+  uint32_t tail;         // 1 once the persistent kernel takes over
+  uint32_t tail_q;       // the queue it resumes from
+  uint32_t tail_n;       // and its length
+  uint32_t pad[3];
+};
+struct WfState {
+  float4* pos;           // p.xyz, distance travelled
+  float4* dir;           // d.xyz, ray stream state (uint bits)
+  float4* e;             // band energies 0-3 at [r], 4-7 at [cap + r]
+  uint32_t* bounce;      // segments traced so far
+  float2* hit;           // closest mesh hit: t, primitive index bits (-1: none)
+  uint32_t* queue;       // queue 0 at [0, cap), queue 1 at [cap, 2 cap)
+  WfCtl* ctl;
+  uint32_t cap;          // rays of the batch
+};
+
+// Epochs of the persistent kernel. As rays end, the lanes of the persistent
+// kernel go idle; an epoch therefore stops once few of its rays remain: every
+// lane parks its ray at the end of its current segment (state saved in the
+// WfState records, id appended to the next epoch's queue) and the next epoch
+// resumes the parked rays in full warps. One record per epoch, cleared
+// before the launch.
+struct alignas(16) EpochCtl {
+  uint32_t n;            // rays queued for this epoch (appended by the previous one)
+  uint32_t fetch;        // queue head
+  uint32_t ended;        // rays of this epoch that ended
+  uint32_t park;         // 1: park rays at their next segment end
+};
+constexpr uint32_t kMaxEpochs = 32;
+struct EpochArgs {
+  const uint32_t* in_q;  // ray ids of this epoch (cur->n of them); null: fresh rays 0 .. total_rays-1
+  uint32_t* out_q;       // the next epoch's queue; null: every ray runs to its end
+  EpochCtl* cur;         // null: a single launch (fresh rays, header ray counter, no parking)
+  EpochCtl* next;
+  uint32_t park_pct;
+  uint32_t park_min;
+  WfState st;            // per-ray records (saved and restored state)
 };
 
 // ----------------------------------------------------------- kernel launchers
-// trace.cu
+// trace.cu. `ep`: one epoch of an epoch chain (null: a single launch).
 cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
                          const DScene* scenes, const DMat* job_mats, const DPanel* panels,
                          const DPanelGroup* groups, float* acc,
                          DLaunch* hdr, uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie,
-                         cudaStream_t s);
+                         cudaStream_t s, const EpochArgs* ep = nullptr);
+// wavefront.cu: wavefront rounds (when shape.wf_iters > 0), then the
+// persistent kernel on the remaining rays, in shape.epochs epochs (ep_q: two
+// queues of st.cap ids; ep_ctl: kMaxEpochs + 1 records, cleared).
+cudaError_t launch_wavefront(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
+                             const DScene* scenes, const DMat* job_mats, const DPanel* panels,
+                             const DPanelGroup* groups, float* acc, DLaunch* hdr, uint32_t* job_segments,
+                             const WfState& st, uint32_t* ep_q, EpochCtl* ep_ctl, const LaunchShape& shape,
+                             int n_sms, bool tie, cudaStream_t s);
 cudaError_t launch_finalize(const DJob* jobs, uint32_t n_jobs, const float* acc, float* out, uint64_t total_out,
                             cudaStream_t s);
 cudaError_t launch_raycast(const DScene* scene, const float* o, const float* d, uint32_t n, float* t,

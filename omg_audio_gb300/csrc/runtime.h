@@ -61,6 +61,9 @@ struct SceneRec {
   int32_t root = 0;
   uint32_t bvh_kind = OMG_BVH_SAH;
   DevBuf<float4> nodes, prims, normals;
+  DevBuf<float4> nodes4;          // 4-wide collapse of `nodes` (host-built trees)
+  int32_t root4 = 0;
+  uint32_t n_nodes4 = 0;
   DevBuf<DMat> mats;
   DevBuf<uint16_t> tri_surface;
   // host copies for export / queries
@@ -96,6 +99,14 @@ struct BatchRec {
   PinBuf<DLaunch> h_hdr;
   PinBuf<uint32_t> h_seg;
   PinBuf<DJob> h_jobs;
+  // wavefront rounds: per-ray state, two ray-id queues, control block
+  DevBuf<float4> d_wf_pos, d_wf_dir, d_wf_e;
+  DevBuf<uint32_t> d_wf_bounce, d_wf_queue;
+  DevBuf<float2> d_wf_hit;
+  DevBuf<WfCtl> d_wf_ctl;
+  WfState wf{};
+  DevBuf<uint32_t> d_ep_q;        // epoch queues (2 x rays)
+  DevBuf<EpochCtl> d_ep_ctl;      // kMaxEpochs + 1 records
   LaunchShape shape;
   cudaGraphExec_t graph = nullptr;         // device-only launch
   cudaGraphExec_t graph_io = nullptr;      // H2D jobs + launch + D2H results

@@ -344,6 +344,89 @@ int32_t flatten_bvh2(const std::vector<float>& ref_boxes, const std::vector<uint
   return 0;
 }
 
+int32_t flatten_bvh4(const std::vector<float>& ref_boxes, const std::vector<uint32_t>& ref_ab,
+                     std::vector<float>& dev_nodes, uint32_t* max_stack) {
+  const size_t nref = ref_ab.size() / 2;
+  dev_nodes.clear();
+  *max_stack = 0;
+  if (nref == 0) return 0;
+  auto is_leaf = [&](uint32_t i) { return (ref_ab[2 * i] & kLeafBit) != 0; };
+  auto leaf_code = [&](uint32_t i) -> int32_t {
+    uint32_t start = ref_ab[2 * i] & ~kLeafBit, count = ref_ab[2 * i + 1];
+    return (int32_t)~((start << 3) | (count - 1));
+  };
+  auto area = [&](uint32_t i) {
+    const float* b = &ref_boxes[6 * i];
+    const double dx = (double)b[3] - b[0], dy = (double)b[4] - b[1], dz = (double)b[5] - b[2];
+    return dx * dy + dy * dz + dz * dx;
+  };
+  if (is_leaf(0)) return leaf_code(0);
+  // children of the 4-wide node grown from binary node i
+  auto gather = [&](uint32_t i, uint32_t* ch) -> int {
+    int n = 2;
+    ch[0] = ref_ab[2 * i];
+    ch[1] = ref_ab[2 * i + 1];
+    while (n < 4) {
+      int best = -1;
+      double ba = -1.0;
+      for (int k = 0; k < n; k++)
+        if (!is_leaf(ch[k]) && area(ch[k]) > ba) {
+          ba = area(ch[k]);
+          best = k;
+        }
+      if (best < 0) break;
+      const uint32_t c = ch[best];
+      ch[best] = ref_ab[2 * c];
+      ch[n++] = ref_ab[2 * c + 1];
+    }
+    return n;
+  };
+  // siblings get consecutive indices (numbered when their parent is written).
+  // A walk pushes at most (internal children - 1) entries per node on its
+  // path; `need` is that sum from the root, its maximum bounds the stack.
+  struct Item {
+    uint32_t ref2;
+    int32_t slot;
+    uint32_t need;
+  };
+  std::vector<Item> st{{0u, 0, 0u}};
+  int32_t next = 1;
+  dev_nodes.assign(32, 0.0f);
+  while (!st.empty()) {
+    const Item it = st.back();
+    st.pop_back();
+    uint32_t ch[4];
+    const int n = gather(it.ref2, ch);
+    int32_t refs[4];
+    uint32_t n_int = 0;
+    for (int k = 0; k < n; k++) n_int += is_leaf(ch[k]) ? 0u : 1u;
+    const uint32_t need = it.need + (n_int ? n_int - 1 : 0);
+    if (need > *max_stack) *max_stack = need;
+    const int32_t slot = it.slot;
+    for (int k = 0; k < 4; k++) {
+      if (k >= n) refs[k] = kEmpty4;
+      else if (is_leaf(ch[k])) refs[k] = leaf_code(ch[k]);
+      else {
+        refs[k] = next++;
+        st.push_back({ch[k], refs[k], need});
+      }
+    }
+    dev_nodes.resize((size_t)next * 32, 0.0f);
+    float* o = &dev_nodes[(size_t)slot * 32];
+    for (int k = 0; k < n; k++) {
+      const float* b = &ref_boxes[6 * ch[k]];
+      o[0 + k] = b[0];
+      o[4 + k] = b[3];
+      o[8 + k] = b[1];
+      o[12 + k] = b[4];
+      o[16 + k] = b[2];
+      o[20 + k] = b[5];
+    }
+    std::memcpy(&o[24], refs, sizeof(refs));
+  }
+  return 0;
+}
+
 // mesh.rs:458-461 per original triangle; .w carries the material id bits.
 void tri_normals(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
                  std::vector<float>& out) {

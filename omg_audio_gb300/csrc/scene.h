@@ -50,6 +50,12 @@ void build_sah(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, st
 // Returns the root ref; dev_nodes gets 16 floats per internal node.
 int32_t flatten_bvh2(const std::vector<float>& ref_boxes, const std::vector<uint32_t>& ref_ab,
                      std::vector<float>& dev_nodes);
+// The same tree with every node's children opened (largest surface area
+// first) until it has 4: returns the root ref; dev_nodes gets 32 floats per
+// node in the DScene::nodes4 layout; max_stack: the deepest traversal stack a
+// walk of it can need.
+int32_t flatten_bvh4(const std::vector<float>& ref_boxes, const std::vector<uint32_t>& ref_ab,
+                     std::vector<float>& dev_nodes, uint32_t* max_stack);
 void tri_normals(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
                  std::vector<float>& out);
 DMat make_dmat(const omg_material& m, uint32_t nb);

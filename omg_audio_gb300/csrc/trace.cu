@@ -6,10 +6,15 @@
 // one iteration of the reference's bounce loop (tracer.rs:103-200): closest
 // hit, receiver test, then absorb / transmit / scatter.
 //
+// The same kernel also finishes the rays that the wavefront rounds
+// (wavefront.cu) leave alive: it then takes ray ids from the tail queue and
+// restores each ray's state instead of starting it.
+//
 // Arithmetic follows the reference's f32 operation order term by term and
 // this file is compiled with -fmad=false, so every f32 result rounds exactly
-// as the reference's (and the f32 oracle's) does. The only transcendental,
-// cos/sin of the Lambert azimuth, is evaluated in double and rounded once.
+// as the reference's (and the f32 oracle's) does. The only transcendentals,
+// cos/sin of the sphere azimuth, come from the f32 sincos of
+// device_common.cuh, which the f32 oracle evaluates identically.
 #include "shade_common.cuh"
 
 namespace omg {
@@ -186,7 +191,18 @@ __device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, f
 // closest-hit walk ends shades its segment and starts the next one at once,
 // while the other lanes of its warp keep walking: per loop iteration a lane
 // takes at most `walk_steps` traversal steps, then shades if its walk is done.
-// Idle lanes refill from the global ray queue.
+// Idle lanes refill from the global ray queue. Walking and shading alternate
+// per warp: lanes whose walk is done wait until `shade_min` of them can shade
+// together (or nothing else is walking), so the shading code, which is long,
+// does not run once per lane.
+//
+// In an epoch chain (ea.cur set) the queue is this epoch's: fresh rays, or
+// parked rays whose state is restored from the per-ray records. Once at most
+// park_pct % of the epoch's rays remain and its queue is drained, each lane
+// parks its ray at the end of its current segment, so that the next epoch
+// runs the survivors in full warps. An epoch whose park signal is never
+// raised (it ended too few rays while rays were still queued) runs its rays
+// to their end, which is only slower.
 template <int NB, bool TIE>
 __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
                                                        uint32_t total_rays, const DScene* __restrict__ scenes,
@@ -194,14 +210,15 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
                                                        const DPanel* __restrict__ panels,
                                                        const DPanelGroup* __restrict__ groups, float* __restrict__ acc,
                                                     DLaunch* __restrict__ hdr, uint32_t* __restrict__ job_segments,
-                                                    uint32_t refill_min, int walk_budget) {
+                                                    uint32_t refill_min, int walk_budget, uint32_t shade_min,
+                                                    EpochArgs ea) {
   const unsigned FULL = 0xffffffffu;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt_mask = (1u << lane) - 1u;
   enum { IDLE = 0, WALK = 1, SHADE = 2 };
   int phase = IDLE;
   bool exhausted = false;
-  uint32_t ji = 0;
+  uint32_t ji = 0, rid = 0;
   float px = 0, py = 0, pz = 0, dx = 0, dy = 0, dz = 0, dist = 0;
   float e[NB];
 #pragma unroll
@@ -217,6 +234,13 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
   Hit h;
   bool have = false;
   uint32_t* err = &hdr->error;
+  const WfState& rs = ea.st;
+  const uint32_t* rq = ea.in_q;
+  const uint32_t n_rays = ea.cur ? (rq ? ea.cur->n : total_rays) : total_rays;
+  uint32_t* fetch = ea.cur ? &ea.cur->fetch : &hdr->ray_counter;
+  const bool may_park = ea.cur && ea.out_q && n_rays > ea.park_min;
+  const uint32_t keep = (uint32_t)(((uint64_t)n_rays * ea.park_pct) / 100u);
+  bool parking = false;
 
   // begin one segment from (p, d): the box hit directly, or a mesh walk
   auto begin_segment = [&](const DJob& J) {
@@ -232,27 +256,44 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
   };
 
   while (true) {
-    // ---- refill idle lanes from the global ray queue (warp-aggregated)
+    // ---- refill idle lanes from the ray queue (warp-aggregated)
     const unsigned idle = __ballot_sync(FULL, phase == IDLE);
     if (!exhausted && idle != 0u && (__popc(idle) >= (int)refill_min || idle == FULL)) {
       uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(&hdr->ray_counter, (uint32_t)__popc(idle));
+      if (lane == 0) base = atomicAdd(fetch, (uint32_t)__popc(idle));
       base = __shfl_sync(FULL, base, 0);
-      if (base >= total_rays) exhausted = true;
+      if (base >= n_rays) exhausted = true;
       if (phase == IDLE) {
-        const uint32_t r = base + (uint32_t)__popc(idle & lt_mask);
-        if (r < total_rays) {
-          ji = find_job(jobs, n_jobs, r);
-          const DJob& J = jobs[ji];
-          rng.init(J.seed, r - J.ray_base);
-          unit_sphere(rng, dx, dy, dz);
-          px = J.src[0]; py = J.src[1]; pz = J.src[2];
+        const uint32_t k = base + (uint32_t)__popc(idle & lt_mask);
+        if (k < n_rays) {
+          if (rq) {
+            rid = rq[k];
+            ji = find_job(jobs, n_jobs, rid);
+            const float4 P = rs.pos[rid], D = rs.dir[rid];
+            px = P.x; py = P.y; pz = P.z; dist = P.w;
+            dx = D.x; dy = D.y; dz = D.z;
+            rng.s = __float_as_uint(D.w);
+            const float4 e0 = rs.e[rid];
+            const float4 e1 = NB > 4 ? rs.e[rs.cap + rid] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const float ev[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
 #pragma unroll
-          for (int b = 0; b < NB; b++) e[b] = J.e0[b];
-          dist = 0.0f;
-          bounce = 0;
-          segs = 0;
-          begin_segment(J);
+            for (int b = 0; b < NB; b++) e[b] = ev[b];
+            bounce = rs.bounce[rid];
+            segs = bounce;
+          } else {
+            rid = k;
+            ji = find_job(jobs, n_jobs, rid);
+            const DJob& J = jobs[ji];
+            rng.init(J.seed, rid - J.ray_base);
+            unit_sphere(rng, dx, dy, dz);
+            px = J.src[0]; py = J.src[1]; pz = J.src[2];
+#pragma unroll
+            for (int b = 0; b < NB; b++) e[b] = J.e0[b];
+            dist = 0.0f;
+            bounce = 0;
+            segs = 0;
+          }
+          begin_segment(jobs[ji]);
         }
       }
     }
@@ -260,9 +301,18 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
       if (exhausted) break;
       continue;
     }
+    // the epoch's park signal (sticky; raised only once its queue is drained)
+    if (may_park && !parking) parking = *((volatile const uint32_t*)&ea.cur->park) != 0u;
+
+    // ---- this iteration either shades or walks, for the whole warp: lanes
+    // whose walk is done wait until at least shade_min of them are ready (or
+    // no lane is walking), so that the shading code runs with full lanes
+    const unsigned walking = __ballot_sync(FULL, phase == WALK);
+    const unsigned ready = __ballot_sync(FULL, phase == SHADE);
+    const bool shade_now = ready != 0u && (walking == 0u || __popc(ready) >= (int)shade_min);
 
     // ---- closest-hit walk, at most walk_budget steps this iteration
-    if (phase == WALK) {
+    if (!shade_now && phase == WALK) {
       const DJob& J = jobs[ji];
       const DScene& S = scenes[J.scene];
       if (walk_steps<TIE>(w, S, px, py, pz, dx, dy, dz, walk_budget, err)) {
@@ -282,22 +332,53 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
         phase = SHADE;
       }
     }
-    if (phase != SHADE) continue;
 
     // ---- one segment of the bounce loop (tracer.rs:103-200)
-    const DJob& J = jobs[ji];
-    if (J.n_groups) have = panels_hit(J, panels, groups, job_mats, px, py, pz, dx, dy, dz, have, h);
-    segs++;
-    const float t_hit = have ? h.t : FLT_MAX;
-
-    bool done = shade_segment<NB>(J, acc, h, have, t_hit, px, py, pz, dx, dy, dz, dist, e, rng);
-    bounce++;
-    if (!done && bounce >= J.max_bounces) done = true;
-    if (done) {
-      atomicAdd(job_segments + ji, segs);
-      phase = IDLE;
-    } else {
-      begin_segment(J);
+    bool ended = false, parked = false;
+    if (shade_now && phase == SHADE) {
+      const DJob& J = jobs[ji];
+      if (J.n_groups) have = panels_hit(J, panels, groups, job_mats, px, py, pz, dx, dy, dz, have, h);
+      segs++;
+      const float t_hit = have ? h.t : FLT_MAX;
+      bool done = shade_segment<NB>(J, acc, h, have, t_hit, px, py, pz, dx, dy, dz, dist, e, rng);
+      bounce++;
+      if (!done && bounce >= J.max_bounces) done = true;
+      if (done) {
+        atomicAdd(job_segments + ji, segs);
+        phase = IDLE;
+        ended = true;
+      } else if (parking) {
+        // save the ray between two segments; the next epoch restores it
+        rs.pos[rid] = make_float4(px, py, pz, dist);
+        rs.dir[rid] = make_float4(dx, dy, dz, __uint_as_float(rng.s));
+        float v[8];
+#pragma unroll
+        for (int b = 0; b < 8; b++) v[b] = b < NB ? e[b] : 0.0f;
+        rs.e[rid] = make_float4(v[0], v[1], v[2], v[3]);
+        if (NB > 4) rs.e[rs.cap + rid] = make_float4(v[4], v[5], v[6], v[7]);
+        rs.bounce[rid] = bounce;
+        phase = IDLE;
+        parked = true;
+      } else {
+        begin_segment(J);
+      }
+    }
+    if (ea.cur) {
+      // warp-aggregated: count the ended rays (and raise the park signal),
+      // append the parked ones to the next epoch's queue
+      const unsigned em = __ballot_sync(FULL, ended);
+      if (em && lane == (uint32_t)(__ffs(em) - 1)) {
+        const uint32_t done_now = atomicAdd(&ea.cur->ended, (uint32_t)__popc(em)) + (uint32_t)__popc(em);
+        if (may_park && n_rays - done_now <= keep && *((volatile const uint32_t*)fetch) >= n_rays)
+          *((volatile uint32_t*)&ea.cur->park) = 1u;
+      }
+      const unsigned pm = __ballot_sync(FULL, parked);
+      if (pm) {
+        uint32_t base = 0;
+        if (lane == (uint32_t)(__ffs(pm) - 1)) base = atomicAdd(&ea.next->n, (uint32_t)__popc(pm));
+        base = __shfl_sync(FULL, base, __ffs(pm) - 1);
+        if (parked) ea.out_q[base + (uint32_t)__popc(pm & lt_mask)] = rid;
+      }
     }
   }
 }
@@ -328,8 +409,10 @@ __global__ void raycast_kernel(const DScene* __restrict__ scene, const float* __
   const DScene S = *scene;
   float t;
   int prim = 0;
-  bool have = mesh_closest<TIE>(S, o[3 * i], o[3 * i + 1], o[3 * i + 2], d[3 * i], d[3 * i + 1], d[3 * i + 2], t,
-                                prim, &hdr->error);
+  const float ox = o[3 * i], oy = o[3 * i + 1], oz = o[3 * i + 2];
+  const float dx = d[3 * i], dy = d[3 * i + 1], dz = d[3 * i + 2];
+  bool have = (TIE && S.nodes4) ? mesh_closest4(S, ox, oy, oz, dx, dy, dz, t, prim, &hdr->error)
+                                : mesh_closest<TIE>(S, ox, oy, oz, dx, dy, dz, t, prim, &hdr->error);
   if (have) {
     t_out[i] = t;
     tri_out[i] = __float_as_uint(__ldg(S.prims + 3 * prim + 1).w);
@@ -344,8 +427,11 @@ __global__ void raycast_kernel(const DScene* __restrict__ scene, const float* __
 cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
                          const DScene* scenes, const DMat* job_mats, const DPanel* panels,
                          const DPanelGroup* groups, float* acc, DLaunch* hdr,
-                         uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie, cudaStream_t s) {
+                         uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie, cudaStream_t s,
+                         const EpochArgs* ep) {
   if (n_jobs == 0 || total_rays == 0) return cudaSuccess;
+  EpochArgs ea{};
+  if (ep) ea = *ep;
   uint32_t threads = shape.block_threads;
   uint64_t want = (uint64_t)n_sms * shape.blocks_per_sm;
   uint64_t need = ((uint64_t)total_rays + threads - 1) / threads;
@@ -353,10 +439,11 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
   if (blocks == 0) blocks = 1;
   uint32_t refill = shape.refill_min == 0 ? 1 : (shape.refill_min > 32 ? 32 : shape.refill_min);
   const int steps = shape.walk_steps == 0 ? 1000000 : (int)shape.walk_steps;
+  const uint32_t shade_min = shape.shade_min == 0 ? 1u : (shape.shade_min > 32 ? 32u : shape.shade_min);
 #define OMG_TRACE_LAUNCH(NB, TIE)                                                                        \
   trace_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, groups, \
                                                    acc, hdr, \
-                                                   job_segments, refill, steps)
+                                                   job_segments, refill, steps, shade_min, ea)
   if (max_nb <= 3) {
     if (tie) OMG_TRACE_LAUNCH(3, true);
     else OMG_TRACE_LAUNCH(3, false);

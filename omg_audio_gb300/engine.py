@@ -366,11 +366,27 @@ class Batch:
         self.ctx._check(lib().omg_batch_kernel_count(self.ctx.h, self.id, C.byref(n)), "omg_batch_kernel_count")
         return n.value
 
-    def autotune(self, reps: int = 2):
+    @staticmethod
+    def _shape_dict(r) -> dict:
+        return {k: getattr(r, k) for k, _ in _lib.omg_tune_result._fields_}
+
+    def autotune(self, reps: int = 2) -> dict:
+        """Time launch shapes on this batch and keep the fastest (omg_batch_autotune)."""
         r = _lib.omg_tune_result()
         self.ctx._check(lib().omg_batch_autotune(self.ctx.h, self.id, reps, C.byref(r)), "omg_batch_autotune")
-        return dict(block_threads=r.block_threads, blocks_per_sm=r.blocks_per_sm, refill_min=r.refill_min,
-                    walk_steps=r.walk_steps, ms=r.ms)
+        return self._shape_dict(r)
+
+    def shape(self) -> dict:
+        r = _lib.omg_tune_result()
+        self.ctx._check(lib().omg_batch_get_shape(self.ctx.h, self.id, C.byref(r)), "omg_batch_get_shape")
+        return self._shape_dict(r)
+
+    def set_shape(self, **kw):
+        """Set launch-shape fields by name (the others keep their values)."""
+        cur = self.shape()
+        cur.update(kw)
+        r = _lib.omg_tune_result(**{k: cur[k] for k, _ in _lib.omg_tune_result._fields_})
+        self.ctx._check(lib().omg_batch_set_shape(self.ctx.h, self.id, C.byref(r)), "omg_batch_set_shape")
 
     def destroy(self):
         if self.id:
