@@ -278,6 +278,9 @@ typedef struct omg_tune_result {
     uint32_t refill_min;         /* a warp refills from the ray queue once this many lanes idle */
     uint32_t walk_steps;         /* traversal steps per lane per loop iteration (0 = whole walk) */
     uint32_t shade_min;          /* lanes of a warp that shade together (1..32; 0 reads as 1) */
+    uint32_t mode;               /* persistent kernel: 0 per-lane state machine, 1 warp-local wavefront
+                                    (walks refill lane by lane; rays shade 32 at a time) */
+    uint32_t wide;               /* 1: persistent walks use the 4-wide tree (tie_mode 1, host-built trees) */
     uint32_t wf_rounds;          /* wavefront rounds before the persistent kernel (0 = none) */
     uint32_t wf_tail;            /* hand over to the persistent kernel at <= this many live rays */
     uint32_t epochs;             /* persistent-kernel epochs, <= 32 (0 = one launch) */

@@ -381,7 +381,8 @@ int32_t prepare_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n
 
 int32_t check_kernel_flags(omg_ctx* ctx, const BatchRec& B) {
   if (B.h_hdr.p->error) {
-    ctx->last_error = "trace kernel: traversal stack or walk budget exceeded";
+    ctx->last_error = "trace kernel: traversal stack, walk budget or loop guard exceeded (flags " +
+                      std::to_string(B.h_hdr.p->error) + ")";
     return OMG_E_OVERFLOW;
   }
   return OMG_OK;
@@ -761,6 +762,8 @@ void shape_to_result(const LaunchShape& sh, float ms, omg_tune_result* r) {
   r->epochs = sh.epochs;
   r->park_pct = sh.park_pct;
   r->shade_min = sh.shade_min;
+  r->mode = sh.mode;
+  r->wide = sh.wide;
   r->ms = ms;
 }
 
@@ -775,11 +778,12 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
   if (it == ctx->batches.end()) return OMG_E_NOT_FOUND;
   BatchRec& B = *it->second;
   if (reps == 0) reps = 3;
-  const uint32_t threads[] = {64, 128, 256};
+  const uint32_t threads[] = {128, 256};
   const uint32_t per_sm[] = {2, 4, 8};
   const uint32_t refill[] = {1, 8};
-  const uint32_t walks[] = {8, 32, 0};
-  const uint32_t shade_mins[] = {1, 12, 24, 32};
+  const uint32_t walks[] = {0, 8, 32};
+  const uint32_t shade_mins[] = {1, 16, 32};
+  const uint32_t wl_walks[] = {0, 4, 8, 16, 32};
   const uint32_t rounds[] = {16, 32, 48, 64, 96, 128, 192};
   const uint32_t tails[] = {0, 2048, 8192, 32768};
   const uint32_t epoch_counts[] = {4, 8, 12, 16, 24};
@@ -804,7 +808,7 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
     return r;
   };
   for (uint32_t th : threads)
-    for (uint32_t ps : per_sm)
+    for (uint32_t ps : per_sm) {
       for (uint32_t rf : refill)
         for (uint32_t wk : walks)
           for (uint32_t sm : shade_mins) {
@@ -817,6 +821,16 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
             sh.shade_min = sm;
             rc = try_shape(sh);
           }
+      for (uint32_t wk : wl_walks) {
+        if (rc || th * ps > 2048) continue;
+        LaunchShape sh;
+        sh.mode = 1;
+        sh.block_threads = th;
+        sh.blocks_per_sm = ps;
+        sh.walk_steps = wk;
+        rc = try_shape(sh);
+      }
+    }
   const LaunchShape persistent = best_shape;
   for (uint32_t ne : epoch_counts)
     for (uint32_t pp : park_pcts) {
@@ -854,7 +868,7 @@ int32_t omg_batch_set_shape(omg_ctx* ctx, uint32_t id, const omg_tune_result* sh
   if (shape->block_threads == 0 || shape->block_threads % 32 != 0 || shape->block_threads > 256 ||
       shape->blocks_per_sm == 0 || shape->block_threads * shape->blocks_per_sm > 2048 || shape->refill_min == 0 ||
       shape->refill_min > 32 || shape->wf_rounds > 4096 || shape->epochs > kMaxEpochs || shape->park_pct > 100 ||
-      shape->shade_min > 32)
+      shape->shade_min > 32 || shape->mode > 1)
     return OMG_E_INVALID;
   BatchRec& B = *it->second;
   LaunchShape sh;
@@ -867,6 +881,8 @@ int32_t omg_batch_set_shape(omg_ctx* ctx, uint32_t id, const omg_tune_result* sh
   sh.epochs = shape->epochs;
   sh.park_pct = shape->park_pct;
   sh.shade_min = shape->shade_min == 0 ? 1u : shape->shade_min;
+  sh.mode = shape->mode;
+  sh.wide = shape->wide ? 1u : 0u;
   B.shape = sh;
   int32_t rc = build_graphs(ctx, B);
   if (rc) return rc;

@@ -303,84 +303,90 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
 // independent of the visit order and a box is skipped only beyond
 // best * (1 + 1e-6), the hit is the one the binary walk finds (up to chains of
 // near-ties, which neither walk orders the reference's way).
+//
+// One node step; returns the next node, or kDone4 once the stack is empty.
+constexpr int kDone4 = 0x7FFFFFFF;
+__device__ __forceinline__ int bvh4_step(const float4* __restrict__ nodes, const float4* __restrict__ prims, int cur,
+                                         float ox, float oy, float oz, float dx, float dy, float dz, float ix,
+                                         float iy, float iz, bool& have, float& t_best, float& t_cull,
+                                         int& prim_best, uint32_t& s_best, uint32_t& tri_best, int* stack_ref,
+                                         float* stack_t, int& sp, uint32_t* err) {
+  const float4* nd = nodes + 8 * cur;
+  const float4 lx = __ldg(nd + 0), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
+  const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5), rf = __ldg(nd + 6);
+  const float tmax = have ? t_cull : FLT_MAX;
+  const float blx[4] = {lx.x, lx.y, lx.z, lx.w}, bhx[4] = {hx.x, hx.y, hx.z, hx.w};
+  const float bly[4] = {ly.x, ly.y, ly.z, ly.w}, bhy[4] = {hy.x, hy.y, hy.z, hy.w};
+  const float blz[4] = {lz.x, lz.y, lz.z, lz.w}, bhz[4] = {hz.x, hz.y, hz.z, hz.w};
+  const int ref[4] = {__float_as_int(rf.x), __float_as_int(rf.y), __float_as_int(rf.z), __float_as_int(rf.w)};
+  float t[4];
+  int r[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    float tk;
+    const bool h = ref[k] != kEmpty4 &&
+                   ray_aabb(blx[k], bly[k], blz[k], bhx[k], bhy[k], bhz[k], ox, oy, oz, ix, iy, iz, tmax, tk);
+    t[k] = h ? tk : FLT_MAX;
+    r[k] = h ? ref[k] : kDone4;
+  }
+  // leaves first, nearest first
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    int bk = -1;
+    float bt = FLT_MAX;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (r[j] < 0 && t[j] <= bt) { bt = t[j]; bk = j; }
+    if (bk < 0) break;
+    if (!have || bt <= t_cull)
+      leaf_test<true>(prims, r[bk], ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best);
+    r[bk] = kDone4;
+    t[bk] = FLT_MAX;
+  }
+  // internal children by entry distance (sorting network): the nearest is
+  // the next node, the others are pushed farthest first
+  auto cswap = [&](int a, int b) {
+    if (t[b] < t[a]) {
+      const float tt = t[a]; t[a] = t[b]; t[b] = tt;
+      const int rr = r[a]; r[a] = r[b]; r[b] = rr;
+    }
+  };
+  cswap(0, 1); cswap(2, 3); cswap(0, 2); cswap(1, 3); cswap(1, 2);
+#pragma unroll
+  for (int k = 3; k >= 1; k--) {
+    if (r[k] == kDone4 || (have && t[k] > t_cull)) continue;
+    if (sp < STACK_DEPTH) { stack_ref[sp] = r[k]; stack_t[sp] = t[k]; sp++; }
+    else atomicOr(err, 1u);
+  }
+  int nxt = (r[0] == kDone4 || (have && t[0] > t_cull)) ? kDone4 : r[0];
+  while (nxt == kDone4 && sp > 0) {
+    sp--;
+    if (have && stack_t[sp] > t_cull) continue;
+    nxt = stack_ref[sp];
+  }
+  return nxt;
+}
+
 __device__ __forceinline__ bool mesh_closest4(const DScene& S, float ox, float oy, float oz, float dx, float dy,
                                               float dz, float& t_best, int& prim_best, uint32_t* err) {
   t_best = FLT_MAX;
   if (S.n_prims == 0) return false;
-  constexpr int kDone = 0x7FFFFFFF;
   const float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
-  const float4* __restrict__ nodes = S.nodes4;
-  const float4* __restrict__ prims = S.prims;
   bool have = false;
   float t_cull = FLT_MAX;
   uint32_t s_best = 0, tri_best = 0;
-  int cur = S.root4;
-  if (cur < 0) {
-    leaf_test<true>(prims, cur, ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best);
-    return have;
-  }
   int stack_ref[STACK_DEPTH];
   float stack_t[STACK_DEPTH];
   int sp = 0;
+  int cur = S.root4;
   uint32_t budget = S.n_nodes4 + 1u;   // every node is entered at most once
-  while (cur != kDone) {
+  while (cur != kDone4) {
     if (budget-- == 0u) {
       atomicOr(err, 4u);
       return have;
     }
-    const float4* nd = nodes + 8 * cur;
-    const float4 lx = __ldg(nd + 0), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
-    const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5), rf = __ldg(nd + 6);
-    const float tmax = have ? t_cull : FLT_MAX;
-    const float blx[4] = {lx.x, lx.y, lx.z, lx.w}, bhx[4] = {hx.x, hx.y, hx.z, hx.w};
-    const float bly[4] = {ly.x, ly.y, ly.z, ly.w}, bhy[4] = {hy.x, hy.y, hy.z, hy.w};
-    const float blz[4] = {lz.x, lz.y, lz.z, lz.w}, bhz[4] = {hz.x, hz.y, hz.z, hz.w};
-    const int ref[4] = {__float_as_int(rf.x), __float_as_int(rf.y), __float_as_int(rf.z), __float_as_int(rf.w)};
-    float t[4];
-    int r[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      float tk;
-      const bool h = ref[k] != kEmpty4 &&
-                     ray_aabb(blx[k], bly[k], blz[k], bhx[k], bhy[k], bhz[k], ox, oy, oz, ix, iy, iz, tmax, tk);
-      t[k] = h ? tk : FLT_MAX;
-      r[k] = h ? ref[k] : kDone;
-    }
-    // leaves first, nearest first
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      int bk = -1;
-      float bt = FLT_MAX;
-#pragma unroll
-      for (int j = 0; j < 4; j++)
-        if (r[j] < 0 && t[j] <= bt) { bt = t[j]; bk = j; }
-      if (bk < 0) break;
-      if (!have || bt <= t_cull)
-        leaf_test<true>(prims, r[bk], ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best);
-      r[bk] = kDone;
-      t[bk] = FLT_MAX;
-    }
-    // internal children by entry distance (sorting network): the nearest is
-    // the next node, the others are pushed farthest first
-    auto cswap = [&](int a, int b) {
-      if (t[b] < t[a]) {
-        const float tt = t[a]; t[a] = t[b]; t[b] = tt;
-        const int rr = r[a]; r[a] = r[b]; r[b] = rr;
-      }
-    };
-    cswap(0, 1); cswap(2, 3); cswap(0, 2); cswap(1, 3); cswap(1, 2);
-#pragma unroll
-    for (int k = 3; k >= 1; k--) {
-      if (r[k] == kDone || (have && t[k] > t_cull)) continue;
-      if (sp < STACK_DEPTH) { stack_ref[sp] = r[k]; stack_t[sp] = t[k]; sp++; }
-      else atomicOr(err, 1u);
-    }
-    cur = (r[0] == kDone || (have && t[0] > t_cull)) ? kDone : r[0];
-    while (cur == kDone && sp > 0) {
-      sp--;
-      if (have && stack_t[sp] > t_cull) continue;
-      cur = stack_ref[sp];
-    }
+    cur = bvh4_step(S.nodes4, S.prims, cur, ox, oy, oz, dx, dy, dz, ix, iy, iz, have, t_best, t_cull, prim_best,
+                    s_best, tri_best, stack_ref, stack_t, sp, err);
   }
   return have;
 }

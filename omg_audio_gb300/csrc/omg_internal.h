@@ -112,7 +112,8 @@ struct alignas(16) DJob {
 // Per-launch header in device memory (scratch: cleared before every launch).
 struct alignas(16) DLaunch {
   uint32_t ray_counter;   // persistent-queue head
-  uint32_t error;         // kernel flags: 1 stack overflow, 2 crossing list overflow, 4 walk budget
+  uint32_t error;         // kernel flags: 1 stack overflow, 2 crossing list overflow, 4 walk budget,
+                          // 8 persistent-kernel loop guard
   uint32_t pad[2];
 };
 
@@ -128,6 +129,8 @@ struct LaunchShape {
   uint32_t refill_min = 1;      // a warp refetches rays once this many lanes are idle
   uint32_t walk_steps = 0;      // traversal steps per lane per loop iteration (0 = a whole walk)
   uint32_t shade_min = 32;      // lanes that shade together (or every waiting lane once none walks)
+  uint32_t mode = 0;            // persistent kernel: 0 lane state machine, 1 warp-local wavefront
+  uint32_t wide = 0;            // persistent walks on the 4-wide tree (near-tie rule only)
   uint32_t wf_iters = 0;        // wavefront rounds before the persistent kernel takes over (0: none)
   uint32_t wf_tail = 0;         // ... or as soon as at most this many rays are alive
   uint32_t epochs = 0;          // persistent-kernel epochs (0: one launch that never parks)

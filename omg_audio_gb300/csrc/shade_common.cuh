@@ -1,6 +1,7 @@
-// Shading helpers shared by the megakernel (trace.cu) and the wavefront
-// kernels (wavefront.cu): compensated histogram adds, the shoebox hit, the
-// panel overlay test and the ray-to-job lookup.
+// Shading helpers shared by the persistent kernels (trace.cu) and the
+// wavefront kernels (wavefront.cu): compensated histogram adds, the shoebox
+// hit, the panel overlay test, the ray-to-job lookup and the shading of a ray
+// from its saved state.
 #pragma once
 #include "device_common.cuh"
 
@@ -233,6 +234,94 @@ __device__ __forceinline__ bool shade_segment(const DJob& J, float* __restrict__
     }
   }
   return done;
+}
+
+// One segment of ray r from its saved state (WfState records): the closest
+// hit (a mesh hit saved by the walk, or the analytic shoebox), the panels,
+// then shade_segment. A surviving ray's state is stored back and true is
+// returned; a finished ray adds its segment count to its job.
+template <int NB>
+__device__ __forceinline__ bool shade_saved_ray(const DJob* __restrict__ jobs, uint32_t n_jobs,
+                                                const DScene* __restrict__ scenes,
+                                                const DMat* __restrict__ job_mats,
+                                                const DPanel* __restrict__ panels,
+                                                const DPanelGroup* __restrict__ groups, float* __restrict__ acc,
+                                                const WfState& st, uint32_t r,
+                                                uint32_t* __restrict__ job_segments) {
+  const uint32_t ji = find_job(jobs, n_jobs, r);
+  const DJob& J = jobs[ji];
+  const float4 P = st.pos[r], D = st.dir[r];
+  float px = P.x, py = P.y, pz = P.z, dist = P.w;
+  float dx = D.x, dy = D.y, dz = D.z;
+  Pcg rng;
+  rng.s = __float_as_uint(D.w);
+  float e[NB];
+  {
+    const float4 e0 = st.e[r];
+    const float4 e1 = NB > 4 ? st.e[st.cap + r] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float ev[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
+#pragma unroll
+    for (int b = 0; b < NB; b++) e[b] = ev[b];
+  }
+  uint32_t bounce = st.bounce[r];
+  Hit h;
+  h.t = FLT_MAX;
+  h.m = nullptr;
+  bool have;
+  if (J.geom == OMG_GEOM_BOX) {
+    have = box_hit(J, job_mats, px, py, pz, dx, dy, dz, h);
+  } else {
+    const float2 H = st.hit[r];
+    const int prim = __float_as_int(H.y);
+    have = prim >= 0;
+    if (have) {
+      const DScene& S = scenes[J.scene];
+      const float4 p0 = __ldg(S.prims + 3 * prim + 0);
+      const float4 p1 = __ldg(S.prims + 3 * prim + 1);
+      const float4 nn = __ldg(S.normals + __float_as_uint(p1.w));
+      float nx = nn.x, ny = nn.y, nz = nn.z;
+      if (nx * dx + ny * dy + nz * dz > 0.0f) { nx = nx * -1.0f; ny = ny * -1.0f; nz = nz * -1.0f; }
+      h.t = H.x;
+      h.nx = nx; h.ny = ny; h.nz = nz;
+      h.m = S.mats + __float_as_uint(p0.w);
+    }
+  }
+  if (J.n_groups) have = panels_hit(J, panels, groups, job_mats, px, py, pz, dx, dy, dz, have, h);
+  const float t_hit = have ? h.t : FLT_MAX;
+  bool done = shade_segment<NB>(J, acc, h, have, t_hit, px, py, pz, dx, dy, dz, dist, e, rng);
+  bounce++;
+  if (!done && bounce >= J.max_bounces) done = true;
+  if (done) {
+    atomicAdd(job_segments + ji, bounce);
+    return false;
+  }
+  st.pos[r] = make_float4(px, py, pz, dist);
+  st.dir[r] = make_float4(dx, dy, dz, __uint_as_float(rng.s));
+  float v[8];
+#pragma unroll
+  for (int b = 0; b < 8; b++) v[b] = b < NB ? e[b] : 0.0f;
+  st.e[r] = make_float4(v[0], v[1], v[2], v[3]);
+  if (NB > 4) st.e[st.cap + r] = make_float4(v[4], v[5], v[6], v[7]);
+  st.bounce[r] = bounce;
+  return true;
+}
+
+// A fresh ray's saved state (tracer.rs:96-102): stream, direction, source,
+// energies, no segment yet.
+template <int NB>
+__device__ __forceinline__ void start_saved_ray(const DJob& J, const WfState& st, uint32_t r) {
+  Pcg rng;
+  rng.init(J.seed, r - J.ray_base);
+  float dx, dy, dz;
+  unit_sphere(rng, dx, dy, dz);
+  st.pos[r] = make_float4(J.src[0], J.src[1], J.src[2], 0.0f);
+  st.dir[r] = make_float4(dx, dy, dz, __uint_as_float(rng.s));
+  float v[8];
+#pragma unroll
+  for (int b = 0; b < 8; b++) v[b] = b < NB ? J.e0[b] : 0.0f;
+  st.e[r] = make_float4(v[0], v[1], v[2], v[3]);
+  if (NB > 4) st.e[st.cap + r] = make_float4(v[4], v[5], v[6], v[7]);
+  st.bounce[r] = 0;
 }
 
 }  // namespace omg

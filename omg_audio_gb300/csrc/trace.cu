@@ -40,6 +40,10 @@ struct Walk {
 };
 
 constexpr int kDone = 0x7FFFFFFF;  // never a node index (< 2^28)
+// Loop iterations of one warp of a persistent kernel before it gives up and
+// flags error 8: far above any legitimate count (each iteration advances a
+// walk, a shading pass or the ray queue).
+constexpr uint32_t kMaxLoop = 1u << 22;
 
 template <bool TIE>
 __device__ __forceinline__ int walk_pop(Walk& w) {
@@ -51,8 +55,11 @@ __device__ __forceinline__ int walk_pop(Walk& w) {
   return kDone;
 }
 
-__device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float dx, float dy, float dz) {
-  w.cur = S.n_prims ? S.root : kDone;
+template <bool TIE>
+__device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float dx, float dy, float dz, bool wide) {
+  // the 4-wide tree (when asked for, and the scene has one) where the
+  // near-tie rule lets the visit order differ
+  w.cur = S.n_prims ? ((TIE && wide && S.nodes4) ? S.root4 : S.root) : kDone;
   w.leaf = 0;
   w.sp = 0;
   w.have = false;
@@ -67,10 +74,26 @@ __device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float dx, f
   w.budget = 2u * S.n_nodes + S.n_prims + 64u;
 }
 
+// Up to `steps` node steps of the 4-wide walk (mesh_closest4 in pieces).
+__device__ __forceinline__ bool walk4_steps(Walk& w, const DScene& S, float ox, float oy, float oz, float dx,
+                                            float dy, float dz, int steps, uint32_t* err) {
+  while (steps-- > 0 && w.cur != kDone) {
+    if (w.budget-- == 0u) {
+      atomicOr(err, 4u);
+      w.cur = kDone;
+      break;
+    }
+    w.cur = bvh4_step(S.nodes4, S.prims, w.cur, ox, oy, oz, dx, dy, dz, w.ix, w.iy, w.iz, w.have, w.t_best,
+                      w.t_cull, w.prim_best, w.s_best, w.tri_best, w.stack_ref, w.stack_t, w.sp, err);
+  }
+  return w.cur == kDone;
+}
+
 // Up to `steps` node visits / leaf tests; returns true when the walk is done.
 template <bool TIE>
 __device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, float oy, float oz, float dx,
-                                           float dy, float dz, int steps, uint32_t* err) {
+                                           float dy, float dz, int steps, bool wide, uint32_t* err) {
+  if (TIE && wide && S.nodes4) return walk4_steps(w, S, ox, oy, oz, dx, dy, dz, steps, err);
   const float4* __restrict__ nodes = S.nodes;
   const float4* __restrict__ prims = S.prims;
   if (!TIE) {
@@ -211,7 +234,7 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
                                                        const DPanelGroup* __restrict__ groups, float* __restrict__ acc,
                                                     DLaunch* __restrict__ hdr, uint32_t* __restrict__ job_segments,
                                                     uint32_t refill_min, int walk_budget, uint32_t shade_min,
-                                                    EpochArgs ea) {
+                                                    bool wide, EpochArgs ea) {
   const unsigned FULL = 0xffffffffu;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt_mask = (1u << lane) - 1u;
@@ -241,6 +264,7 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
   const bool may_park = ea.cur && ea.out_q && n_rays > ea.park_min;
   const uint32_t keep = (uint32_t)(((uint64_t)n_rays * ea.park_pct) / 100u);
   bool parking = false;
+  uint32_t iters = 0;   // loop guard (warp-uniform: every lane runs every iteration)
 
   // begin one segment from (p, d): the box hit directly, or a mesh walk
   auto begin_segment = [&](const DJob& J) {
@@ -250,12 +274,16 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
       have = box_hit(J, job_mats, px, py, pz, dx, dy, dz, h);
       phase = SHADE;
     } else {
-      walk_begin(w, scenes[J.scene], dx, dy, dz);
+      walk_begin<TIE>(w, scenes[J.scene], dx, dy, dz, wide);
       phase = WALK;
     }
   };
 
   while (true) {
+    if (++iters > kMaxLoop) {
+      atomicOr(err, 8u);
+      break;
+    }
     // ---- refill idle lanes from the ray queue (warp-aggregated)
     const unsigned idle = __ballot_sync(FULL, phase == IDLE);
     if (!exhausted && idle != 0u && (__popc(idle) >= (int)refill_min || idle == FULL)) {
@@ -315,7 +343,7 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
     if (!shade_now && phase == WALK) {
       const DJob& J = jobs[ji];
       const DScene& S = scenes[J.scene];
-      if (walk_steps<TIE>(w, S, px, py, pz, dx, dy, dz, walk_budget, err)) {
+      if (walk_steps<TIE>(w, S, px, py, pz, dx, dy, dz, walk_budget, wide, err)) {
         have = w.have;
         h.t = FLT_MAX;
         h.m = nullptr;
@@ -383,6 +411,177 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
   }
 }
 
+// The tracer as a wavefront inside each warp. A lane walks one ray at a time;
+// when its walk ends, the ray id goes to the warp's shading queue and the lane
+// takes the next ray to walk from the warp's walk queue (or the global ray
+// queue). Once 32 rays wait in the shading queue (or nothing is left to walk)
+// the whole warp shades them together, from their saved state, and the
+// survivors join the walk queue. Walks thus refill lane by lane, and the long
+// shading code always runs with full warps. A warp owns at most 63 rays
+// between two fetches from the ray queue (fetching only once its walk queue
+// is empty, with at most 31 waiting for shading and 32 walking), so each
+// queue holds 64 ids.
+//
+// Epochs (ea.cur set) work as in trace_kernel: once parking, survivors of a
+// shading pass and rays waiting to walk go to the next epoch's queue.
+template <int NB, bool TIE>
+__global__ void __launch_bounds__(256, 4) trace_wl_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
+                                                          uint32_t total_rays, const DScene* __restrict__ scenes,
+                                                          const DMat* __restrict__ job_mats,
+                                                          const DPanel* __restrict__ panels,
+                                                          const DPanelGroup* __restrict__ groups,
+                                                          float* __restrict__ acc, DLaunch* __restrict__ hdr,
+                                                          uint32_t* __restrict__ job_segments, int walk_budget,
+                                                          bool wide, EpochArgs ea) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr uint32_t kNone = 0xFFFFFFFFu;
+  constexpr uint32_t kQ = 64;
+  __shared__ uint32_t s_shade[8][kQ];
+  __shared__ uint32_t s_walk[8][kQ];
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint32_t* shade_q = s_shade[threadIdx.x >> 5];
+  uint32_t* walk_q = s_walk[threadIdx.x >> 5];
+  uint32_t sh_head = 0, sh_cnt = 0, wk_head = 0, wk_cnt = 0;   // warp-uniform
+  const WfState& st = ea.st;
+  const uint32_t* rq = ea.in_q;
+  const uint32_t n_rays = ea.cur ? (rq ? ea.cur->n : total_rays) : total_rays;
+  uint32_t* fetch = ea.cur ? &ea.cur->fetch : &hdr->ray_counter;
+  const bool may_park = ea.cur && ea.out_q && n_rays > ea.park_min;
+  const uint32_t keep = (uint32_t)(((uint64_t)n_rays * ea.park_pct) / 100u);
+  bool parking = false, exhausted = false;
+  uint32_t* err = &hdr->error;
+
+  // the walking ray of this lane
+  uint32_t rid = kNone;
+  const DScene* wsc = nullptr;
+  float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0;
+  int walk_stack_ref[STACK_DEPTH];
+  float walk_stack_t[STACK_DEPTH];
+  Walk w;
+  w.stack_ref = walk_stack_ref;
+  w.stack_t = walk_stack_t;
+
+  auto start_walk = [&](uint32_t r) {
+    const DJob& J = jobs[find_job(jobs, n_jobs, r)];
+    const float4 P = st.pos[r], D = st.dir[r];
+    ox = P.x; oy = P.y; oz = P.z;
+    dx = D.x; dy = D.y; dz = D.z;
+    wsc = scenes + J.scene;
+    walk_begin<TIE>(w, *wsc, dx, dy, dz, wide);
+    rid = r;
+  };
+  // ended rays (and the park signal), parked rays to the next epoch's queue
+  auto epoch_tally = [&](bool ended, bool parked, uint32_t r) {
+    if (!ea.cur) return;
+    const unsigned em = __ballot_sync(FULL, ended);
+    if (em && lane == (uint32_t)(__ffs(em) - 1)) {
+      const uint32_t done_now = atomicAdd(&ea.cur->ended, (uint32_t)__popc(em)) + (uint32_t)__popc(em);
+      if (may_park && n_rays - done_now <= keep && *((volatile const uint32_t*)fetch) >= n_rays)
+        *((volatile uint32_t*)&ea.cur->park) = 1u;
+    }
+    const unsigned pm = __ballot_sync(FULL, parked);
+    if (pm) {
+      uint32_t base = 0;
+      if (lane == (uint32_t)(__ffs(pm) - 1)) base = atomicAdd(&ea.next->n, (uint32_t)__popc(pm));
+      base = __shfl_sync(FULL, base, __ffs(pm) - 1);
+      if (parked) ea.out_q[base + (uint32_t)__popc(pm & lt_mask)] = r;
+    }
+  };
+
+  uint32_t iters = 0;   // loop guard (warp-uniform)
+  while (true) {
+    if (++iters > kMaxLoop) {
+      atomicOr(err, 8u);
+      break;
+    }
+    if (may_park && !parking) parking = *((volatile const uint32_t*)&ea.cur->park) != 0u;
+    if (parking && wk_cnt) {
+      // rays waiting to walk are between two segments: park them as they are
+      const uint32_t m = wk_cnt < 32u ? wk_cnt : 32u;
+      const bool pk = lane < m;
+      const uint32_t r = pk ? walk_q[(wk_head + lane) % kQ] : kNone;
+      wk_head += m;
+      wk_cnt -= m;
+      epoch_tally(false, pk, r);
+      __syncwarp();
+      continue;
+    }
+    unsigned walking = __ballot_sync(FULL, rid != kNone);
+
+    // ---- shading pass: a full warp of rays, or whatever waits once nothing can walk
+    if (sh_cnt >= 32u || (sh_cnt && !walking && !wk_cnt && (exhausted || parking))) {
+      const uint32_t m = sh_cnt < 32u ? sh_cnt : 32u;
+      bool alive = false, ended = false;
+      uint32_t r = kNone;
+      if (lane < m) {
+        r = shade_q[(sh_head + lane) % kQ];
+        alive = shade_saved_ray<NB>(jobs, n_jobs, scenes, job_mats, panels, groups, acc, st, r, job_segments);
+        ended = !alive;
+      }
+      sh_head += m;
+      sh_cnt -= m;
+      const bool parked = alive && parking;
+      alive = alive && !parking;
+      const unsigned am = __ballot_sync(FULL, alive);
+      if (alive) walk_q[(wk_head + wk_cnt + (uint32_t)__popc(am & lt_mask)) % kQ] = r;
+      wk_cnt += (uint32_t)__popc(am);
+      epoch_tally(ended, parked, r);
+      __syncwarp();
+      continue;
+    }
+
+    // ---- idle lanes take rays: the walk queue first, then the ray queue
+    unsigned idle = ~walking;
+    if (idle && wk_cnt) {
+      const uint32_t rank = (uint32_t)__popc(idle & lt_mask);
+      const uint32_t k = (uint32_t)__popc(idle) < wk_cnt ? (uint32_t)__popc(idle) : wk_cnt;
+      if (rid == kNone && rank < k) start_walk(walk_q[(wk_head + rank) % kQ]);
+      wk_head += k;
+      wk_cnt -= k;
+      idle = __ballot_sync(FULL, rid == kNone);
+    }
+    if (idle && !wk_cnt && !exhausted && !parking) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(fetch, (uint32_t)__popc(idle));
+      base = __shfl_sync(FULL, base, 0);
+      if (base >= n_rays) exhausted = true;
+      bool to_shade = false;
+      uint32_t r = kNone;
+      if (rid == kNone) {
+        const uint32_t k = base + (uint32_t)__popc(idle & lt_mask);
+        if (k < n_rays) {
+          r = rq ? rq[k] : k;
+          const DJob& J = jobs[find_job(jobs, n_jobs, r)];
+          if (!rq) start_saved_ray<NB>(J, st, r);
+          // a shoebox needs no walk: its hit is found when the ray is shaded
+          if (J.geom == OMG_GEOM_BOX) to_shade = true;
+          else start_walk(r);
+        }
+      }
+      const unsigned bm = __ballot_sync(FULL, to_shade);
+      if (to_shade) shade_q[(sh_head + sh_cnt + (uint32_t)__popc(bm & lt_mask)) % kQ] = r;
+      sh_cnt += (uint32_t)__popc(bm);
+    }
+    walking = __ballot_sync(FULL, rid != kNone);
+    if (!walking && !sh_cnt && !wk_cnt && (exhausted || parking)) break;
+
+    // ---- walk, at most walk_budget steps this iteration
+    bool finished = false;
+    if (rid != kNone && walk_steps<TIE>(w, *wsc, ox, oy, oz, dx, dy, dz, walk_budget, wide, err)) {
+      st.hit[rid] = make_float2(w.t_best, __int_as_float(w.have ? w.prim_best : -1));
+      finished = true;
+    }
+    const unsigned fm = __ballot_sync(FULL, finished);
+    if (finished) {
+      shade_q[(sh_head + sh_cnt + (uint32_t)__popc(fm & lt_mask)) % kQ] = rid;
+      rid = kNone;
+    }
+    sh_cnt += (uint32_t)__popc(fm);
+    __syncwarp();
+  }
+}
+
 // out = sum + comp per float, bins then dirs, per job.
 __global__ void finalize_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs, const float* __restrict__ acc,
                                 float* __restrict__ out) {
@@ -440,10 +639,16 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
   uint32_t refill = shape.refill_min == 0 ? 1 : (shape.refill_min > 32 ? 32 : shape.refill_min);
   const int steps = shape.walk_steps == 0 ? 1000000 : (int)shape.walk_steps;
   const uint32_t shade_min = shape.shade_min == 0 ? 1u : (shape.shade_min > 32 ? 32u : shape.shade_min);
-#define OMG_TRACE_LAUNCH(NB, TIE)                                                                        \
-  trace_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, groups, \
-                                                   acc, hdr, \
-                                                   job_segments, refill, steps, shade_min, ea)
+  // the warp-local wavefront needs the per-ray records and at most 8 warps a block
+  const bool wl = shape.mode == 1 && ea.st.pos && threads <= 256;
+  const bool wide = shape.wide != 0;
+#define OMG_TRACE_LAUNCH(NB, TIE)                                                                         \
+  if (wl)                                                                                                      \
+    trace_wl_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels,    \
+                                                        groups, acc, hdr, job_segments, steps, wide, ea);            \
+  else                                                                                                         \
+    trace_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, groups, \
+                                                     acc, hdr, job_segments, refill, steps, shade_min, wide, ea)
   if (max_nb <= 3) {
     if (tie) OMG_TRACE_LAUNCH(3, true);
     else OMG_TRACE_LAUNCH(3, false);

@@ -233,7 +233,7 @@ cudaError_t launch_wavefront(const DJob* jobs, uint32_t n_jobs, uint32_t total_r
                              int n_sms, bool tie, cudaStream_t s) {
   const bool staged = st.ctl && ep_q && ep_ctl && st.cap >= total_rays;
   const bool rounds = staged && shape.wf_iters > 0;
-  if (!staged || (!rounds && shape.epochs == 0))
+  if (!staged || (!rounds && shape.epochs == 0 && shape.mode == 0))
     return launch_trace(jobs, n_jobs, total_rays, max_nb, scenes, job_mats, panels, groups, acc, hdr, job_segments,
                         shape, n_sms, tie, s);
   if (n_jobs == 0 || total_rays == 0) return cudaSuccess;
