@@ -279,7 +279,10 @@ typedef struct omg_tune_result {
     uint32_t walk_steps;         /* traversal steps per lane per loop iteration (0 = whole walk) */
     uint32_t shade_min;          /* lanes of a warp that shade together (1..32; 0 reads as 1) */
     uint32_t mode;               /* persistent kernel: 0 per-lane state machine, 1 warp-local wavefront
-                                    (walks refill lane by lane; rays shade 32 at a time) */
+                                    (walks refill lane by lane; rays shade 32 at a time), 2 the same with
+                                    each walk split over 4 lanes of a 4-wide tree (tie_mode 1 and
+                                    host-built trees; otherwise mode 0 runs) */
+    uint32_t tail_mode;          /* persistent kernel of epochs after the first (same values) */
     uint32_t wide;               /* 1: persistent walks use the 4-wide tree (tie_mode 1, host-built trees) */
     uint32_t wf_rounds;          /* wavefront rounds before the persistent kernel (0 = none) */
     uint32_t wf_tail;            /* hand over to the persistent kernel at <= this many live rays */

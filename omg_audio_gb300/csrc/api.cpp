@@ -64,6 +64,7 @@ int32_t sync_scene_table(omg_ctx* ctx) {
     d.n_prims = s.n_prims;
     d.n_bands = s.n_bands;
     d.nodes4 = s.n_nodes4 ? s.nodes4.p : nullptr;
+    d.nodes4c = s.n_nodes4 ? s.nodes4c.p : nullptr;
     d.root4 = s.root4;
     d.n_nodes4 = s.n_nodes4;
   }
@@ -164,6 +165,7 @@ int32_t fill_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jo
   B.max_bins = 0;
   B.n_bin_floats = 0;
   B.n_dir_floats = 0;
+  bool coop_ok = P.tie_mode != 0;
   // per-job panel materials are placed after all box wall materials
   for (uint32_t i = 0; i < n_jobs; i++) {
     const omg_job& j = jobs[i];
@@ -208,6 +210,7 @@ int32_t fill_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jo
       if (it == ctx->scenes.end()) return OMG_E_NOT_FOUND;
       if (it->second->n_bands != nb) return OMG_E_INVALID;
       d.scene = j.scene_id;
+      if (it->second->n_nodes4 == 0) coop_ok = false;
     } else {
       return OMG_E_INVALID;
     }
@@ -248,6 +251,7 @@ int32_t fill_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jo
     r.bin_dt = P.bin_dt;
   }
   B.total_rays = (uint32_t)rays;
+  B.coop_ok = coop_ok;
   B.n_acc = acc;
   B.n_out = out;
   return OMG_OK;
@@ -312,9 +316,13 @@ int32_t record_launch(omg_ctx* ctx, BatchRec& B, cudaStream_t s, int parts = 3) 
     CK(cudaMemsetAsync(B.d_acc.p, 0, B.n_acc * sizeof(float), s));
     CK(cudaMemsetAsync(B.d_seg.p, 0, B.n_jobs * sizeof(uint32_t), s));
     CK(cudaMemsetAsync(B.d_ep_ctl.p, 0, (kMaxEpochs + 1) * sizeof(EpochCtl), s));
+    // cooperative walks need the near-tie rule and a 4-wide tree in every scene
+    LaunchShape eff = B.shape;
+    if (eff.mode == 2 && !B.coop_ok) eff.mode = 0;
+    if (eff.tail_mode == 2 && !B.coop_ok) eff.tail_mode = 0;
     CK(launch_wavefront(B.d_jobs.p, B.n_jobs, B.total_rays, B.max_nb, ctx->d_scenes.p, B.d_job_mats.p,
                         B.d_panels.p, B.d_groups.p, B.d_acc.p, B.d_hdr.p, B.d_seg.p, B.wf, B.d_ep_q.p,
-                        B.d_ep_ctl.p, B.shape, ctx->n_sms, ctx->prm.tie_mode != 0, s));
+                        B.d_ep_ctl.p, eff, ctx->n_sms, ctx->prm.tie_mode != 0, s));
   }
   if (parts & 2) {
     CK(launch_finalize(B.d_jobs.p, B.n_jobs, B.d_acc.p, B.d_out.p, B.n_out, s));
@@ -763,6 +771,7 @@ void shape_to_result(const LaunchShape& sh, float ms, omg_tune_result* r) {
   r->park_pct = sh.park_pct;
   r->shade_min = sh.shade_min;
   r->mode = sh.mode;
+  r->tail_mode = sh.tail_mode;
   r->wide = sh.wide;
   r->ms = ms;
 }
@@ -786,8 +795,9 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
   const uint32_t wl_walks[] = {0, 4, 8, 16, 32};
   const uint32_t rounds[] = {16, 32, 48, 64, 96, 128, 192};
   const uint32_t tails[] = {0, 2048, 8192, 32768};
-  const uint32_t epoch_counts[] = {4, 8, 12, 16, 24};
-  const uint32_t park_pcts[] = {25, 40, 55, 70};
+  const uint32_t epoch_counts[] = {2, 3, 4, 8};
+  const uint32_t park_pcts[] = {5, 10, 20, 40};
+  const uint32_t tail_modes[] = {0, 2};
   cudaEvent_t e0, e1;
   cudaStream_t cs;
   CK(cudaEventCreate(&e0));
@@ -829,17 +839,22 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
         sh.blocks_per_sm = ps;
         sh.walk_steps = wk;
         rc = try_shape(sh);
+        if (rc || !B.coop_ok || th != 256) continue;
+        sh.mode = 2;
+        rc = try_shape(sh);
       }
     }
   const LaunchShape persistent = best_shape;
-  for (uint32_t ne : epoch_counts)
-    for (uint32_t pp : park_pcts) {
-      if (rc) continue;
-      LaunchShape sh = persistent;
-      sh.epochs = ne;
-      sh.park_pct = pp;
-      rc = try_shape(sh);
-    }
+  for (uint32_t tm : tail_modes)
+    for (uint32_t ne : epoch_counts)
+      for (uint32_t pp : park_pcts) {
+        if (rc || (tm == 2 && !B.coop_ok)) continue;
+        LaunchShape sh = persistent;
+        sh.epochs = ne;
+        sh.park_pct = pp;
+        sh.tail_mode = tm;
+        rc = try_shape(sh);
+      }
   const LaunchShape chained = best_shape;
   for (uint32_t nr : rounds)
     for (uint32_t tl : tails) {
@@ -868,7 +883,7 @@ int32_t omg_batch_set_shape(omg_ctx* ctx, uint32_t id, const omg_tune_result* sh
   if (shape->block_threads == 0 || shape->block_threads % 32 != 0 || shape->block_threads > 256 ||
       shape->blocks_per_sm == 0 || shape->block_threads * shape->blocks_per_sm > 2048 || shape->refill_min == 0 ||
       shape->refill_min > 32 || shape->wf_rounds > 4096 || shape->epochs > kMaxEpochs || shape->park_pct > 100 ||
-      shape->shade_min > 32 || shape->mode > 1)
+      shape->shade_min > 32 || shape->mode > 2 || shape->tail_mode > 2)
     return OMG_E_INVALID;
   BatchRec& B = *it->second;
   LaunchShape sh;
@@ -882,6 +897,7 @@ int32_t omg_batch_set_shape(omg_ctx* ctx, uint32_t id, const omg_tune_result* sh
   sh.park_pct = shape->park_pct;
   sh.shade_min = shape->shade_min == 0 ? 1u : shape->shade_min;
   sh.mode = shape->mode;
+  sh.tail_mode = shape->tail_mode;
   sh.wide = shape->wide ? 1u : 0u;
   B.shape = sh;
   int32_t rc = build_graphs(ctx, B);

@@ -93,6 +93,23 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
     if (S->n_nodes4) {
       CK(S->nodes4.alloc((size_t)S->n_nodes4 * 8));
       CK(cudaMemcpy(S->nodes4.p, dev_nodes4.data(), dev_nodes4.size() * 4, cudaMemcpyHostToDevice));
+      // child by child: (lo.x, lo.y, lo.z, hi.x), (hi.y, hi.z, ref, 0)
+      std::vector<float> aos((size_t)S->n_nodes4 * 32, 0.0f);
+      for (size_t n = 0; n < S->n_nodes4; n++) {
+        const float* q = &dev_nodes4[32 * n];
+        for (int k = 0; k < 4; k++) {
+          float* o = &aos[32 * n + 8 * k];
+          o[0] = q[0 + k];   // lo.x
+          o[1] = q[8 + k];   // lo.y
+          o[2] = q[16 + k];  // lo.z
+          o[3] = q[4 + k];   // hi.x
+          o[4] = q[12 + k];  // hi.y
+          o[5] = q[20 + k];  // hi.z
+          o[6] = q[24 + k];  // ref bits
+        }
+      }
+      CK(S->nodes4c.alloc((size_t)S->n_nodes4 * 8));
+      CK(cudaMemcpy(S->nodes4c.p, aos.data(), aos.size() * 4, cudaMemcpyHostToDevice));
     }
   } else {
     // LBVH: upload the primitives in tessellation order, build on the device

@@ -57,6 +57,10 @@ struct DScene {
   const float4* nodes4;
   int32_t root4;
   uint32_t n_nodes4;
+  // The 4-wide tree once more, child by child for walks that split a node's
+  // children over 4 lanes: 32 B per child, child k of node n at float4 index
+  // 8 n + 2 k: (lo.x, lo.y, lo.z, hi.x), (hi.y, hi.z, ref bits, 0).
+  const float4* nodes4c;
 };
 constexpr int32_t kEmpty4 = 0x7FFFFFFE;
 
@@ -129,8 +133,13 @@ struct LaunchShape {
   uint32_t refill_min = 1;      // a warp refetches rays once this many lanes are idle
   uint32_t walk_steps = 0;      // traversal steps per lane per loop iteration (0 = a whole walk)
   uint32_t shade_min = 32;      // lanes that shade together (or every waiting lane once none walks)
-  uint32_t mode = 0;            // persistent kernel: 0 lane state machine, 1 warp-local wavefront
+  uint32_t mode = 0;            // persistent kernel: 0 lane state machine, 1 warp-local wavefront,
+                                // 2 cooperative 4-lane walks
+  uint32_t tail_mode = 0;       // the persistent kernel of epochs after the first
   uint32_t wide = 0;            // persistent walks on the 4-wide tree (near-tie rule only)
+  // mode 2: the persistent kernel walks each ray with 4 lanes (one child of a
+  // 4-wide node each) and shades 32 rays at a time (near-tie rule, every
+  // mesh scene of the batch host-built)
   uint32_t wf_iters = 0;        // wavefront rounds before the persistent kernel takes over (0: none)
   uint32_t wf_tail = 0;         // ... or as soon as at most this many rays are alive
   uint32_t epochs = 0;          // persistent-kernel epochs (0: one launch that never parks)
@@ -189,6 +198,11 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
                          const DPanelGroup* groups, float* acc,
                          DLaunch* hdr, uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie,
                          cudaStream_t s, const EpochArgs* ep = nullptr);
+// coop.cu: the mode-2 persistent kernel (same arguments as launch_trace).
+cudaError_t launch_trace_coop(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
+                              const DScene* scenes, const DMat* job_mats, const DPanel* panels,
+                              const DPanelGroup* groups, float* acc, DLaunch* hdr, uint32_t* job_segments,
+                              const LaunchShape& shape, int n_sms, const EpochArgs& ea, cudaStream_t s);
 // wavefront.cu: wavefront rounds (when shape.wf_iters > 0), then the
 // persistent kernel on the remaining rays, in shape.epochs epochs (ep_q: two
 // queues of st.cap ids; ep_ctl: kMaxEpochs + 1 records, cleared).

@@ -62,6 +62,7 @@ struct SceneRec {
   uint32_t bvh_kind = OMG_BVH_SAH;
   DevBuf<float4> nodes, prims, normals;
   DevBuf<float4> nodes4;          // 4-wide collapse of `nodes` (host-built trees)
+  DevBuf<float4> nodes4c;         // the same, child by child
   int32_t root4 = 0;
   uint32_t n_nodes4 = 0;
   DevBuf<DMat> mats;
@@ -105,6 +106,7 @@ struct BatchRec {
   DevBuf<float2> d_wf_hit;
   DevBuf<WfCtl> d_wf_ctl;
   WfState wf{};
+  bool coop_ok = false;           // near-tie rule and every mesh scene has a 4-wide tree (mode 2)
   DevBuf<uint32_t> d_ep_q;        // epoch queues (2 x rays)
   DevBuf<EpochCtl> d_ep_ctl;      // kMaxEpochs + 1 records
   LaunchShape shape;

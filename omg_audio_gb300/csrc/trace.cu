@@ -631,6 +631,9 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
   if (n_jobs == 0 || total_rays == 0) return cudaSuccess;
   EpochArgs ea{};
   if (ep) ea = *ep;
+  if (shape.mode == 2 && tie && ea.st.pos)
+    return launch_trace_coop(jobs, n_jobs, total_rays, max_nb, scenes, job_mats, panels, groups, acc, hdr,
+                             job_segments, shape, n_sms, ea, s);
   uint32_t threads = shape.block_threads;
   uint64_t want = (uint64_t)n_sms * shape.blocks_per_sm;
   uint64_t need = ((uint64_t)total_rays + threads - 1) / threads;

@@ -264,8 +264,10 @@ cudaError_t launch_wavefront(const DJob* jobs, uint32_t n_jobs, uint32_t total_r
     a.park_pct = shape.park_pct;
     a.park_min = shape.park_min;
     a.st = st;
+    LaunchShape sk = shape;
+    if (k > 0) sk.mode = shape.tail_mode;
     cudaError_t e = launch_trace(jobs, n_jobs, total_rays, max_nb, scenes, job_mats, panels, groups, acc, hdr,
-                                 job_segments, shape, n_sms, tie, s, &a);
+                                 job_segments, sk, n_sms, tie, s, &a);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

@@ -8,10 +8,10 @@ Every shape traces the same rays with the same operations, so per job:
   - the segment count equals the f32-trajectory oracle's exactly;
   - the compensated FP32 histogram is within 1e-5 (relative, bins holding
     >= 1e-6 of the band total) of the oracle's f32 trajectories summed in FP64.
-Shapes cover both persistent kernels (per-lane state machine, warp-local
-wavefront) alone and in epochs, on the binary and the 4-wide tree, a
-hand-over after a few rounds, a hand-over at a live-ray threshold, and rounds
-to the last ray.
+Shapes cover the three persistent kernels (per-lane state machine, warp-local
+wavefront, cooperative 4-lane walks) alone and in epochs, on the binary and
+the 4-wide tree, a hand-over after a few rounds, a hand-over at a live-ray
+threshold, and rounds to the last ray.
 """
 import numpy as np
 import pytest
@@ -37,9 +37,15 @@ SHAPES = [dict(mode=0, wf_rounds=0, wf_tail=0, epochs=0),
           dict(mode=1, wf_rounds=0, wf_tail=0, epochs=32, park_pct=95, walk_steps=16),
           dict(mode=1, wf_rounds=5, wf_tail=0, epochs=4, park_pct=60, walk_steps=8),
           dict(mode=0, wf_rounds=0, wf_tail=0, epochs=0, walk_steps=8, wide=1),
-          dict(mode=1, wf_rounds=0, wf_tail=0, epochs=3, park_pct=50, walk_steps=4, wide=1)]
+          dict(mode=1, wf_rounds=0, wf_tail=0, epochs=3, park_pct=50, walk_steps=4, wide=1),
+          dict(mode=2, wf_rounds=0, wf_tail=0, epochs=0, walk_steps=0),
+          dict(mode=2, wf_rounds=0, wf_tail=0, epochs=0, walk_steps=3),
+          dict(mode=2, wf_rounds=0, wf_tail=0, epochs=6, park_pct=50, walk_steps=0),
+          dict(mode=2, wf_rounds=4, wf_tail=0, epochs=3, park_pct=60, walk_steps=8),
+          dict(mode=0, tail_mode=2, wf_rounds=0, wf_tail=0, epochs=2, park_pct=30, walk_steps=0)]
 for _s in SHAPES:
     _s.setdefault("wide", 0)
+    _s.setdefault("tail_mode", _s["mode"])
 
 
 def _launches(shape):
@@ -95,7 +101,7 @@ def mixed(oracle):
 
 @pytest.mark.parametrize("shape", SHAPES,
                          ids=[f"m{s['mode']}-r{s['wf_rounds']}-t{s['wf_tail']}-e{s['epochs']}-w{s.get('walk_steps', '')}"
-                              f"{'-wide' if s['wide'] else ''}" for s in SHAPES])
+                              f"{'-wide' if s['wide'] else ''}-t{s['tail_mode']}" for s in SHAPES])
 def test_wavefront_shapes_match_the_oracle(mixed, shape):
     ctx, jobs, panels, ref = mixed
     b = ctx.batch(jobs, panels)
@@ -129,7 +135,8 @@ def test_wavefront_eight_bands(oracle):
                             max_time=r.max_time))
         assert max(r.n_bands for r in rooms) == 8
         b = ctx.batch(jobs)
-        for shape in (SHAPES[1], SHAPES[3], SHAPES[5], SHAPES[7], SHAPES[10], SHAPES[12], SHAPES[13]):
+        for shape in (SHAPES[1], SHAPES[3], SHAPES[5], SHAPES[7], SHAPES[10], SHAPES[12], SHAPES[13], SHAPES[14],
+                      SHAPES[16], SHAPES[18]):
             b.set_shape(**shape)
             b.launch()
             res = b.read()
