@@ -5,8 +5,9 @@ with shared walls, 1 x 2.1 m door holes and glass panes, 49k primitives after
 tessellation; 64 source/listener pairs x 4096 rays x 3 bands, 2000 x 1 ms
 bins (2 s), <= 200 bounces, energy floor 1e-6; plus the 512-ray golden-spiral
 dome fan for each of the 64 listeners. A step traces all 64 pairs and all 64
-domes. Inputs (scene, jobs) are resident in HBM; the BVH (~3 MB) fits in L2,
-so L2 is flushed (a 256 MB write) before every timed step.
+domes (the domes on a second stream, overlapping the trace). Inputs (scene,
+jobs) are resident in HBM; the BVH (~3 MB) fits in L2, so L2 is flushed (a
+256 MB write) before every timed step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -40,6 +41,16 @@ DOME_RAYS = 512
 CFG = dict(n_bands=3, n_bins=2000, bin_dt=0.001, max_time=2.0, max_bounces=200, energy_floor=1e-6)
 WORKLOAD = "multiroom-40rooms-49k-prims: 64 pairs x 4096 rays x 3 bands, 2000 x 1 ms bins, 200 bounces, " \
            "floor 1e-6, + 64 x 512-ray dome fans"
+
+
+def traffic():
+    """DRAM bytes (read + write) of one trace part, from the ncu capture whose
+    summary is committed under profiles/ (None when there is none)."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh).get("trace_multiroom_64x4096", {}).get("dram_bytes")
+    return None
 
 
 def peaks():
@@ -185,7 +196,10 @@ def run_ours(args):
     from omg_audio_gb300 import _lib
 
     case = build_case()
-    ctx = Context(TraceConfig(device=local, timeout_ms=60000, tie_mode=1, **CFG))
+    cfg = dict(CFG)
+    if args.max_bounces:
+        cfg["max_bounces"] = args.max_bounces
+    ctx = Context(TraceConfig(device=local, timeout_ms=60000, tie_mode=1, **cfg))
     # a dedicated stream: the library launches on it and the events are recorded on it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -197,29 +211,42 @@ def run_ours(args):
     jobs = [Job(src, lis, N_RAYS, seed=1000 + p, scene=scene, panel_offset=0, n_panels=len(case.panels))
             for p, (src, lis) in enumerate(case.pairs[:args.pairs])]
     batch = ctx.batch(jobs, case.panels)
-    tune = batch.autotune(reps=1) if args.autotune else None
+    if args.shape:
+        batch.set_shape(**json.loads(args.shape))
+        tune = batch.shape()
+    else:
+        tune = batch.autotune(reps=1) if args.autotune else None
     dome = DomeProbe(ctx, scene, case.glass, n_fan=DOME_RAYS)
+    dome_stream = torch.cuda.Stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def step(ev=None):
-        if ev:
-            ev[0].record(stream)
+        """One step: the 64 dome fans on a second stream while the batch traces
+        (clear + trace, then finalize + reverb) on the first; the step ends when
+        both have."""
+        start = torch.cuda.Event(enable_timing=True) if ev is None else ev[0]
+        start.record(stream)
+        dome_stream.wait_event(start)
+        dome.submit(case.listeners, n_rays=DOME_RAYS, stream=dome_stream.cuda_stream)
         batch.launch(1)
         if ev:
             ev[1].record(stream)
         batch.launch(2)
+        stream.wait_stream(dome_stream)
         if ev:
             ev[2].record(stream)
 
     for _ in range(max(args.warmup, 0)):
         step()
-        dome.sample(case.listeners, n_rays=DOME_RAYS)
+        torch.cuda.synchronize()
+        dome.collect()
     torch.cuda.synchronize()
     if args.profile:
         # small case for a profiler: the launches only, nothing timed or printed
         for _ in range(args.steps):
             step()
-        torch.cuda.synchronize()
+            torch.cuda.synchronize()
+            dome.collect()
         return 0
     if ws > 1:
         dist.barrier()
@@ -230,37 +257,44 @@ def run_ours(args):
         for k in range(args.steps):
             flush.zero_()
             step(evs[k])
-        torch.cuda.synchronize()
-        # the dome fan of every listener, same steps (its own host round trip)
+            torch.cuda.synchronize()
+            dres = dome.collect()
+        # the dome fans alone (device time on their stream), for the record
         for k in range(args.steps):
             flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(dome_stream)
+            dome.submit(case.listeners, n_rays=DOME_RAYS, stream=dome_stream.cuda_stream)
+            b.record(dome_stream)
             torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            dres = dome.sample(case.listeners, n_rays=DOME_RAYS)
-            dome_ms.append(1e3 * (time.perf_counter() - t0))
+            dome.collect()
+            dome_ms.append(a.elapsed_time(b))
         torch.cuda.synchronize()
     trace_ms = np.array([e[0].elapsed_time(e[1]) for e in evs])
     step_ms = np.array([e[0].elapsed_time(e[2]) for e in evs])
     segments = batch.segments()
     dome_seg = dres["segments"]["escape_events"] + dres["segments"]["through_calls"]
-    t_step = float(np.mean(step_ms)) + float(np.mean(dome_ms))
+    t_step = float(np.mean(step_ms))
     if ws > 1:
         t = torch.tensor([t_step], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_step = float(t.item())
     value = ws * (segments + dome_seg) / (t_step * 1e-3)
 
-    # end to end: the host-buffer C-ABI call (H2D jobs, launch, D2H echograms) + the dome call
+    # end to end through the C ABI with host buffers: the dome submitted on its
+    # stream (eyes up, fans, bins down), the batch call (jobs up, trace,
+    # echograms and reverb down) meanwhile, then the dome collected
     e2e_ms = []
     for k in range(max(1, args.steps)):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        dome.submit(case.listeners, n_rays=DOME_RAYS, stream=dome_stream.cuda_stream)
         ctx.trace_batch(jobs, case.panels)
-        dome.sample(case.listeners, n_rays=DOME_RAYS)
+        dome.collect()
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     h2d, d2h = ctx.io_bytes()
-    d2h += 64 * 9 * (3 + 3) * 4 + 64 * DOME_RAYS * (1 + 12)
+    d2h += 64 * 9 * (3 + 3) * 4 + 2 * 4 + 16
     h2d += 64 * 12
     e2e = ws * (segments + dome_seg) / (float(np.mean(e2e_ms)) * 1e-3)
 
@@ -280,16 +314,18 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "prims": scene.info()["prims"], "bvh": args.bvh,
                        "l2": "flushed (256 MB write) before every timed step", "segments_per_step": segments,
                        "dome_segments_per_step": dome_seg, "trace_ms": float(np.mean(trace_ms)),
-                       "finalize_reverb_ms": float(np.mean(step_ms - trace_ms)),
-                       "dome_ms": float(np.mean(dome_ms)), "autotune": tune,
+                       "step_ms": float(np.mean(step_ms)),
+                       "dome_alone_ms": float(np.mean(dome_ms)),
+                       "dome": "the 64 fans on a second stream, overlapping the trace", "autotune": tune,
                        "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "ms_per_step": float(np.mean(e2e_ms))},
             "gpu_launches": int(args.steps * (batch.kernel_count() + 2)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "frac": achieved / peak, "traffic": traffic(), "peak_kind": peak_kind,
                          "bytes_per_segment": bseg, **{k: round(v, 4) for k, v in parts.items()},
-                         "kernel": "trace_kernel<3> (clear + trace part, CUDA events)"},
+                         "kernel": "the trace part of a step (persistent trace kernels, CUDA events on their "
+                                   "stream)"},
             "cpu_baseline": {"value": cpu["segments"] / cpu["seconds"], "unit": UNIT, "cores": threads,
                              "kind": "port",
                              "sample": f"{args.ref_pairs} of {N_PAIRS} pairs x {N_RAYS} rays (f32 oracle, "
@@ -313,6 +349,10 @@ def main():
     ap.add_argument("--ref-pairs", type=int, default=64)
     ap.add_argument("--pairs", type=int, default=N_PAIRS, help="pairs traced per step (default: the workload's 64)")
     ap.add_argument("--profile", action="store_true", help="launches only (a small case under a profiler)")
+    ap.add_argument("--max-bounces", type=int, default=0,
+                    help="profiling variant: cap the bounces (0: the workload's 200)")
+    ap.add_argument("--shape", default="",
+                    help="launch shape as JSON (omg_tune_result fields), instead of the autotuner")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the launch-shape autotuner (it runs once, before the warm-up)")
     args = ap.parse_args()

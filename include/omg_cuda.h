@@ -324,6 +324,20 @@ int32_t omg_dome_destroy(omg_ctx* ctx, uint32_t probe_id);
 int32_t omg_dome_sample(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint32_t n_eyes,
                         const omg_dome_panel* leaves, uint32_t n_leaves, uint32_t n_rays, uint32_t max_events,
                         omg_dome_bin* out, float* raw_energy, uint8_t* escape, float* ray_tp);
+/* The same sample in two calls, so that it can overlap other work (a batch
+ * trace on another stream): submit enqueues the inputs, the kernels and the
+ * result copies on cuda_stream (NULL: the context's stream) and returns at
+ * once; collect waits (bounded by omg_params.timeout_ms) and copies the
+ * results out. `want` selects the optional outputs collect may return:
+ * 1 raw_energy, 2 escape, 4 ray_tp. One sample per probe may be in flight. */
+#define OMG_DOME_WANT_RAW 1u
+#define OMG_DOME_WANT_ESCAPE 2u
+#define OMG_DOME_WANT_TP 4u
+int32_t omg_dome_submit(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint32_t n_eyes,
+                        const omg_dome_panel* leaves, uint32_t n_leaves, uint32_t n_rays, uint32_t max_events,
+                        uint32_t want, void* cuda_stream);
+int32_t omg_dome_collect(omg_ctx* ctx, uint32_t probe_id, omg_dome_bin* out, float* raw_energy, uint8_t* escape,
+                         float* ray_tp);
 /* Work of the probe's last sample: trace_escape events (dome.rs:333-380) and
  * trace_through calls (dome.rs:390-422), summed over listeners. */
 int32_t omg_dome_segments(omg_ctx* ctx, uint32_t probe_id, uint64_t* escape_events, uint64_t* through_calls);

@@ -123,6 +123,8 @@ SIGNATURES = {
     "omg_dome_create": (I32, [P, U32, P, U32, U32, U32, PU32]),
     "omg_dome_destroy": (I32, [P, U32]),
     "omg_dome_sample": (I32, [P, U32, P, U32, P, U32, U32, U32, P, P, P, P]),
+    "omg_dome_submit": (I32, [P, U32, C.c_void_p, U32, C.c_void_p, U32, U32, U32, U32, C.c_void_p]),
+    "omg_dome_collect": (I32, [P, U32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "omg_dome_segments": (I32, [P, U32, PU64, PU64]),
     "omg_trace_box_noalloc": (I32, [C.POINTER(omg_box_job), C.POINTER(omg_params), P, P, P]),
 }

@@ -22,6 +22,14 @@ struct DomeRec {
   DevBuf<uint32_t> events;
   cudaEvent_t done = nullptr;
   uint64_t last_events[2] = {0, 0};
+  // pinned staging of a submitted sample (inputs up, results down)
+  PinBuf<float> h_eyes, h_energy, h_dir, h_raw, h_tp;
+  PinBuf<uint8_t> h_esc;
+  PinBuf<DDomePanel> h_panels;
+  PinBuf<DLaunch> h_hdr;
+  PinBuf<uint32_t> h_events;
+  bool pending = false;
+  uint32_t p_eyes = 0, p_rays = 0, p_flags = 0;
   ~DomeRec() {
     if (done) cudaEventDestroy(done);
   }
@@ -88,20 +96,32 @@ int32_t omg_dome_destroy(omg_ctx* ctx, uint32_t probe_id) {
   if (!ctx) return OMG_E_INVALID;
   auto it = ctx->probes.find(probe_id);
   if (it == ctx->probes.end()) return OMG_E_NOT_FOUND;
+  // a submitted sample may still use the probe's buffers (on any stream)
+  if (it->second->pending) {
+    int32_t rc = wait_event(ctx, it->second->done, timeout_of(ctx));
+    if (rc) return rc;
+  }
   cudaStreamSynchronize(ctx->stream);
   ctx->probes.erase(it);
   return OMG_OK;
 }
 
-int32_t omg_dome_sample(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint32_t n_eyes,
-                        const omg_dome_panel* leaves, uint32_t n_leaves, uint32_t n_rays, uint32_t max_events,
-                        omg_dome_bin* out, float* raw_energy, uint8_t* escape, float* ray_tp) {
-  if (!ctx || !eyes || !n_eyes || (n_leaves && !leaves) || !out || n_rays == 0 || max_events == 0)
-    return OMG_E_INVALID;
-  auto it = ctx->probes.find(probe_id);
-  if (it == ctx->probes.end()) return OMG_E_NOT_FOUND;
-  DomeRec& D = *it->second;
+}  // extern "C"
+
+namespace {
+
+enum : uint32_t { kWantRaw = 1, kWantEscape = 2, kWantTp = 4 };
+
+// Enqueue one sample on stream s: inputs through pinned staging, the dome
+// kernels, results into pinned staging, then the probe's event.
+int32_t dome_submit(omg_ctx* ctx, DomeRec& D, const float* eyes, uint32_t n_eyes, const omg_dome_panel* leaves,
+                    uint32_t n_leaves, uint32_t n_rays, uint32_t max_events, uint32_t flags, cudaStream_t s) {
+  if (!eyes || !n_eyes || (n_leaves && !leaves) || n_rays == 0 || max_events == 0) return OMG_E_INVALID;
   if (n_rays > D.n_fan) return OMG_E_INVALID;
+  if (D.pending) {
+    ctx->last_error = "dome: the previous sample was not collected";
+    return OMG_E_INVALID;
+  }
   auto sit = ctx->scenes.find(D.scene_id);
   if (sit == ctx->scenes.end()) return OMG_E_NOT_FOUND;
   for (uint32_t i = 0; i < 3 * n_eyes; i++)
@@ -112,7 +132,6 @@ int32_t omg_dome_sample(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint
     if (!valid_dome_panel(leaves[i], nb)) return OMG_E_INVALID;
     pans.push_back(to_dpanel(leaves[i], nb));
   }
-  cudaStream_t s = ctx->stream;
   if (n_eyes > D.eye_cap) {
     // grow the per-listener EMA state, keeping existing slots
     uint32_t cap = std::max(n_eyes, D.eye_cap * 2);
@@ -134,18 +153,36 @@ int32_t omg_dome_sample(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint
     D.eye_cap = cap;
   }
   const uint64_t nr = (uint64_t)n_eyes * n_rays;
-  if (D.eyes.n < 3ull * n_eyes) CK(D.eyes.alloc(3ull * n_eyes));
+  if (D.eyes.n < 3ull * n_eyes) {
+    CK(D.eyes.alloc(3ull * n_eyes));
+    CK(D.h_eyes.alloc(3ull * n_eyes));
+  }
   if (D.tp.n < nr * nb) CK(D.tp.alloc(nr * nb));
   if (D.esc.n < nr) CK(D.esc.alloc(nr));
   if (D.raw.n < 9ull * nb * n_eyes) {
     CK(D.raw.alloc(9ull * nb * n_eyes));
     CK(D.energy.alloc(9ull * nb * n_eyes));
     CK(D.dir.alloc(27ull * n_eyes));
+    CK(D.h_raw.alloc(9ull * nb * n_eyes));
+    CK(D.h_energy.alloc(9ull * nb * n_eyes));
+    CK(D.h_dir.alloc(27ull * n_eyes));
   }
-  if (D.panels.n < pans.size()) CK(D.panels.alloc(pans.size()));
-  CK(cudaMemcpyAsync(D.eyes.p, eyes, 12ull * n_eyes, cudaMemcpyHostToDevice, s));
-  if (!pans.empty())
-    CK(cudaMemcpyAsync(D.panels.p, pans.data(), pans.size() * sizeof(DDomePanel), cudaMemcpyHostToDevice, s));
+  if ((flags & kWantEscape) && D.h_esc.n < nr) CK(D.h_esc.alloc(nr));
+  if ((flags & kWantTp) && D.h_tp.n < nr * nb) CK(D.h_tp.alloc(nr * nb));
+  if (D.panels.n < pans.size()) {
+    CK(D.panels.alloc(pans.size()));
+    CK(D.h_panels.alloc(pans.size()));
+  }
+  if (!D.h_hdr.p) {
+    CK(D.h_hdr.alloc(1));
+    CK(D.h_events.alloc(2));
+  }
+  std::memcpy(D.h_eyes.p, eyes, 12ull * n_eyes);
+  CK(cudaMemcpyAsync(D.eyes.p, D.h_eyes.p, 12ull * n_eyes, cudaMemcpyHostToDevice, s));
+  if (!pans.empty()) {
+    std::memcpy(D.h_panels.p, pans.data(), pans.size() * sizeof(DDomePanel));
+    CK(cudaMemcpyAsync(D.panels.p, D.h_panels.p, pans.size() * sizeof(DDomePanel), cudaMemcpyHostToDevice, s));
+  }
   CK(cudaMemsetAsync(D.hdr.p, 0, sizeof(DLaunch), s));
   CK(cudaMemsetAsync(D.events.p, 0, 8, s));
   DDomeLaunch L;
@@ -172,34 +209,87 @@ int32_t omg_dome_sample(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint
   L.events = D.events.p;
   L.tie = ctx->prm.tie_mode;
   CK(launch_dome(L, s));
-  std::vector<float> energy(9ull * nb * n_eyes), dir(27ull * n_eyes);
-  CK(cudaMemcpyAsync(energy.data(), D.energy.p, energy.size() * 4, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(dir.data(), D.dir.p, dir.size() * 4, cudaMemcpyDeviceToHost, s));
-  if (raw_energy) CK(cudaMemcpyAsync(raw_energy, D.raw.p, 9ull * nb * n_eyes * 4, cudaMemcpyDeviceToHost, s));
-  if (escape) CK(cudaMemcpyAsync(escape, D.esc.p, nr, cudaMemcpyDeviceToHost, s));
-  if (ray_tp) CK(cudaMemcpyAsync(ray_tp, D.tp.p, nr * nb * 4, cudaMemcpyDeviceToHost, s));
-  DLaunch h;
-  uint32_t ev[2];
-  CK(cudaMemcpyAsync(&h, D.hdr.p, sizeof(h), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(ev, D.events.p, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(D.h_energy.p, D.energy.p, 9ull * nb * n_eyes * 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(D.h_dir.p, D.dir.p, 27ull * n_eyes * 4, cudaMemcpyDeviceToHost, s));
+  if (flags & kWantRaw) CK(cudaMemcpyAsync(D.h_raw.p, D.raw.p, 9ull * nb * n_eyes * 4, cudaMemcpyDeviceToHost, s));
+  if (flags & kWantEscape) CK(cudaMemcpyAsync(D.h_esc.p, D.esc.p, nr, cudaMemcpyDeviceToHost, s));
+  if (flags & kWantTp) CK(cudaMemcpyAsync(D.h_tp.p, D.tp.p, nr * nb * 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(D.h_hdr.p, D.hdr.p, sizeof(DLaunch), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(D.h_events.p, D.events.p, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(D.done, s));
+  D.pending = true;
+  D.p_eyes = n_eyes;
+  D.p_rays = n_rays;
+  D.p_flags = flags;
+  return OMG_OK;
+}
+
+// Wait (bounded) for a submitted sample and copy its results out.
+int32_t dome_collect(omg_ctx* ctx, DomeRec& D, omg_dome_bin* out, float* raw_energy, uint8_t* escape,
+                     float* ray_tp) {
+  if (!D.pending) {
+    ctx->last_error = "dome: nothing submitted";
+    return OMG_E_INVALID;
+  }
   int32_t rc = wait_event(ctx, D.done, timeout_of(ctx));
   if (rc) return rc;
-  if (h.error) {
-    ctx->last_error = (h.error & 2u) ? "dome: too many crossings on one straight-through segment"
-                                     : "dome: traversal stack overflow";
+  D.pending = false;
+  const uint32_t nb = D.nb, n_eyes = D.p_eyes;
+  const uint64_t nr = (uint64_t)n_eyes * D.p_rays;
+  if (D.h_hdr.p->error) {
+    ctx->last_error = (D.h_hdr.p->error & 2u) ? "dome: too many crossings on one straight-through segment"
+                                              : "dome: traversal stack overflow";
     return OMG_E_OVERFLOW;
   }
-  D.last_events[0] = ev[0];
-  D.last_events[1] = ev[1];
-  for (uint32_t e = 0; e < n_eyes; e++)
-    for (uint32_t k = 0; k < 9; k++) {
-      omg_dome_bin& o = out[e * 9 + k];
-      std::memset(&o, 0, sizeof(o));
-      for (int c = 0; c < 3; c++) o.dir[c] = dir[(e * 9 + k) * 3 + c];
-      for (uint32_t b = 0; b < nb; b++) o.energy[b] = energy[(e * 9 + k) * nb + b];
-    }
+  D.last_events[0] = D.h_events.p[0];
+  D.last_events[1] = D.h_events.p[1];
+  if (out)
+    for (uint32_t e = 0; e < n_eyes; e++)
+      for (uint32_t k = 0; k < 9; k++) {
+        omg_dome_bin& o = out[e * 9 + k];
+        std::memset(&o, 0, sizeof(o));
+        for (int c = 0; c < 3; c++) o.dir[c] = D.h_dir.p[(e * 9 + k) * 3 + c];
+        for (uint32_t b = 0; b < nb; b++) o.energy[b] = D.h_energy.p[(e * 9 + k) * nb + b];
+      }
+  if (raw_energy && (D.p_flags & kWantRaw)) std::memcpy(raw_energy, D.h_raw.p, 9ull * nb * n_eyes * 4);
+  if (escape && (D.p_flags & kWantEscape)) std::memcpy(escape, D.h_esc.p, nr);
+  if (ray_tp && (D.p_flags & kWantTp)) std::memcpy(ray_tp, D.h_tp.p, nr * nb * 4);
   return OMG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t omg_dome_sample(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint32_t n_eyes,
+                        const omg_dome_panel* leaves, uint32_t n_leaves, uint32_t n_rays, uint32_t max_events,
+                        omg_dome_bin* out, float* raw_energy, uint8_t* escape, float* ray_tp) {
+  if (!ctx || !out) return OMG_E_INVALID;
+  auto it = ctx->probes.find(probe_id);
+  if (it == ctx->probes.end()) return OMG_E_NOT_FOUND;
+  DomeRec& D = *it->second;
+  const uint32_t flags = (raw_energy ? kWantRaw : 0u) | (escape ? kWantEscape : 0u) | (ray_tp ? kWantTp : 0u);
+  int32_t rc = dome_submit(ctx, D, eyes, n_eyes, leaves, n_leaves, n_rays, max_events, flags, ctx->stream);
+  if (rc) return rc;
+  return dome_collect(ctx, D, out, raw_energy, escape, ray_tp);
+}
+
+int32_t omg_dome_submit(omg_ctx* ctx, uint32_t probe_id, const float* eyes, uint32_t n_eyes,
+                        const omg_dome_panel* leaves, uint32_t n_leaves, uint32_t n_rays, uint32_t max_events,
+                        uint32_t want, void* cuda_stream) {
+  if (!ctx) return OMG_E_INVALID;
+  auto it = ctx->probes.find(probe_id);
+  if (it == ctx->probes.end()) return OMG_E_NOT_FOUND;
+  cudaStream_t s = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : ctx->stream;
+  return dome_submit(ctx, *it->second, eyes, n_eyes, leaves, n_leaves, n_rays, max_events, want & 7u, s);
+}
+
+int32_t omg_dome_collect(omg_ctx* ctx, uint32_t probe_id, omg_dome_bin* out, float* raw_energy, uint8_t* escape,
+                         float* ray_tp) {
+  if (!ctx) return OMG_E_INVALID;
+  auto it = ctx->probes.find(probe_id);
+  if (it == ctx->probes.end()) return OMG_E_NOT_FOUND;
+  return dome_collect(ctx, *it->second, out, raw_energy, escape, ray_tp);
 }
 
 // Segments (escape events + straight-through calls) of the probe's last sample.

@@ -474,6 +474,35 @@ class DomeProbe:
         rc = lib().omg_dome_sample(self.ctx.h, self.id, _p(eyes), n_eyes, arr, len(leaves), n_rays, max_events, out,
                                    _p(raw), _p(esc), _p(tp))
         self.ctx._check(rc, "omg_dome_sample")
+        return self._result(out, n_eyes, raw, esc, tp)
+
+    def submit(self, eyes, leaves: Sequence = (), n_rays: Optional[int] = None, max_events: int = 6,
+               stream: int = 0, want: int = 0):
+        """Enqueue a sample on a CUDA stream (0: the context's) and return at
+        once (omg_dome_submit); collect() waits for it. want: 1 raw, 2 escape,
+        4 per-ray throughput."""
+        eyes = np.ascontiguousarray(eyes, np.float32).reshape(-1, 3)
+        n_rays = n_rays or self.n_fan
+        arr = dome_panels_to_c(leaves, self.nb)
+        rc = lib().omg_dome_submit(self.ctx.h, self.id, _p(eyes), len(eyes), arr, len(leaves), n_rays, max_events,
+                                   want, C.c_void_p(stream) if stream else None)
+        self.ctx._check(rc, "omg_dome_submit")
+        self._pending = (len(eyes), n_rays, want)
+
+    def collect(self):
+        n_eyes, n_rays, want = self._pending
+        nb = self.nb
+        out = (_lib.omg_dome_bin * (9 * n_eyes))()
+        raw = np.zeros((n_eyes, 9, nb), np.float32)
+        esc = np.zeros((n_eyes, n_rays), np.uint8)
+        tp = np.zeros((n_eyes, n_rays, nb), np.float32)
+        rc = lib().omg_dome_collect(self.ctx.h, self.id, out, _p(raw), _p(esc), _p(tp))
+        self.ctx._check(rc, "omg_dome_collect")
+        return self._result(out, n_eyes, raw if want & 1 else None, esc if want & 2 else None,
+                            tp if want & 4 else None)
+
+    def _result(self, out, n_eyes, raw, esc, tp):
+        nb = self.nb
         energy = np.array([[out[e * 9 + k].energy[:nb] for k in range(9)] for e in range(n_eyes)], np.float32)
         dirs = np.array([[out[e * 9 + k].dir[:] for k in range(9)] for e in range(n_eyes)], np.float32)
         ev, th = C.c_uint64(), C.c_uint64()

@@ -83,3 +83,38 @@ def test_dome_matches_f32_oracle_exactly(ctx, oracle):
         assert np.array_equal(g["dir"][e], r32["dir"])
     probe.destroy()
     scene.release()
+
+
+def test_dome_submit_collect_overlapping_a_batch(ctx_tie):
+    """omg_dome_submit on a second stream, a batch trace on the context's
+    stream meanwhile, then omg_dome_collect: the same bins, flags and
+    throughputs as the synchronous call (the fan is deterministic)."""
+    import torch
+    from omg_audio_gb300 import Job
+    ctx = ctx_tie
+    case = W.multiroom(seed=2)
+    mb = MeshBuilder()
+    case.recorder.replay(mb)
+    scene = ctx.upload_builder(mb)
+    eyes = case.listeners[:32]
+    ref_probe = DomeProbe(ctx, scene, case.glass, n_fan=512)
+    ref = ref_probe.sample(eyes, n_rays=512)
+    probe = DomeProbe(ctx, scene, case.glass, n_fan=512)
+    side = torch.cuda.Stream()
+    probe.submit(eyes, n_rays=512, stream=side.cuda_stream, want=7)
+    jobs = [Job(src, lis, 2048, seed=40 + p, scene=scene, panel_offset=0, n_panels=len(case.panels))
+            for p, (src, lis) in enumerate(case.pairs[:8])]
+    res = ctx.trace_batch(jobs, case.panels)
+    got = probe.collect()
+    assert all(rv.segments > 0 for _, rv in res)
+    for k in ("energy", "dir", "raw", "escape", "ray_tp"):
+        assert np.array_equal(got[k], ref[k]), k
+    assert got["segments"] == ref["segments"]
+    # a second submit before collect is refused
+    probe.submit(eyes, n_rays=512)
+    with pytest.raises(Exception):
+        probe.submit(eyes, n_rays=512)
+    probe.collect()
+    probe.destroy()
+    ref_probe.destroy()
+    scene.release()
