@@ -342,6 +342,51 @@ int32_t omg_dome_collect(omg_ctx* ctx, uint32_t probe_id, omg_dome_bin* out, flo
  * trace_through calls (dome.rs:390-422), summed over listeners. */
 int32_t omg_dome_segments(omg_ctx* ctx, uint32_t probe_id, uint64_t* escape_events, uint64_t* through_calls);
 
+/* --------------------------------------------------------------- surrogate */
+/* No counterpart in the reference: the learned surrogate of the tracer. An
+ * ensemble of `members` MLPs n_in -> hidden (x n_hidden, GELU) -> n_out,
+ * trained on the GPU with tensor-core (tcgen05) BF16 GEMMs accumulating in
+ * FP32, FP32 master weights and AdamW. Inputs and targets are standardized
+ * per column from the training data. */
+typedef struct omg_mlp_config {
+    uint32_t n_in;               /* 38 for the room surrogate */
+    uint32_t hidden;             /* multiple of 16, <= 256 */
+    uint32_t n_hidden;           /* hidden layers (4) */
+    uint32_t n_out;              /* <= 256 (192 = 64 log-time bins x 3 bands) */
+    uint32_t members;            /* ensemble size, 1..16: their spread is the uncertainty */
+    uint32_t seed;               /* weight init */
+} omg_mlp_config;
+typedef struct omg_mlp_train_config {
+    uint32_t epochs;
+    uint32_t batch;              /* multiple of 128 */
+    float lr, lr_final;          /* cosine decay from lr to lr_final over all steps */
+    float weight_decay;          /* AdamW, on weights (not biases) */
+    float beta1, beta2, eps;
+    uint32_t seed;               /* shuffling */
+} omg_mlp_train_config;
+int32_t omg_mlp_create(omg_ctx* ctx, const omg_mlp_config* cfg, uint32_t* mlp_id);
+int32_t omg_mlp_destroy(omg_ctx* ctx, uint32_t mlp_id);
+/* The training set, n rows of n_in inputs and n_out targets (host, row-major). */
+int32_t omg_mlp_set_data(omg_ctx* ctx, uint32_t mlp_id, const float* x, const float* y, uint32_t n);
+/* Train every member for `epochs` passes over the data; epoch_loss (nullable,
+ * members x epochs): the standardized MSE of each epoch's last batch. */
+int32_t omg_mlp_train(omg_ctx* ctx, uint32_t mlp_id, const omg_mlp_train_config* cfg, float* epoch_loss);
+/* Predict n rows: ensemble mean (and spread, nullable) in the targets' units. */
+int32_t omg_surrogate_predict(omg_ctx* ctx, uint32_t mlp_id, const float* x, uint32_t n, float* y_mean,
+                              float* y_std);
+/* One forward + backward of `member` on standardized x, y (n multiple of 128):
+ * the loss and every layer's gradients (W row-major, then b), layer by layer. */
+int32_t omg_mlp_grad(omg_ctx* ctx, uint32_t mlp_id, uint32_t member, const float* x, const float* y, uint32_t n,
+                     float* loss, float* grads);
+/* Checkpoint: what = 1 standardization + weights, 2 AdamW moments + step.
+ * out = NULL returns the count only. set_params restores the same layout. */
+int32_t omg_mlp_params(omg_ctx* ctx, uint32_t mlp_id, uint32_t what, float* out, uint64_t* count);
+int32_t omg_mlp_set_params(omg_ctx* ctx, uint32_t mlp_id, uint32_t what, const float* in, uint64_t count);
+/* The tensor-core GEMM alone (tests): C[m x n] = A[m x k] . B[n x k]^T, A and B
+ * bf16 bit patterns, row-major with k contiguous; C f32. */
+int32_t omg_tc_gemm(omg_ctx* ctx, const uint16_t* a, const uint16_t* b, float* c, uint32_t m, uint32_t n,
+                    uint32_t k);
+
 /* ---------------------------------------------------------------- no-alloc */
 /* No counterpart in the reference: an addition of this library.
  * omg_trace_box for callers that must not allocate device memory: an audio

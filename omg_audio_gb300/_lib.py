@@ -73,6 +73,17 @@ class omg_tune_result(C.Structure):
                 ("epochs", C.c_uint32), ("park_pct", C.c_uint32), ("ms", C.c_float)]
 
 
+class omg_mlp_config(C.Structure):
+    _fields_ = [("n_in", C.c_uint32), ("hidden", C.c_uint32), ("n_hidden", C.c_uint32), ("n_out", C.c_uint32),
+                ("members", C.c_uint32), ("seed", C.c_uint32)]
+
+
+class omg_mlp_train_config(C.Structure):
+    _fields_ = [("epochs", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_float), ("lr_final", C.c_float),
+                ("weight_decay", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+                ("seed", C.c_uint32)]
+
+
 P, U32, U64, I32, F = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int32, C.c_float
 PU32, PU64 = C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)
 
@@ -126,6 +137,15 @@ SIGNATURES = {
     "omg_dome_submit": (I32, [P, U32, C.c_void_p, U32, C.c_void_p, U32, U32, U32, U32, C.c_void_p]),
     "omg_dome_collect": (I32, [P, U32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "omg_dome_segments": (I32, [P, U32, PU64, PU64]),
+    "omg_mlp_create": (I32, [P, C.POINTER(omg_mlp_config), PU32]),
+    "omg_mlp_destroy": (I32, [P, U32]),
+    "omg_mlp_set_data": (I32, [P, U32, P, P, U32]),
+    "omg_mlp_train": (I32, [P, U32, C.POINTER(omg_mlp_train_config), P]),
+    "omg_surrogate_predict": (I32, [P, U32, P, U32, P, P]),
+    "omg_mlp_grad": (I32, [P, U32, U32, P, P, U32, P, P]),
+    "omg_mlp_params": (I32, [P, U32, U32, P, PU64]),
+    "omg_mlp_set_params": (I32, [P, U32, U32, P, U64]),
+    "omg_tc_gemm": (I32, [P, P, P, P, U32, U32, U32]),
     "omg_trace_box_noalloc": (I32, [C.POINTER(omg_box_job), C.POINTER(omg_params), P, P, P]),
 }
 

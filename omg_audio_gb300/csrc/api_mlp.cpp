@@ -1,0 +1,555 @@
+// C ABI of the GB300 tracer (include/omg_cuda.h), part 4: the learned
+// surrogate. An ensemble of MLPs (n_in -> hidden x n_hidden -> n_out, GELU)
+// trained on the GPU with the tensor-core GEMM (mlp.cu): BF16 weights and
+// activations, FP32 accumulation, FP32 master weights, AdamW with a cosine
+// learning-rate decay, MSE on standardized targets. Inference returns the
+// ensemble mean and spread in the caller's units.
+#include <cmath>
+#include <numeric>
+#include <random>
+
+#include "runtime.h"
+
+using namespace omg;
+
+namespace omg {
+
+struct MlpLayer {
+  uint32_t in = 0, out = 0;
+  DevBuf<float> W, b, mW, vW, mb, vb, gW, gb;
+  DevBuf<uint16_t> Wh;   // bf16 copy of W
+};
+
+struct MlpRec {
+  omg_mlp_config cfg{};
+  std::vector<std::vector<MlpLayer>> members;   // [member][layer]
+  // standardization (host and device)
+  std::vector<float> x_mean, x_std, y_mean, y_std;
+  DevBuf<float> d_x_mean, d_x_std;
+  // dataset (standardized, device)
+  uint32_t n_data = 0;
+  DevBuf<float> X, Y;
+  DevBuf<uint32_t> perm;
+  uint64_t step = 0;
+  // work buffers for a batch of `cap` rows
+  uint32_t cap = 0;
+  DevBuf<uint16_t> xh;                    // batch input (bf16)
+  DevBuf<float> t;                        // batch targets
+  std::vector<DevBuf<float>> Z;           // pre-activations per layer
+  std::vector<DevBuf<uint16_t>> A;        // bf16 activations per hidden layer
+  DevBuf<float> out, dY, dX, dZ, loss_parts;
+  DevBuf<uint16_t> dZh;
+  DevBuf<uint32_t> err;
+  PinBuf<float> h_loss;
+};
+
+}  // namespace omg
+
+namespace {
+
+constexpr uint32_t kLossParts = 64;
+
+uint32_t n_layers(const MlpRec& M) { return M.cfg.n_hidden + 1; }
+
+int32_t ensure_batch(omg_ctx* ctx, MlpRec& M, uint32_t rows) {
+  if (rows <= M.cap) return OMG_OK;
+  const uint32_t L = n_layers(M), H = M.cfg.hidden;
+  CK(M.xh.alloc((size_t)rows * M.cfg.n_in));
+  CK(M.t.alloc((size_t)rows * M.cfg.n_out));
+  M.Z.resize(L);
+  M.A.resize(L);
+  for (uint32_t l = 0; l < L; l++) {
+    const uint32_t o = l + 1 == L ? M.cfg.n_out : H;
+    CK(M.Z[l].alloc((size_t)rows * o));
+    CK(M.A[l].alloc((size_t)rows * o));
+  }
+  const uint32_t wide = std::max(std::max(H, M.cfg.n_out), M.cfg.n_in);
+  CK(M.out.alloc((size_t)rows * M.cfg.n_out));
+  CK(M.dY.alloc((size_t)rows * wide));
+  CK(M.dX.alloc((size_t)rows * wide));
+  CK(M.dZ.alloc((size_t)rows * wide));
+  CK(M.dZh.alloc((size_t)rows * wide));
+  M.cap = rows;
+  return OMG_OK;
+}
+
+// X0 (bf16, rows x n_in) -> out (f32, rows x n_out); keeps Z and A for backward
+int32_t forward(omg_ctx* ctx, MlpRec& M, uint32_t e, uint32_t rows, cudaStream_t s) {
+  const uint32_t L = n_layers(M);
+  auto& net = M.members[e];
+  const uint16_t* x = M.xh.p;
+  uint32_t in = M.cfg.n_in;
+  for (uint32_t l = 0; l < L; l++) {
+    MlpLayer& Ly = net[l];
+    const bool last = l + 1 == L;
+    GemmArgs g{};
+    g.A = x;
+    g.a_rs = in;
+    g.a_ks = 1;
+    g.B = Ly.Wh.p;
+    g.b_rs = Ly.in;
+    g.b_ks = 1;
+    g.M = rows;
+    g.N = Ly.out;
+    g.K = in;
+    g.n_tile = Ly.out <= 256 ? ((Ly.out + 15) & ~15u) : 256;
+    g.bias = Ly.b.p;
+    g.err = M.err.p;
+    if (last) {
+      g.D = M.out.p;
+      g.ldd = Ly.out;
+    } else {
+      g.Z = M.Z[l].p;
+      g.ldz = Ly.out;
+      g.Y = M.A[l].p;
+      g.ldy = Ly.out;
+      g.act = 1;
+    }
+    CK(launch_gemm(g, 1, s));
+    x = M.A[l].p;
+    in = Ly.out;
+  }
+  return OMG_OK;
+}
+
+// gradients of the MSE (targets in M.t) into the layers' gW, gb; loss parts
+int32_t backward(omg_ctx* ctx, MlpRec& M, uint32_t e, uint32_t rows, cudaStream_t s) {
+  const uint32_t L = n_layers(M);
+  auto& net = M.members[e];
+  CK(launch_mse(M.out.p, M.t.p, nullptr, rows, M.cfg.n_out, M.dZ.p, M.dZh.p, M.loss_parts.p, kLossParts, s));
+  for (int l = (int)L - 1; l >= 0; l--) {
+    MlpLayer& Ly = net[l];
+    const uint16_t* xin = l == 0 ? M.xh.p : M.A[l - 1].p;
+    // dW = dZ^T . X  (reduction over the batch, split over grid z)
+    CK(cudaMemsetAsync(Ly.gW.p, 0, (size_t)Ly.out * Ly.in * 4, s));
+    GemmArgs g{};
+    g.A = M.dZh.p;
+    g.a_rs = 1;
+    g.a_ks = Ly.out;
+    g.B = xin;
+    g.b_rs = 1;
+    g.b_ks = Ly.in;
+    g.M = Ly.out;
+    g.N = Ly.in;
+    g.K = rows;
+    g.n_tile = Ly.in <= 256 ? ((Ly.in + 15) & ~15u) : 256;
+    g.D = Ly.gW.p;
+    g.ldd = Ly.in;
+    g.accumulate = 1;
+    g.err = M.err.p;
+    const uint32_t split = std::max(1u, std::min(32u, rows / 256u));
+    CK(launch_gemm(g, split, s));
+    CK(launch_colsum(M.dZ.p, rows, Ly.out, Ly.gb.p, s));
+    if (l == 0) break;
+    // dX = dZ . W, then dZ of the layer below through GELU'
+    GemmArgs h{};
+    h.A = M.dZh.p;
+    h.a_rs = Ly.out;
+    h.a_ks = 1;
+    h.B = Ly.Wh.p;
+    h.b_rs = 1;
+    h.b_ks = Ly.in;
+    h.M = rows;
+    h.N = Ly.in;
+    h.K = Ly.out;
+    h.n_tile = Ly.in <= 256 ? ((Ly.in + 15) & ~15u) : 256;
+    h.D = M.dX.p;
+    h.ldd = Ly.in;
+    h.err = M.err.p;
+    CK(launch_gemm(h, 1, s));
+    CK(launch_gelu_back(M.dX.p, M.Z[l - 1].p, M.dZ.p, M.dZh.p, (uint64_t)rows * Ly.in, s));
+  }
+  return OMG_OK;
+}
+
+int32_t check_err(omg_ctx* ctx, MlpRec& M) {
+  uint32_t e = 0;
+  CK(cudaMemcpyAsync(&e, M.err.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (e) {
+    ctx->last_error = "surrogate GEMM: an mbarrier wait ran out";
+    CK(cudaMemsetAsync(M.err.p, 0, 4, ctx->stream));
+    return OMG_E_TIMEOUT;
+  }
+  return OMG_OK;
+}
+
+bool valid_cfg(const omg_mlp_config& c) {
+  return c.n_in >= 1 && c.n_in <= 1024 && c.hidden >= 16 && c.hidden <= 256 && c.hidden % 16 == 0 &&
+         c.n_hidden >= 1 && c.n_hidden <= 16 && c.n_out >= 1 && c.n_out <= 256 && c.members >= 1 &&
+         c.members <= 16;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t omg_mlp_create(omg_ctx* ctx, const omg_mlp_config* cfg, uint32_t* id) {
+  if (!ctx || !cfg || !id || !valid_cfg(*cfg)) return OMG_E_INVALID;
+  std::shared_ptr<MlpRec> M(new MlpRec());
+  M->cfg = *cfg;
+  const uint32_t L = cfg->n_hidden + 1;
+  std::mt19937_64 rng(cfg->seed ? cfg->seed : 1u);
+  M->members.resize(cfg->members);
+  for (uint32_t e = 0; e < cfg->members; e++) {
+    M->members[e].resize(L);
+    uint32_t in = cfg->n_in;
+    for (uint32_t l = 0; l < L; l++) {
+      MlpLayer& Ly = M->members[e][l];
+      Ly.in = in;
+      Ly.out = l + 1 == L ? cfg->n_out : cfg->hidden;
+      const size_t nw = (size_t)Ly.out * Ly.in;
+      // He-style normal init (std sqrt(2 / fan_in)), zero biases
+      std::normal_distribution<float> nd(0.0f, std::sqrt(2.0f / (float)Ly.in));
+      std::vector<float> w(nw);
+      for (auto& v : w) v = nd(rng);
+      if (l + 1 == L)
+        for (auto& v : w) v *= 0.5f;
+      CK(Ly.W.alloc(nw));
+      CK(Ly.Wh.alloc(nw));
+      CK(Ly.mW.alloc(nw));
+      CK(Ly.vW.alloc(nw));
+      CK(Ly.gW.alloc(nw));
+      CK(Ly.b.alloc(Ly.out));
+      CK(Ly.mb.alloc(Ly.out));
+      CK(Ly.vb.alloc(Ly.out));
+      CK(Ly.gb.alloc(Ly.out));
+      CK(cudaMemcpy(Ly.W.p, w.data(), nw * 4, cudaMemcpyHostToDevice));
+      CK(cudaMemset(Ly.mW.p, 0, nw * 4));
+      CK(cudaMemset(Ly.vW.p, 0, nw * 4));
+      CK(cudaMemset(Ly.b.p, 0, Ly.out * 4));
+      CK(cudaMemset(Ly.mb.p, 0, Ly.out * 4));
+      CK(cudaMemset(Ly.vb.p, 0, Ly.out * 4));
+      CK(launch_to_bf16(Ly.W.p, Ly.Wh.p, nw, ctx->stream));
+      in = Ly.out;
+    }
+  }
+  M->x_mean.assign(cfg->n_in, 0.0f);
+  M->x_std.assign(cfg->n_in, 1.0f);
+  M->y_mean.assign(cfg->n_out, 0.0f);
+  M->y_std.assign(cfg->n_out, 1.0f);
+  CK(M->loss_parts.alloc(kLossParts));
+  CK(M->h_loss.alloc(kLossParts));
+  CK(M->err.alloc(1));
+  CK(cudaMemsetAsync(M->err.p, 0, 4, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *id = ctx->next_mlp++;
+  ctx->mlps[*id] = M;
+  return OMG_OK;
+}
+
+int32_t omg_mlp_destroy(omg_ctx* ctx, uint32_t id) {
+  if (!ctx) return OMG_E_INVALID;
+  auto it = ctx->mlps.find(id);
+  if (it == ctx->mlps.end()) return OMG_E_NOT_FOUND;
+  cudaStreamSynchronize(ctx->stream);
+  ctx->mlps.erase(it);
+  return OMG_OK;
+}
+
+int32_t omg_mlp_set_data(omg_ctx* ctx, uint32_t id, const float* x, const float* y, uint32_t n) {
+  if (!ctx || !x || !y || n == 0) return OMG_E_INVALID;
+  auto it = ctx->mlps.find(id);
+  if (it == ctx->mlps.end()) return OMG_E_NOT_FOUND;
+  MlpRec& M = *it->second;
+  const uint32_t ni = M.cfg.n_in, no = M.cfg.n_out;
+  // standardization from the data (FP64 sums)
+  for (int which = 0; which < 2; which++) {
+    const float* d = which ? y : x;
+    const uint32_t c = which ? no : ni;
+    std::vector<double> s(c, 0.0), q(c, 0.0);
+    for (uint64_t i = 0; i < n; i++)
+      for (uint32_t k = 0; k < c; k++) {
+        const double v = d[i * c + k];
+        if (!std::isfinite(v)) return OMG_E_INVALID;
+        s[k] += v;
+        q[k] += v * v;
+      }
+    std::vector<float>& mean = which ? M.y_mean : M.x_mean;
+    std::vector<float>& sd = which ? M.y_std : M.x_std;
+    for (uint32_t k = 0; k < c; k++) {
+      const double m = s[k] / n, var = std::max(q[k] / n - m * m, 0.0);
+      mean[k] = (float)m;
+      sd[k] = (float)std::max(std::sqrt(var), 1e-6);
+    }
+  }
+  std::vector<float> xs((size_t)n * ni), ys((size_t)n * no);
+  for (uint64_t i = 0; i < n; i++) {
+    for (uint32_t k = 0; k < ni; k++) xs[i * ni + k] = (x[i * ni + k] - M.x_mean[k]) / M.x_std[k];
+    for (uint32_t k = 0; k < no; k++) ys[i * no + k] = (y[i * no + k] - M.y_mean[k]) / M.y_std[k];
+  }
+  CK(M.X.alloc(xs.size()));
+  CK(M.Y.alloc(ys.size()));
+  CK(M.perm.alloc(n));
+  CK(cudaMemcpy(M.X.p, xs.data(), xs.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(M.Y.p, ys.data(), ys.size() * 4, cudaMemcpyHostToDevice));
+  M.n_data = n;
+  return OMG_OK;
+}
+
+int32_t omg_mlp_train(omg_ctx* ctx, uint32_t id, const omg_mlp_train_config* tc, float* epoch_loss) {
+  if (!ctx || !tc || tc->epochs == 0 || tc->batch == 0 || tc->batch % 128 != 0) return OMG_E_INVALID;
+  auto it = ctx->mlps.find(id);
+  if (it == ctx->mlps.end()) return OMG_E_NOT_FOUND;
+  MlpRec& M = *it->second;
+  if (M.n_data < tc->batch) return OMG_E_INVALID;
+  int32_t rc = ensure_batch(ctx, M, tc->batch);
+  if (rc) return rc;
+  cudaStream_t s = ctx->stream;
+  const uint32_t L = n_layers(M), B = tc->batch;
+  const uint32_t steps_per_epoch = M.n_data / B;
+  const uint64_t total = (uint64_t)steps_per_epoch * tc->epochs;
+  std::mt19937_64 rng(tc->seed ? tc->seed : 7u);
+  std::vector<uint32_t> perm(M.n_data);
+  for (uint32_t e = 0; e < M.cfg.members; e++) {
+    uint64_t t = 0;
+    for (uint32_t ep = 0; ep < tc->epochs; ep++) {
+      std::iota(perm.begin(), perm.end(), 0u);
+      std::shuffle(perm.begin(), perm.end(), rng);
+      CK(cudaMemcpyAsync(M.perm.p, perm.data(), (size_t)M.n_data * 4, cudaMemcpyHostToDevice, s));
+      double ep_loss = 0.0;
+      for (uint32_t st = 0; st < steps_per_epoch; st++, t++) {
+        CK(launch_gather_rows(M.X.p, M.cfg.n_in, M.perm.p + (size_t)st * B, B, nullptr, M.xh.p, s));
+        CK(launch_gather_rows(M.Y.p, M.cfg.n_out, M.perm.p + (size_t)st * B, B, M.t.p, nullptr, s));
+        if ((rc = forward(ctx, M, e, B, s))) return rc;
+        if ((rc = backward(ctx, M, e, B, s))) return rc;
+        // cosine decay from lr to lr_final
+        const double prog = total > 1 ? (double)t / (double)(total - 1) : 1.0;
+        const float lr = (float)(tc->lr_final + 0.5 * (tc->lr - tc->lr_final) * (1.0 + std::cos(3.14159265358979323846 * prog)));
+        const double step = (double)(t + 1);
+        const float bc1 = (float)(1.0 - std::pow((double)tc->beta1, step));
+        const float bc2 = (float)(1.0 - std::pow((double)tc->beta2, step));
+        for (uint32_t l = 0; l < L; l++) {
+          MlpLayer& Ly = M.members[e][l];
+          CK(launch_adamw(Ly.W.p, Ly.mW.p, Ly.vW.p, Ly.gW.p, Ly.Wh.p, (uint64_t)Ly.out * Ly.in, lr, tc->beta1,
+                          tc->beta2, tc->eps, tc->weight_decay, bc1, bc2, s));
+          CK(launch_adamw(Ly.b.p, Ly.mb.p, Ly.vb.p, Ly.gb.p, nullptr, Ly.out, lr, tc->beta1, tc->beta2, tc->eps,
+                          0.0f, bc1, bc2, s));
+        }
+        if (epoch_loss && (st + 1 == steps_per_epoch)) {
+          CK(cudaMemcpyAsync(M.h_loss.p, M.loss_parts.p, kLossParts * 4, cudaMemcpyDeviceToHost, s));
+          CK(cudaStreamSynchronize(s));
+          for (uint32_t k = 0; k < kLossParts; k++) ep_loss += M.h_loss.p[k];
+        }
+      }
+      if (epoch_loss) epoch_loss[(size_t)e * tc->epochs + ep] = (float)ep_loss;
+    }
+  }
+  M.step += total;
+  return check_err(ctx, M);
+}
+
+int32_t omg_surrogate_predict(omg_ctx* ctx, uint32_t id, const float* x, uint32_t n, float* y_mean, float* y_std) {
+  if (!ctx || !x || !y_mean || n == 0) return OMG_E_INVALID;
+  auto it = ctx->mlps.find(id);
+  if (it == ctx->mlps.end()) return OMG_E_NOT_FOUND;
+  MlpRec& M = *it->second;
+  const uint32_t ni = M.cfg.n_in, no = M.cfg.n_out, E = M.cfg.members;
+  const uint32_t chunk = 16384;
+  int32_t rc = ensure_batch(ctx, M, std::min(n, chunk));
+  if (rc) return rc;
+  cudaStream_t s = ctx->stream;
+  std::vector<float> xs((size_t)std::min(n, chunk) * ni), yo((size_t)std::min(n, chunk) * no);
+  std::vector<double> acc, acc2;
+  DevBuf<float> xd;
+  CK(xd.alloc(xs.size()));
+  for (uint32_t r0 = 0; r0 < n; r0 += chunk) {
+    const uint32_t rows = std::min(chunk, n - r0);
+    for (uint64_t i = 0; i < rows; i++)
+      for (uint32_t k = 0; k < ni; k++)
+        xs[i * ni + k] = (x[(r0 + i) * ni + k] - M.x_mean[k]) / M.x_std[k];
+    CK(cudaMemcpyAsync(xd.p, xs.data(), (size_t)rows * ni * 4, cudaMemcpyHostToDevice, s));
+    CK(launch_to_bf16(xd.p, M.xh.p, (uint64_t)rows * ni, s));
+    acc.assign((size_t)rows * no, 0.0);
+    acc2.assign((size_t)rows * no, 0.0);
+    for (uint32_t e = 0; e < E; e++) {
+      if ((rc = forward(ctx, M, e, rows, s))) return rc;
+      CK(cudaMemcpyAsync(yo.data(), M.out.p, (size_t)rows * no * 4, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      for (uint64_t i = 0; i < (uint64_t)rows * no; i++) {
+        const double v = (double)yo[i] * M.y_std[i % no] + M.y_mean[i % no];
+        acc[i] += v;
+        acc2[i] += v * v;
+      }
+    }
+    for (uint64_t i = 0; i < (uint64_t)rows * no; i++) {
+      const double m = acc[i] / E;
+      y_mean[(uint64_t)r0 * no + i] = (float)m;
+      if (y_std) y_std[(uint64_t)r0 * no + i] = (float)std::sqrt(std::max(acc2[i] / E - m * m, 0.0));
+    }
+  }
+  return check_err(ctx, M);
+}
+
+// One forward/backward of `member` on standardized inputs and targets: the
+// loss and the gradients of every layer (W row-major, then b), in order.
+int32_t omg_mlp_grad(omg_ctx* ctx, uint32_t id, uint32_t member, const float* x, const float* y, uint32_t n,
+                     float* loss, float* grads) {
+  if (!ctx || !x || !y || n == 0 || n % 128 != 0) return OMG_E_INVALID;
+  auto it = ctx->mlps.find(id);
+  if (it == ctx->mlps.end()) return OMG_E_NOT_FOUND;
+  MlpRec& M = *it->second;
+  if (member >= M.cfg.members) return OMG_E_INVALID;
+  int32_t rc = ensure_batch(ctx, M, n);
+  if (rc) return rc;
+  cudaStream_t s = ctx->stream;
+  DevBuf<float> xd;
+  CK(xd.alloc((size_t)n * M.cfg.n_in));
+  CK(cudaMemcpyAsync(xd.p, x, (size_t)n * M.cfg.n_in * 4, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(M.t.p, y, (size_t)n * M.cfg.n_out * 4, cudaMemcpyHostToDevice, s));
+  CK(launch_to_bf16(xd.p, M.xh.p, (uint64_t)n * M.cfg.n_in, s));
+  if ((rc = forward(ctx, M, member, n, s))) return rc;
+  if ((rc = backward(ctx, M, member, n, s))) return rc;
+  CK(cudaMemcpyAsync(M.h_loss.p, M.loss_parts.p, kLossParts * 4, cudaMemcpyDeviceToHost, s));
+  size_t off = 0;
+  for (auto& Ly : M.members[member]) {
+    if (grads) {
+      CK(cudaMemcpyAsync(grads + off, Ly.gW.p, (size_t)Ly.out * Ly.in * 4, cudaMemcpyDeviceToHost, s));
+      off += (size_t)Ly.out * Ly.in;
+      CK(cudaMemcpyAsync(grads + off, Ly.gb.p, (size_t)Ly.out * 4, cudaMemcpyDeviceToHost, s));
+      off += Ly.out;
+    }
+  }
+  CK(cudaStreamSynchronize(s));
+  if (loss) {
+    double l = 0.0;
+    for (uint32_t k = 0; k < kLossParts; k++) l += M.h_loss.p[k];
+    *loss = (float)l;
+  }
+  return check_err(ctx, M);
+}
+
+// Parameters: what = 1: standardization (x mean, x std, y mean, y std) then
+// every member's layers (W row-major, b); what = 2: the AdamW moments (mW, vW,
+// mb, vb per layer per member) then the step count. out = null: count only.
+int32_t omg_mlp_params(omg_ctx* ctx, uint32_t id, uint32_t what, float* out, uint64_t* count) {
+  if (!ctx || !count || (what != 1 && what != 2)) return OMG_E_INVALID;
+  auto it = ctx->mlps.find(id);
+  if (it == ctx->mlps.end()) return OMG_E_NOT_FOUND;
+  MlpRec& M = *it->second;
+  uint64_t n = 0;
+  auto put_host = [&](const std::vector<float>& v) {
+    if (out) std::copy(v.begin(), v.end(), out + n);
+    n += v.size();
+  };
+  auto put_dev = [&](const float* p, size_t k) -> cudaError_t {
+    if (out) {
+      cudaError_t e = cudaMemcpy(out + n, p, k * 4, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return e;
+    }
+    n += k;
+    return cudaSuccess;
+  };
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (what == 1) {
+    put_host(M.x_mean);
+    put_host(M.x_std);
+    put_host(M.y_mean);
+    put_host(M.y_std);
+    for (auto& net : M.members)
+      for (auto& Ly : net) {
+        CK(put_dev(Ly.W.p, (size_t)Ly.out * Ly.in));
+        CK(put_dev(Ly.b.p, Ly.out));
+      }
+  } else {
+    for (auto& net : M.members)
+      for (auto& Ly : net) {
+        CK(put_dev(Ly.mW.p, (size_t)Ly.out * Ly.in));
+        CK(put_dev(Ly.vW.p, (size_t)Ly.out * Ly.in));
+        CK(put_dev(Ly.mb.p, Ly.out));
+        CK(put_dev(Ly.vb.p, Ly.out));
+      }
+    if (out) out[n] = (float)M.step;
+    n += 1;
+  }
+  *count = n;
+  return OMG_OK;
+}
+
+int32_t omg_mlp_set_params(omg_ctx* ctx, uint32_t id, uint32_t what, const float* in, uint64_t count) {
+  if (!ctx || !in || (what != 1 && what != 2)) return OMG_E_INVALID;
+  auto it = ctx->mlps.find(id);
+  if (it == ctx->mlps.end()) return OMG_E_NOT_FOUND;
+  MlpRec& M = *it->second;
+  uint64_t need = 0;
+  int32_t rc = omg_mlp_params(ctx, id, what, nullptr, &need);
+  if (rc) return rc;
+  if (count != need) return OMG_E_INVALID;
+  uint64_t n = 0;
+  auto get_host = [&](std::vector<float>& v) {
+    std::copy(in + n, in + n + v.size(), v.begin());
+    n += v.size();
+  };
+  auto get_dev = [&](float* p, size_t k) -> cudaError_t {
+    cudaError_t e = cudaMemcpy(p, in + n, k * 4, cudaMemcpyHostToDevice);
+    n += k;
+    return e;
+  };
+  if (what == 1) {
+    get_host(M.x_mean);
+    get_host(M.x_std);
+    get_host(M.y_mean);
+    get_host(M.y_std);
+    for (auto& net : M.members)
+      for (auto& Ly : net) {
+        CK(get_dev(Ly.W.p, (size_t)Ly.out * Ly.in));
+        CK(get_dev(Ly.b.p, Ly.out));
+        CK(launch_to_bf16(Ly.W.p, Ly.Wh.p, (uint64_t)Ly.out * Ly.in, ctx->stream));
+      }
+  } else {
+    for (auto& net : M.members)
+      for (auto& Ly : net) {
+        CK(get_dev(Ly.mW.p, (size_t)Ly.out * Ly.in));
+        CK(get_dev(Ly.vW.p, (size_t)Ly.out * Ly.in));
+        CK(get_dev(Ly.mb.p, Ly.out));
+        CK(get_dev(Ly.vb.p, Ly.out));
+      }
+    M.step = (uint64_t)in[n];
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return OMG_OK;
+}
+
+// The tensor-core GEMM alone: C[M x N] (f32) = A[M x K] . B[N x K]^T, A and B
+// given as bf16 bit patterns in host memory (row-major, K contiguous).
+int32_t omg_tc_gemm(omg_ctx* ctx, const uint16_t* a, const uint16_t* b, float* c, uint32_t m, uint32_t n,
+                    uint32_t k) {
+  if (!ctx || !a || !b || !c || m == 0 || n == 0 || k == 0) return OMG_E_INVALID;
+  cudaStream_t s = ctx->stream;
+  DevBuf<uint16_t> da, db;
+  DevBuf<float> dc;
+  DevBuf<uint32_t> err;
+  CK(da.alloc((size_t)m * k));
+  CK(db.alloc((size_t)n * k));
+  CK(dc.alloc((size_t)m * n));
+  CK(err.alloc(1));
+  CK(cudaMemsetAsync(err.p, 0, 4, s));
+  CK(cudaMemcpyAsync(da.p, a, (size_t)m * k * 2, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(db.p, b, (size_t)n * k * 2, cudaMemcpyHostToDevice, s));
+  GemmArgs g{};
+  g.A = da.p;
+  g.a_rs = k;
+  g.a_ks = 1;
+  g.B = db.p;
+  g.b_rs = k;
+  g.b_ks = 1;
+  g.M = m;
+  g.N = n;
+  g.K = k;
+  g.n_tile = n <= 256 ? ((n + 15) & ~15u) : 256;
+  g.D = dc.p;
+  g.ldd = n;
+  g.err = err.p;
+  CK(launch_gemm(g, 1, s));
+  uint32_t e = 0;
+  CK(cudaMemcpyAsync(c, dc.p, (size_t)m * n * 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (e) {
+    ctx->last_error = "tensor-core GEMM: an mbarrier wait ran out";
+    return OMG_E_TIMEOUT;
+  }
+  return OMG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,300 @@
+// The surrogate's dense layers on the tensor cores: a tcgen05 GEMM with the
+// accumulator in TMEM, fused bias + GELU epilogues, and the elementwise and
+// optimizer kernels of training (GELU backward, bias gradients, MSE loss,
+// AdamW on FP32 master weights with BF16 copies).
+//
+// GEMM: D[M x N] = A[M x K] . B[N x K]^T with A, B in BF16 and FP32
+// accumulation. Operands are read through strides, so transposed operands of
+// the backward pass need no copies: element (m, k) of A is A[m a_rs + k a_ks].
+// One CTA of 128 threads computes a 128 x n_tile tile (n_tile <= 256): each
+// round stages a 64-wide K chunk of both operands into shared memory (K-major
+// core matrices, tc_gemm.cuh), one thread issues four K = 16 MMAs and commits
+// them to an mbarrier, and the CTA waits (bounded) before the next round. The
+// epilogue reads the accumulator lanes of each warp with tcgen05.ld. A grid z
+// dimension splits K; the split partials are added atomically.
+#include <algorithm>
+
+#include <cuda_bf16.h>
+
+#include "omg_internal.h"
+#include "tc_gemm.cuh"
+
+namespace omg {
+
+namespace {
+
+constexpr uint32_t kTileM = 128;
+constexpr uint32_t kMaxTileN = 256;
+constexpr uint32_t kPolls = 1u << 24;   // mbarrier poll limit (error 16 in the error word)
+
+__device__ __forceinline__ float gelu_f(float z) {
+  // tanh form of GELU
+  const float k0 = 0.7978845608028654f, k1 = 0.044715f;
+  const float u = k0 * (z + k1 * z * z * z);
+  return 0.5f * z * (1.0f + tanhf(u));
+}
+
+__device__ __forceinline__ float gelu_grad(float z) {
+  const float k0 = 0.7978845608028654f, k1 = 0.044715f;
+  const float u = k0 * (z + k1 * z * z * z);
+  const float t = tanhf(u);
+  const float du = k0 * (1.0f + 3.0f * k1 * z * z);
+  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * du;
+}
+
+// Stage rows [r0, r0 + rows) x K [k0, k0 + 64) of an operand into a tile.
+__device__ __forceinline__ void stage(uint8_t* tile, const __nv_bfloat16* __restrict__ X, int64_t rs, int64_t ks,
+                                      uint32_t r0, uint32_t rows, uint32_t R, uint32_t k0, uint32_t K) {
+  const uint32_t pieces = rows * 8u;  // 16-byte pieces: (row, k8)
+  for (uint32_t p = threadIdx.x; p < pieces; p += blockDim.x) {
+    // consecutive threads take consecutive rows of the same k8 (coalesced when ks != 1)
+    const uint32_t r = p % rows, k8 = p / rows;
+    const uint32_t gr = r0 + r, gk = k0 + 8u * k8;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (gr < R) {
+      const __nv_bfloat16* src = X + (int64_t)gr * rs + (int64_t)gk * ks;
+      if (ks == 1 && gk + 8u <= K && ((reinterpret_cast<uintptr_t>(src) & 15u) == 0u)) {
+        v = *reinterpret_cast<const uint4*>(src);
+      } else {
+        uint16_t h[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          h[j] = 0;
+          if (gk + (uint32_t)j < K) h[j] = __bfloat16_as_ushort(src[(int64_t)j * ks]);
+        }
+        v.x = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+        v.y = (uint32_t)h[2] | ((uint32_t)h[3] << 16);
+        v.z = (uint32_t)h[4] | ((uint32_t)h[5] << 16);
+        v.w = (uint32_t)h[6] | ((uint32_t)h[7] << 16);
+      }
+    }
+    *reinterpret_cast<uint4*>(tile + tc::tile_offset(r, 8u * k8)) = v;
+  }
+}
+
+__global__ void __launch_bounds__(128, 1) gemm_kernel(GemmArgs g) {
+  const __nv_bfloat16* __restrict__ gA = static_cast<const __nv_bfloat16*>(g.A);
+  const __nv_bfloat16* __restrict__ gB = static_cast<const __nv_bfloat16*>(g.B);
+  __nv_bfloat16* gY = static_cast<__nv_bfloat16*>(g.Y);
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sa = smem;                                   // 128 x 64 bf16 = 16 KB
+  uint8_t* sb = smem + kTileM * tc::kChunkK * 2;        // n_tile x 64 bf16 <= 32 KB
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t taddr_s;
+  __shared__ uint32_t failed;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint32_t m0 = blockIdx.x * kTileM;
+  const uint32_t n0 = blockIdx.y * g.n_tile;
+  const uint32_t nt = min(g.n_tile, g.N - n0);          // columns of this tile
+  const uint32_t nt16 = (nt + 15u) & ~15u;              // MMA N (multiple of 16)
+  // this CTA's K range
+  const uint32_t k_per = ((g.K + gridDim.z - 1) / gridDim.z + tc::kChunkK - 1) / tc::kChunkK * tc::kChunkK;
+  const uint32_t kb = blockIdx.z * k_per;
+  const uint32_t ke = min(g.K, kb + k_per);
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&mbar, 1);
+    failed = 0;
+  }
+  if (warp == 0) tc::tmem_alloc(&taddr_s, kMaxTileN);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = taddr_s;
+  const uint32_t idesc = tc::idesc_bf16_f32(nt16, kTileM);
+  uint32_t phase = 0;
+  bool any = false;
+  for (uint32_t k0 = kb; k0 < ke; k0 += tc::kChunkK) {
+    stage(sa, gA, g.a_rs, g.a_ks, m0, kTileM, g.M, k0, ke);
+    stage(sb, gB, g.b_rs, g.b_ks, n0, nt16, n0 + nt, k0, ke);
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc::fence_after_sync();
+      const uint32_t a0 = tc::smem_u32(sa), b0 = tc::smem_u32(sb);
+#pragma unroll
+      for (uint32_t s = 0; s < tc::kChunkK / 16u; s++)
+        tc::mma_bf16(taddr, tc::smem_desc(a0 + 256u * s), tc::smem_desc(b0 + 256u * s), idesc, any || s > 0);
+      tc::mma_commit(&mbar);
+    }
+    any = true;
+    // the tiles are read asynchronously: wait before restaging them
+    if (!tc::mbar_wait(&mbar, phase, kPolls)) failed = 1;
+    phase ^= 1u;
+    __syncthreads();
+    if (failed) break;
+  }
+  tc::fence_after_sync();
+  if (!failed && any) {
+    const uint32_t row = m0 + warp * 32u + lane;
+    const uint32_t lane_addr = taddr + ((warp * 32u) << 16);
+    for (uint32_t c = 0; c < nt16; c += 16u) {
+      float v[16];
+      tc::tmem_ld16(lane_addr + c, v);
+      if (row >= g.M) continue;
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const uint32_t col = n0 + c + (uint32_t)j;
+        if (c + (uint32_t)j >= nt) break;
+        float z = v[j];
+        if (g.bias) z += g.bias[col];
+        if (g.D) {
+          float* d = g.D + (int64_t)row * g.ldd + col;
+          if (g.accumulate) atomicAdd(d, z);
+          else *d = z;
+        }
+        if (g.Z) g.Z[(int64_t)row * g.ldz + col] = z;
+        if (gY) gY[(int64_t)row * g.ldy + col] = __float2bfloat16_rn(g.act ? gelu_f(z) : z);
+      }
+    }
+  } else if (failed) {
+    // give the MMAs in flight one more bounded wait before the TMEM is freed
+    tc::mbar_wait(&mbar, phase ^ 1u, kPolls);
+    if (threadIdx.x == 0 && g.err) atomicOr(g.err, 16u);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, kMaxTileN);
+}
+
+// dZ = dA * GELU'(Z) (f32 in, bf16 and f32 out)
+__global__ void gelu_back_kernel(const float* __restrict__ dA, const float* __restrict__ Z, float* __restrict__ dZ,
+                                 __nv_bfloat16* __restrict__ dZh, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const float d = dA[i] * gelu_grad(Z[i]);
+    dZ[i] = d;
+    dZh[i] = __float2bfloat16_rn(d);
+  }
+}
+
+// column sums of X [rows x cols] (bias gradients); one thread per column
+__global__ void colsum_kernel(const float* __restrict__ X, uint32_t rows, uint32_t cols, float* __restrict__ out) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.0f;
+  for (uint32_t r = 0; r < rows; r++) s += X[(uint64_t)r * cols + c];
+  out[c] = s;
+}
+
+// MSE over [rows x cols] with a per-column weight: dY = 2 w (Y - T) / (rows cols),
+// bf16 copy of dY for the GEMMs, per-block partial losses
+__global__ void mse_kernel(const float* __restrict__ Y, const float* __restrict__ T, const float* __restrict__ w,
+                           uint32_t rows, uint32_t cols, float* __restrict__ dY, __nv_bfloat16* __restrict__ dYh,
+                           float* __restrict__ loss_parts) {
+  __shared__ float red[256];
+  const uint64_t n = (uint64_t)rows * cols;
+  const float scale = 2.0f / (float)n;
+  float acc = 0.0f;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const float wc = w ? w[i % cols] : 1.0f;
+    const float e = Y[i] - T[i];
+    acc += wc * e * e;
+    const float d = scale * wc * e;
+    dY[i] = d;
+    dYh[i] = __float2bfloat16_rn(d);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (uint32_t s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) loss_parts[blockIdx.x] = red[0] / (float)n;
+}
+
+// AdamW on FP32 master weights; writes the BF16 copy used by the GEMMs.
+__global__ void adamw_kernel(float* __restrict__ W, float* __restrict__ m, float* __restrict__ v,
+                             const float* __restrict__ g, __nv_bfloat16* __restrict__ Wh, uint64_t n, float lr,
+                             float b1, float b2, float eps, float wd, float bc1, float bc2) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float mh = mi / bc1, vh = vi / bc2;
+    float w = W[i];
+    w = w - lr * (mh / (sqrtf(vh) + eps) + wd * w);
+    W[i] = w;
+    if (Wh) Wh[i] = __float2bfloat16_rn(w);
+  }
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    y[i] = __float2bfloat16_rn(x[i]);
+}
+
+// out[r] = X[idx[r]] (row gather of a [n x cols] f32 matrix), optional bf16 copy
+__global__ void gather_rows_kernel(const float* __restrict__ X, uint32_t cols, const uint32_t* __restrict__ idx,
+                                   uint32_t rows, float* __restrict__ out, __nv_bfloat16* __restrict__ out_h) {
+  const uint64_t n = (uint64_t)rows * cols;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t r = (uint32_t)(i / cols), c = (uint32_t)(i % cols);
+    const float v = X[(uint64_t)idx[r] * cols + c];
+    if (out) out[i] = v;
+    if (out_h) out_h[i] = __float2bfloat16_rn(v);
+  }
+}
+
+}  // namespace
+
+size_t gemm_smem_bytes() { return (size_t)(kTileM + kMaxTileN) * tc::kChunkK * 2; }
+
+cudaError_t launch_gemm(const GemmArgs& g, uint32_t k_split, cudaStream_t s) {
+  if (g.M == 0 || g.N == 0 || g.K == 0) return cudaSuccess;
+  if (g.n_tile == 0 || g.n_tile > kMaxTileN || (g.n_tile & 15u)) return cudaErrorInvalidValue;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)gemm_smem_bytes());
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  dim3 grid((g.M + kTileM - 1) / kTileM, (g.N + g.n_tile - 1) / g.n_tile, k_split ? k_split : 1);
+  gemm_kernel<<<grid, 128, gemm_smem_bytes(), s>>>(g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gelu_back(const float* dA, const float* Z, float* dZ, void* dZh, uint64_t n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  gelu_back_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+      dA, Z, dZ, static_cast<__nv_bfloat16*>(dZh), n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_colsum(const float* X, uint32_t rows, uint32_t cols, float* out, cudaStream_t s) {
+  colsum_kernel<<<(cols + 127) / 128, 128, 0, s>>>(X, rows, cols, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mse(const float* Y, const float* T, const float* w, uint32_t rows, uint32_t cols, float* dY,
+                       void* dYh, float* loss_parts, uint32_t n_parts, cudaStream_t s) {
+  mse_kernel<<<n_parts, 256, 0, s>>>(Y, T, w, rows, cols, dY, static_cast<__nv_bfloat16*>(dYh), loss_parts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adamw(float* W, float* m, float* v, const float* g, void* Wh, uint64_t n, float lr, float b1,
+                         float b2, float eps, float wd, float bc1, float bc2, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  adamw_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+      W, m, v, g, static_cast<__nv_bfloat16*>(Wh), n, lr, b1, b2, eps, wd, bc1, bc2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_bf16(const float* x, void* y, uint64_t n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  to_bf16_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+      x, static_cast<__nv_bfloat16*>(y), n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_rows(const float* X, uint32_t cols, const uint32_t* idx, uint32_t rows, float* out,
+                               void* out_bf16, cudaStream_t s) {
+  if (rows == 0) return cudaSuccess;
+  const uint64_t n = (uint64_t)rows * cols;
+  gather_rows_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+      X, cols, idx, rows, out, static_cast<__nv_bfloat16*>(out_bf16));
+  return cudaGetLastError();
+}
+
+}  // namespace omg

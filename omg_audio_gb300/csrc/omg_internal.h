@@ -262,6 +262,38 @@ struct DDomeLaunch {
   uint32_t tie;               // near-tie rule of the escape raycasts (omg_params.tie_mode)
 };
 cudaError_t launch_dome(const DDomeLaunch& L, cudaStream_t s);
+
+// mlp.cu: tensor-core GEMM D[M x N] = A[M x K] . B[N x K]^T (bf16 in, f32
+// accumulate) with strided operands and a fused epilogue.
+struct GemmArgs {
+  const void* A;            // __nv_bfloat16; element (m, k) at A[m a_rs + k a_ks]
+  int64_t a_rs, a_ks;
+  const void* B;            // element (n, k) at B[n b_rs + k b_ks]
+  int64_t b_rs, b_ks;
+  uint32_t M, N, K;
+  uint32_t n_tile;          // columns per CTA: multiple of 16, <= 256
+  const float* bias;        // [N] or null
+  float* D;                 // f32 [M x ldd] or null
+  int64_t ldd;
+  uint32_t accumulate;      // 1: D += (atomically; K split over grid z)
+  float* Z;                 // pre-activation f32 or null
+  int64_t ldz;
+  void* Y;                  // __nv_bfloat16 activation out or null
+  int64_t ldy;
+  uint32_t act;             // 0 none, 1 GELU (tanh form)
+  uint32_t* err;            // error word: 16 = an mbarrier wait ran out
+};
+size_t gemm_smem_bytes();
+cudaError_t launch_gemm(const GemmArgs& g, uint32_t k_split, cudaStream_t s);
+cudaError_t launch_gelu_back(const float* dA, const float* Z, float* dZ, void* dZh, uint64_t n, cudaStream_t s);
+cudaError_t launch_colsum(const float* X, uint32_t rows, uint32_t cols, float* out, cudaStream_t s);
+cudaError_t launch_mse(const float* Y, const float* T, const float* w, uint32_t rows, uint32_t cols, float* dY,
+                       void* dYh, float* loss_parts, uint32_t n_parts, cudaStream_t s);
+cudaError_t launch_adamw(float* W, float* m, float* v, const float* g, void* Wh, uint64_t n, float lr, float b1,
+                         float b2, float eps, float wd, float bc1, float bc2, cudaStream_t s);
+cudaError_t launch_to_bf16(const float* x, void* y, uint64_t n, cudaStream_t s);
+cudaError_t launch_gather_rows(const float* X, uint32_t cols, const uint32_t* idx, uint32_t rows, float* out,
+                               void* out_bf16, cudaStream_t s);
 cudaError_t build_dome_fan(float4* fan, uint32_t n_fan, cudaStream_t s);
 
 }  // namespace omg

@@ -130,6 +130,7 @@ struct Ticket {
 };
 
 struct DomeRec;
+struct MlpRec;
 
 }  // namespace omg
 
@@ -151,6 +152,8 @@ struct omg_ctx {
   uint32_t next_ticket = 1;
   std::map<uint32_t, std::shared_ptr<omg::DomeRec>> probes;
   uint32_t next_probe = 1;
+  std::map<uint32_t, std::shared_ptr<omg::MlpRec>> mlps;   // surrogate networks
+  uint32_t next_mlp = 1;
   // raycast query scratch
   omg::DevBuf<float> q_o, q_d, q_t;
   omg::DevBuf<uint32_t> q_tri;

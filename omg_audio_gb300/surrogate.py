@@ -1,0 +1,341 @@
+"""The learned surrogate of the tracer (no reference counterpart).
+
+`Mlp` wraps the C ABI's tensor-core MLP ensemble (omg_mlp_*). `RoomSurrogate`
+is the room-acoustics surrogate on top of it: it maps a shoebox room with up
+to four apertures and a source/listener pose (38 input floats) to the
+energy-decay curve (EDC, Schroeder backward integral) at 64 log-spaced times
+per band (192 outputs, dB), is trained on echograms the GPU tracer produces,
+and answers with the tracer as its fallback wherever the inputs leave the
+training range or the ensemble's spread exceeds a threshold.
+
+Inputs (38): room size (3); per-surface per-band absorption (6 x 3, surfaces in
+the shoebox order x-, x+, y-, y+, z-, z+); aperture openness (4, one per side
+wall); source and listener position as fractions of the room size (3 + 3);
+and seven derived features: log volume, log surface area, log
+source-listener distance, the Sabine RT60 per band (3, from the surface and
+aperture absorption) and the open aperture area fraction.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import struct
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import lib
+from .materials import Material
+
+N_IN = 38
+N_TIMES = 64
+N_BANDS = 3
+N_OUT = N_TIMES * N_BANDS
+EDC_T0, EDC_T1 = 0.005, 2.0            # seconds: the EDC sample times span this range
+EDC_TIMES = np.geomspace(EDC_T0, EDC_T1, N_TIMES)
+EDC_FLOOR_DB = -100.0
+APERTURE_W, APERTURE_H = 1.5, 2.0      # metres: one aperture centred on each side wall, from the floor
+C_SOUND = 343.0
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Mlp:
+    """An ensemble of MLPs on the GPU (omg_mlp_create / set_data / train /
+    omg_surrogate_predict / omg_mlp_grad / omg_mlp_params)."""
+
+    def __init__(self, ctx, n_in: int, hidden: int = 256, n_hidden: int = 4, n_out: int = N_OUT, members: int = 4,
+                 seed: int = 1):
+        self.ctx = ctx
+        self.cfg = _lib.omg_mlp_config(n_in, hidden, n_hidden, n_out, members, seed)
+        mid = C.c_uint32()
+        ctx._check(lib().omg_mlp_create(ctx.h, C.byref(self.cfg), C.byref(mid)), "omg_mlp_create")
+        self.id = mid.value
+
+    def set_data(self, x, y):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        assert x.shape[1] == self.cfg.n_in and y.shape[1] == self.cfg.n_out and len(x) == len(y)
+        self.ctx._check(lib().omg_mlp_set_data(self.ctx.h, self.id, _p(x), _p(y), len(x)), "omg_mlp_set_data")
+
+    def train(self, epochs: int, batch: int = 4096, lr: float = 1e-3, lr_final: float = 1e-5,
+              weight_decay: float = 1e-4, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
+              seed: int = 7) -> np.ndarray:
+        tc = _lib.omg_mlp_train_config(epochs, batch, lr, lr_final, weight_decay, beta1, beta2, eps, seed)
+        losses = np.zeros((self.cfg.members, epochs), np.float32)
+        self.ctx._check(lib().omg_mlp_train(self.ctx.h, self.id, C.byref(tc), _p(losses)), "omg_mlp_train")
+        return losses
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        mean = np.zeros((len(x), self.cfg.n_out), np.float32)
+        std = np.zeros_like(mean)
+        self.ctx._check(lib().omg_surrogate_predict(self.ctx.h, self.id, _p(x), len(x), _p(mean), _p(std)),
+                        "omg_surrogate_predict")
+        return mean, std
+
+    def grad(self, x, y, member: int = 0):
+        """Loss and [(dW, db)] of one member on standardized x, y."""
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        shapes = self._shapes()
+        total = sum(o * i + o for o, i in shapes)
+        g = np.zeros(total, np.float32)
+        loss = C.c_float()
+        self.ctx._check(lib().omg_mlp_grad(self.ctx.h, self.id, member, _p(x), _p(y), len(x), C.byref(loss), _p(g)),
+                        "omg_mlp_grad")
+        out, off = [], 0
+        for o, i in shapes:
+            out.append((g[off:off + o * i].reshape(o, i), g[off + o * i:off + o * i + o]))
+            off += o * i + o
+        return loss.value, out
+
+    def _shapes(self):
+        c = self.cfg
+        dims = [c.n_in] + [c.hidden] * c.n_hidden + [c.n_out]
+        return [(dims[k + 1], dims[k]) for k in range(len(dims) - 1)]
+
+    def _params(self, what: int) -> np.ndarray:
+        n = C.c_uint64()
+        self.ctx._check(lib().omg_mlp_params(self.ctx.h, self.id, what, None, C.byref(n)), "omg_mlp_params")
+        out = np.zeros(n.value, np.float32)
+        self.ctx._check(lib().omg_mlp_params(self.ctx.h, self.id, what, _p(out), C.byref(n)), "omg_mlp_params")
+        return out
+
+    def layers(self, member: int = 0):
+        """[(W, b)] of one member (FP32 master weights)."""
+        p = self._params(1)
+        c = self.cfg
+        off = 2 * c.n_in + 2 * c.n_out
+        per = sum(o * i + o for o, i in self._shapes())
+        off += member * per
+        out = []
+        for o, i in self._shapes():
+            out.append((p[off:off + o * i].reshape(o, i).astype(np.float64),
+                        p[off + o * i:off + o * i + o].astype(np.float64)))
+            off += o * i + o
+        return out
+
+    # checkpoint: a plain binary with a header (magic, version, config, counts)
+    MAGIC = b"OMGSURR1"
+
+    def save(self, path: str):
+        w, m = self._params(1), self._params(2)
+        c = self.cfg
+        with open(path, "wb") as fh:
+            fh.write(self.MAGIC)
+            fh.write(struct.pack("<6I2Q", c.n_in, c.hidden, c.n_hidden, c.n_out, c.members, c.seed, len(w), len(m)))
+            fh.write(w.tobytes())
+            fh.write(m.tobytes())
+
+    @classmethod
+    def load(cls, ctx, path: str) -> "Mlp":
+        with open(path, "rb") as fh:
+            if fh.read(8) != cls.MAGIC:
+                raise ValueError("not a surrogate checkpoint")
+            n_in, hidden, n_hidden, n_out, members, seed, nw, nm = struct.unpack("<6I2Q", fh.read(40))
+            w = np.frombuffer(fh.read(4 * nw), np.float32)
+            m = np.frombuffer(fh.read(4 * nm), np.float32)
+        net = cls(ctx, n_in, hidden, n_hidden, n_out, members, seed)
+        ctx._check(lib().omg_mlp_set_params(ctx.h, net.id, 1, _p(np.ascontiguousarray(w)), len(w)), "omg_mlp_set_params")
+        ctx._check(lib().omg_mlp_set_params(ctx.h, net.id, 2, _p(np.ascontiguousarray(m)), len(m)), "omg_mlp_set_params")
+        return net
+
+    def close(self):
+        if self.id:
+            lib().omg_mlp_destroy(self.ctx.h, self.id)
+            self.id = 0
+
+
+# ------------------------------------------------------------------ rooms
+@dataclass
+class Room:
+    size: np.ndarray          # (3,)
+    alpha: np.ndarray         # (6, 3) per surface, per band
+    openness: np.ndarray      # (4,) apertures on x-, x+, y-, y+
+    src: np.ndarray           # (3,)
+    lis: np.ndarray           # (3,)
+
+
+# the training family: sizes, absorption and openness ranges (inputs outside
+# them make the surrogate fall back to the tracer)
+SIZE_LO = np.array([4.0, 4.0, 2.5])
+SIZE_HI = np.array([16.0, 12.0, 6.0])
+ALPHA_LO, ALPHA_HI = 0.02, 0.4
+SCATTERING = 0.1
+
+
+def sample_rooms(n: int, seed: int) -> list:
+    rng = np.random.default_rng(seed)
+    rooms = []
+    for _ in range(n):
+        size = rng.uniform(SIZE_LO, SIZE_HI)
+        alpha = rng.uniform(ALPHA_LO, ALPHA_HI, (6, N_BANDS))
+        n_ap = rng.integers(0, 5)
+        openness = np.zeros(4)
+        openness[rng.permutation(4)[:n_ap]] = rng.uniform(0.0, 1.0, n_ap)
+        # poses >= 1 m from every wall
+        src = rng.uniform(1.0, size - 1.0)
+        lis = rng.uniform(1.0, size - 1.0)
+        rooms.append(Room(size, alpha, openness, src, lis))
+    return rooms
+
+
+def aperture_boxes(size):
+    """One aperture per side wall (x-, x+, y-, y+): a panel box flush with the
+    wall, APERTURE_W wide (clipped to the wall), APERTURE_H high from the
+    floor (clipped)."""
+    sx, sy, sz = size
+    h = min(APERTURE_H, sz - 0.1)
+    out = []
+    for k in range(4):
+        axis = 0 if k < 2 else 1
+        other = 1 - axis
+        span = (sy if axis == 0 else sx)
+        w = min(APERTURE_W, span - 0.2)
+        c = 0.5 * span
+        mn, mx = np.zeros(3), np.zeros(3)
+        wall = 0.0 if k % 2 == 0 else (sx if axis == 0 else sy)
+        # a thin slab on the room side of the wall: it is met before the wall
+        mn[axis], mx[axis] = (wall - 0.05, wall + 0.001) if k % 2 == 0 else (wall - 0.001, wall + 0.05)
+        mn[other], mx[other] = c - 0.5 * w, c + 0.5 * w
+        mn[2], mx[2] = 0.0, h
+        out.append((mn, mx, w * h))
+    return out
+
+
+def features(r: Room) -> np.ndarray:
+    sx, sy, sz = r.size
+    V = sx * sy * sz
+    areas = np.array([sy * sz, sy * sz, sx * sz, sx * sz, sx * sy, sx * sy])
+    S = areas.sum()
+    ap = aperture_boxes(r.size)
+    ap_area = np.array([a[2] for a in ap])
+    # Sabine: A_b = sum_s area_s alpha_sb, with each aperture area absorbing
+    # `openness` instead of the wall's alpha
+    A = (areas[:, None] * r.alpha).sum(0)
+    for k in range(4):
+        A += ap_area[k] * (r.openness[k] - r.alpha[k])
+    A = np.maximum(A, 1e-3)
+    sabine = 0.161 * V / A
+    d = np.linalg.norm(r.src - r.lis)
+    return np.concatenate([r.size, r.alpha.reshape(-1), r.openness, r.src / r.size, r.lis / r.size,
+                           [np.log(V), np.log(S), np.log(max(d, 1e-3))], sabine,
+                           [float((ap_area * r.openness).sum() / S)]]).astype(np.float32)
+
+
+def in_range(x: np.ndarray) -> np.ndarray:
+    """Rows whose primary inputs lie inside the training family."""
+    size = x[:, 0:3]
+    alpha = x[:, 3:21]
+    op = x[:, 21:25]
+    frac = x[:, 25:31]
+    return (np.all(size >= SIZE_LO - 1e-6, 1) & np.all(size <= SIZE_HI + 1e-6, 1) &
+            np.all(alpha >= ALPHA_LO - 1e-6, 1) & np.all(alpha <= ALPHA_HI + 1e-6, 1) &
+            np.all((op >= 0) & (op <= 1), 1) & np.all((frac >= 0) & (frac <= 1), 1))
+
+
+def edc_db(bins: np.ndarray, bin_dt: float) -> np.ndarray:
+    """EDC in dB (Schroeder backward integral, FP64) at EDC_TIMES, per band:
+    bins [n_bins x NB] -> [N_TIMES x NB], linear interpolation between bins."""
+    b = np.asarray(bins, np.float64)
+    tail = np.cumsum(b[::-1], axis=0)[::-1]
+    total = np.maximum(tail[0:1], 1e-300)
+    e = tail / total
+    t = (np.arange(len(b)) + 0.0) * bin_dt
+    out = np.empty((N_TIMES, b.shape[1]))
+    for k in range(b.shape[1]):
+        out[:, k] = np.interp(EDC_TIMES, t, e[:, k])
+    return np.maximum(10.0 * np.log10(np.maximum(out, 1e-30)), EDC_FLOOR_DB)
+
+
+def rt60_from_edc(edc: np.ndarray) -> np.ndarray:
+    """RT60 per band from an EDC on the EDC_TIMES grid: 60 dB over the time the
+    curve takes from -5 to -25 dB (the reference's T20 form, tracer.rs:205-257),
+    crossings interpolated in time. edc: [..., N_TIMES, NB] -> [..., NB]."""
+    e = np.asarray(edc, np.float64)
+    shp = e.shape[:-2]
+    e2 = e.reshape(-1, N_TIMES, e.shape[-1])
+    out = np.full((e2.shape[0], e.shape[-1]), np.nan)
+    for i in range(e2.shape[0]):
+        for k in range(e.shape[-1]):
+            c = e2[i, :, k]
+            t5 = _cross(c, -5.0)
+            t25 = _cross(c, -25.0)
+            if t5 is not None and t25 is not None and t25 > t5:
+                out[i, k] = 60.0 * (t25 - t5) / 20.0
+    return out.reshape(*shp, e.shape[-1])
+
+
+def _cross(c, level):
+    idx = np.nonzero(c <= level)[0]
+    if len(idx) == 0:
+        return None
+    j = idx[0]
+    if j == 0:
+        return float(EDC_TIMES[0])
+    t0, t1, c0, c1 = EDC_TIMES[j - 1], EDC_TIMES[j], c[j - 1], c[j]
+    return float(t0 + (t1 - t0) * (level - c0) / (c1 - c0)) if c1 != c0 else float(t1)
+
+
+def trace_rooms(ctx, rooms: Sequence[Room], n_rays: int, seed: int, chunk: int = 4096):
+    """Echograms of the rooms from the GPU tracer (shoebox jobs with the
+    aperture panels), batched; returns (bins [n x n_bins x NB], reverb)."""
+    from .engine import Job
+    from .tracer import ReverbParams  # noqa: F401
+    cfg = ctx.cfg
+    bins_all, rv_all = [], []
+    for c0 in range(0, len(rooms), chunk):
+        part = rooms[c0:c0 + chunk]
+        jobs, panels = [], []
+        for k, r in enumerate(part):
+            walls = [Material(tuple(float(a) for a in r.alpha[w]), SCATTERING, (0.0,) * N_BANDS) for w in range(6)]
+            off = len(panels)
+            for (mn, mx, _), op in zip(aperture_boxes(r.size), r.openness):
+                panels.append((tuple(mn), tuple(mx), Material((float(op),) * N_BANDS, 0.0, (0.0,) * N_BANDS)))
+            jobs.append(Job(tuple(r.src), tuple(r.lis), n_rays, seed=seed + c0 + k, box_size=tuple(r.size),
+                            box_walls=walls, panel_offset=off, n_panels=4))
+        res = ctx.trace_batch(jobs, panels)
+        for e, rv in res:
+            bins_all.append(e.bins.copy())
+            rv_all.append(rv)
+    return np.stack(bins_all), rv_all
+
+
+class RoomSurrogate:
+    """Per-room EDC from the MLP ensemble, with the tracer as fallback."""
+
+    def __init__(self, ctx, members: int = 4, hidden: int = 256, n_hidden: int = 4, seed: int = 1):
+        self.ctx = ctx
+        self.net = Mlp(ctx, N_IN, hidden, n_hidden, N_OUT, members, seed)
+        self.threshold_db = 3.0
+
+    def fit(self, rooms, edcs, epochs: int, batch: int = 4096, **kw) -> np.ndarray:
+        x = np.stack([features(r) for r in rooms])
+        y = np.asarray(edcs, np.float32).reshape(len(rooms), -1)
+        self.net.set_data(x, y)
+        return self.net.train(epochs, batch, **kw)
+
+    def predict(self, rooms):
+        """EDC [n x N_TIMES x NB] (dB), spread [same], usable mask."""
+        x = np.stack([features(r) for r in rooms])
+        mean, std = self.net.predict(x)
+        mean = mean.reshape(len(rooms), N_TIMES, N_BANDS)
+        std = std.reshape(len(rooms), N_TIMES, N_BANDS)
+        # the spread that matters: the curve above the -30 dB point the RT60 reads
+        sig = np.where(mean >= -30.0, std, 0.0).max(axis=(1, 2))
+        ok = in_range(x) & (sig <= self.threshold_db)
+        return mean, std, ok
+
+    def answer(self, rooms, n_rays: int = 4096, seed: int = 1):
+        """EDCs for every room: the surrogate's where usable, the tracer's elsewhere."""
+        edc, _, ok = self.predict(rooms)
+        fallback = [i for i in range(len(rooms)) if not ok[i]]
+        if fallback:
+            bins, _ = trace_rooms(self.ctx, [rooms[i] for i in fallback], n_rays, seed)
+            for j, i in enumerate(fallback):
+                edc[i] = edc_db(bins[j], self.ctx.cfg.bin_dt)
+        return edc, ok
