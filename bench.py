@@ -183,6 +183,67 @@ def run_reference(args):
     return 0
 
 
+def surrogate_leg(args, device):
+    """The learned surrogate against the GPU tracer on the config-1 room family
+    (shoebox, 6 x 3 absorptions, up to 4 apertures, poses): training data from
+    the tracer (1024 rays per room), the tensor-core MLP ensemble trained on the
+    GPU, then held-out rooms answered by both. Reported: RT60 error of the
+    surrogate's EDC against the tracer's (4096 rays), the Sabine formula's error
+    (the method without the network), and ms per room of each, end to end
+    through the C ABI with host buffers."""
+    from omg_audio_gb300 import Context, TraceConfig
+    from omg_audio_gb300 import surrogate as S
+    ctx = Context(TraceConfig(device=device, n_bands=3, n_bins=2000, bin_dt=0.001, max_time=2.0, max_bounces=200,
+                              energy_floor=1e-6, timeout_ms=120000))
+    t0 = time.perf_counter()
+    train = S.sample_rooms(args.surrogate_rooms, seed=1)
+    bins, _ = S.trace_rooms(ctx, train, 1024, seed=100)
+    edc = S.edc_db(bins, 0.001)
+    del bins
+    t_data = time.perf_counter() - t0
+    sur = S.RoomSurrogate(ctx, members=4)
+    t0 = time.perf_counter()
+    losses = sur.fit(train, edc, epochs=args.surrogate_epochs, batch=4096, lr=2e-3, lr_final=2e-5,
+                     weight_decay=1e-4)
+    t_train = time.perf_counter() - t0
+    test = S.sample_rooms(args.surrogate_test, seed=99)
+    S.trace_rooms(ctx, test.take(np.arange(64)), 4096, seed=7)      # warm-up
+    sur.predict(test.take(np.arange(64)))
+    t0 = time.perf_counter()
+    bins_t, _ = S.trace_rooms(ctx, test, 4096, seed=7)
+    t_trace = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    pred, std, ok = sur.predict(test)
+    t_pred = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    S.features(test)
+    t_feat = time.perf_counter() - t0
+    edc_t = S.edc_db(bins_t, 0.001)
+    rt_t = S.rt60_from_edc(edc_t)
+    err = np.abs(S.rt60_from_edc(pred) / rt_t - 1.0)
+    sab = np.abs(S.features(test)[:, S.SABINE_COLS] / rt_t - 1.0)
+    n = len(test)
+    ctx.close()
+    return {
+        "family": "shoebox 4-16 x 4-12 x 2.5-6 m, absorption U[0.02,0.4] x 6 surfaces x 3 bands, scattering 0.1, "
+                  "0-4 apertures 1.5 x 2 m with openness U[0,1], poses >= 1 m from walls",
+        "network": "38 -> 256 x4 (GELU) -> 192 (64 log-time EDC points x 3 bands), 4-member ensemble, BF16 "
+                   "tcgen05 GEMMs, FP32 accumulate and master weights, AdamW",
+        "train_rooms": len(train), "train_rays": 1024, "epochs": args.surrogate_epochs,
+        "data_s": t_data, "train_s": t_train, "final_loss": float(np.mean(losses[:, -1])),
+        "test_rooms": n, "judge_rays": 4096,
+        "rt60_err_median": float(np.nanmedian(err)), "rt60_err_p90": float(np.nanpercentile(err, 90)),
+        "frac_rooms_all_bands_within_5pct": float(np.mean(np.nan_to_num(err, nan=1.0).max(1) <= 0.05)),
+        "sabine_rt60_err_median": float(np.nanmedian(sab)),
+        "edc_rmse_db": float(np.sqrt(np.mean((pred - edc_t) ** 2))),
+        "usable_frac": float(np.mean(ok)),
+        "tracer_ms_per_room": 1e3 * t_trace / n, "surrogate_ms_per_room": 1e3 * t_pred / n,
+        "speedup": t_trace / t_pred, "surrogate_features_ms_per_room": 1e3 * t_feat / n,
+        "timing": "wall clock of the calls with host buffers: trace_rooms (batched jobs, echograms down) vs "
+                  "RoomSurrogate.predict (input features, omg_surrogate_query, decay curves down)",
+    }
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -332,6 +393,8 @@ def run_ours(args):
                                        f"{threads} threads)"},
             "clocks": clk.summary(),
         }
+        if args.surrogate:
+            line["surrogate"] = surrogate_leg(args, local)
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()
@@ -349,6 +412,11 @@ def main():
     ap.add_argument("--ref-pairs", type=int, default=64)
     ap.add_argument("--pairs", type=int, default=N_PAIRS, help="pairs traced per step (default: the workload's 64)")
     ap.add_argument("--profile", action="store_true", help="launches only (a small case under a profiler)")
+    ap.add_argument("--no-surrogate", dest="surrogate", action="store_false",
+                    help="skip the surrogate leg (train on tracer data, compare with the tracer)")
+    ap.add_argument("--surrogate-rooms", type=int, default=131072, help="training rooms (1 M: the full config)")
+    ap.add_argument("--surrogate-epochs", type=int, default=60)
+    ap.add_argument("--surrogate-test", type=int, default=16384, help="held-out rooms")
     ap.add_argument("--max-bounces", type=int, default=0,
                     help="profiling variant: cap the bounces (0: the workload's 200)")
     ap.add_argument("--shape", default="",

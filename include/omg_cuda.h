@@ -374,6 +374,11 @@ int32_t omg_mlp_train(omg_ctx* ctx, uint32_t mlp_id, const omg_mlp_train_config*
 /* Predict n rows: ensemble mean (and spread, nullable) in the targets' units. */
 int32_t omg_surrogate_predict(omg_ctx* ctx, uint32_t mlp_id, const float* x, uint32_t n, float* y_mean,
                               float* y_std);
+/* The same, returning per row only the largest ensemble spread among the
+ * outputs whose mean is >= level (the usability check of a decay curve) instead
+ * of the full spread. */
+int32_t omg_surrogate_query(omg_ctx* ctx, uint32_t mlp_id, const float* x, uint32_t n, float* y_mean,
+                            float* row_spread, float level);
 /* One forward + backward of `member` on standardized x, y (n multiple of 128):
  * the loss and every layer's gradients (W row-major, then b), layer by layer. */
 int32_t omg_mlp_grad(omg_ctx* ctx, uint32_t mlp_id, uint32_t member, const float* x, const float* y, uint32_t n,

@@ -142,6 +142,7 @@ SIGNATURES = {
     "omg_mlp_set_data": (I32, [P, U32, P, P, U32]),
     "omg_mlp_train": (I32, [P, U32, C.POINTER(omg_mlp_train_config), P]),
     "omg_surrogate_predict": (I32, [P, U32, P, U32, P, P]),
+    "omg_surrogate_query": (I32, [P, U32, P, U32, P, P, F]),
     "omg_mlp_grad": (I32, [P, U32, U32, P, P, U32, P, P]),
     "omg_mlp_params": (I32, [P, U32, U32, P, PU64]),
     "omg_mlp_set_params": (I32, [P, U32, U32, P, U64]),

@@ -5,6 +5,7 @@
 // learning-rate decay, MSE on standardized targets. Inference returns the
 // ensemble mean and spread in the caller's units.
 #include <cmath>
+#include <cstring>
 #include <numeric>
 #include <random>
 
@@ -25,7 +26,11 @@ struct MlpRec {
   std::vector<std::vector<MlpLayer>> members;   // [member][layer]
   // standardization (host and device)
   std::vector<float> x_mean, x_std, y_mean, y_std;
-  DevBuf<float> d_x_mean, d_x_std;
+  DevBuf<float> d_x_mean, d_x_std, d_y_mean, d_y_std;
+  // inference buffers
+  uint32_t icap = 0;
+  DevBuf<float> xin, acc, acc2;
+  PinBuf<float> h_x, h_mean, h_std;
   // dataset (standardized, device)
   uint32_t n_data = 0;
   DevBuf<float> X, Y;
@@ -174,6 +179,20 @@ int32_t check_err(omg_ctx* ctx, MlpRec& M) {
   return OMG_OK;
 }
 
+int32_t sync_norm(omg_ctx* ctx, MlpRec& M) {
+  if (!M.d_x_mean.p) {
+    CK(M.d_x_mean.alloc(M.cfg.n_in));
+    CK(M.d_x_std.alloc(M.cfg.n_in));
+    CK(M.d_y_mean.alloc(M.cfg.n_out));
+    CK(M.d_y_std.alloc(M.cfg.n_out));
+  }
+  CK(cudaMemcpy(M.d_x_mean.p, M.x_mean.data(), M.cfg.n_in * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(M.d_x_std.p, M.x_std.data(), M.cfg.n_in * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(M.d_y_mean.p, M.y_mean.data(), M.cfg.n_out * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(M.d_y_std.p, M.y_std.data(), M.cfg.n_out * 4, cudaMemcpyHostToDevice));
+  return OMG_OK;
+}
+
 bool valid_cfg(const omg_mlp_config& c) {
   return c.n_in >= 1 && c.n_in <= 1024 && c.hidden >= 16 && c.hidden <= 256 && c.hidden % 16 == 0 &&
          c.n_hidden >= 1 && c.n_hidden <= 16 && c.n_out >= 1 && c.n_out <= 256 && c.members >= 1 &&
@@ -233,6 +252,8 @@ int32_t omg_mlp_create(omg_ctx* ctx, const omg_mlp_config* cfg, uint32_t* id) {
   CK(M->err.alloc(1));
   CK(cudaMemsetAsync(M->err.p, 0, 4, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  int32_t rc = sync_norm(ctx, *M);
+  if (rc) return rc;
   *id = ctx->next_mlp++;
   ctx->mlps[*id] = M;
   return OMG_OK;
@@ -278,6 +299,8 @@ int32_t omg_mlp_set_data(omg_ctx* ctx, uint32_t id, const float* x, const float*
     for (uint32_t k = 0; k < ni; k++) xs[i * ni + k] = (x[i * ni + k] - M.x_mean[k]) / M.x_std[k];
     for (uint32_t k = 0; k < no; k++) ys[i * no + k] = (y[i * no + k] - M.y_mean[k]) / M.y_std[k];
   }
+  int32_t rc = sync_norm(ctx, M);
+  if (rc) return rc;
   CK(M.X.alloc(xs.size()));
   CK(M.Y.alloc(ys.size()));
   CK(M.perm.alloc(n));
@@ -339,46 +362,73 @@ int32_t omg_mlp_train(omg_ctx* ctx, uint32_t id, const omg_mlp_train_config* tc,
   return check_err(ctx, M);
 }
 
-int32_t omg_surrogate_predict(omg_ctx* ctx, uint32_t id, const float* x, uint32_t n, float* y_mean, float* y_std) {
+}  // extern "C"
+
+namespace {
+
+// Shared by omg_surrogate_predict and omg_surrogate_query: y_std (full
+// spread) and/or row_spread (per row, the largest spread among outputs whose
+// mean is >= level) are optional.
+int32_t surrogate_run(omg_ctx* ctx, uint32_t id, const float* x, uint32_t n, float* y_mean, float* y_std,
+                      float* row_spread, float level) {
   if (!ctx || !x || !y_mean || n == 0) return OMG_E_INVALID;
   auto it = ctx->mlps.find(id);
   if (it == ctx->mlps.end()) return OMG_E_NOT_FOUND;
   MlpRec& M = *it->second;
   const uint32_t ni = M.cfg.n_in, no = M.cfg.n_out, E = M.cfg.members;
-  const uint32_t chunk = 16384;
-  int32_t rc = ensure_batch(ctx, M, std::min(n, chunk));
+  const uint32_t chunk = 32768;
+  const uint32_t rows_max = std::min(n, chunk);
+  int32_t rc = ensure_batch(ctx, M, rows_max);
   if (rc) return rc;
+  if (M.icap < rows_max) {
+    CK(M.xin.alloc((size_t)rows_max * ni));
+    CK(M.acc.alloc((size_t)rows_max * no));
+    CK(M.acc2.alloc((size_t)rows_max * no));
+    CK(M.h_x.alloc((size_t)rows_max * ni));
+    CK(M.h_mean.alloc((size_t)rows_max * no));
+    CK(M.h_std.alloc((size_t)rows_max * no));
+    M.icap = rows_max;
+  }
   cudaStream_t s = ctx->stream;
-  std::vector<float> xs((size_t)std::min(n, chunk) * ni), yo((size_t)std::min(n, chunk) * no);
-  std::vector<double> acc, acc2;
-  DevBuf<float> xd;
-  CK(xd.alloc(xs.size()));
+  // everything on the device: standardize, every member's forward, the
+  // ensemble's mean and spread in the targets' units
   for (uint32_t r0 = 0; r0 < n; r0 += chunk) {
     const uint32_t rows = std::min(chunk, n - r0);
-    for (uint64_t i = 0; i < rows; i++)
-      for (uint32_t k = 0; k < ni; k++)
-        xs[i * ni + k] = (x[(r0 + i) * ni + k] - M.x_mean[k]) / M.x_std[k];
-    CK(cudaMemcpyAsync(xd.p, xs.data(), (size_t)rows * ni * 4, cudaMemcpyHostToDevice, s));
-    CK(launch_to_bf16(xd.p, M.xh.p, (uint64_t)rows * ni, s));
-    acc.assign((size_t)rows * no, 0.0);
-    acc2.assign((size_t)rows * no, 0.0);
+    const uint64_t nx = (uint64_t)rows * ni, ny = (uint64_t)rows * no;
+    std::memcpy(M.h_x.p, x + (uint64_t)r0 * ni, nx * 4);
+    CK(cudaMemcpyAsync(M.xin.p, M.h_x.p, nx * 4, cudaMemcpyHostToDevice, s));
+    CK(launch_standardize(M.xin.p, M.d_x_mean.p, M.d_x_std.p, ni, nx, M.xh.p, s));
     for (uint32_t e = 0; e < E; e++) {
       if ((rc = forward(ctx, M, e, rows, s))) return rc;
-      CK(cudaMemcpyAsync(yo.data(), M.out.p, (size_t)rows * no * 4, cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      for (uint64_t i = 0; i < (uint64_t)rows * no; i++) {
-        const double v = (double)yo[i] * M.y_std[i % no] + M.y_mean[i % no];
-        acc[i] += v;
-        acc2[i] += v * v;
-      }
+      CK(launch_ensemble(M.out.p, M.d_y_mean.p, M.d_y_std.p, no, ny, M.acc.p, M.acc2.p, e == 0, e + 1 == E,
+                         1.0f / (float)E, s));
     }
-    for (uint64_t i = 0; i < (uint64_t)rows * no; i++) {
-      const double m = acc[i] / E;
-      y_mean[(uint64_t)r0 * no + i] = (float)m;
-      if (y_std) y_std[(uint64_t)r0 * no + i] = (float)std::sqrt(std::max(acc2[i] / E - m * m, 0.0));
+    CK(cudaMemcpyAsync(M.h_mean.p, M.acc.p, ny * 4, cudaMemcpyDeviceToHost, s));
+    if (y_std) CK(cudaMemcpyAsync(M.h_std.p, M.acc2.p, ny * 4, cudaMemcpyDeviceToHost, s));
+    if (row_spread) {
+      // the per-row spread reuses the bf16 input buffer's space as f32 scratch
+      CK(launch_row_spread(M.acc.p, M.acc2.p, no, rows, level, M.xin.p, s));
+      CK(cudaMemcpyAsync(row_spread + r0, M.xin.p, (size_t)rows * 4, cudaMemcpyDeviceToHost, s));
     }
+    CK(cudaStreamSynchronize(s));
+    std::memcpy(y_mean + (uint64_t)r0 * no, M.h_mean.p, ny * 4);
+    if (y_std) std::memcpy(y_std + (uint64_t)r0 * no, M.h_std.p, ny * 4);
   }
   return check_err(ctx, M);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t omg_surrogate_predict(omg_ctx* ctx, uint32_t id, const float* x, uint32_t n, float* y_mean, float* y_std) {
+  return surrogate_run(ctx, id, x, n, y_mean, y_std, nullptr, 0.0f);
+}
+
+int32_t omg_surrogate_query(omg_ctx* ctx, uint32_t id, const float* x, uint32_t n, float* y_mean,
+                            float* row_spread, float level) {
+  if (!row_spread) return OMG_E_INVALID;
+  return surrogate_run(ctx, id, x, n, y_mean, nullptr, row_spread, level);
 }
 
 // One forward/backward of `member` on standardized inputs and targets: the
@@ -496,6 +546,8 @@ int32_t omg_mlp_set_params(omg_ctx* ctx, uint32_t id, uint32_t what, const float
         CK(get_dev(Ly.b.p, Ly.out));
         CK(launch_to_bf16(Ly.W.p, Ly.Wh.p, (uint64_t)Ly.out * Ly.in, ctx->stream));
       }
+    int32_t rc2 = sync_norm(ctx, M);
+    if (rc2) return rc2;
   } else {
     for (auto& net : M.members)
       for (auto& Ly : net) {

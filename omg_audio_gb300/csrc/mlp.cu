@@ -236,7 +236,75 @@ __global__ void gather_rows_kernel(const float* __restrict__ X, uint32_t cols, c
   }
 }
 
+// (x - mean) / std per column, to bf16 (inference inputs)
+__global__ void standardize_kernel(const float* __restrict__ x, const float* __restrict__ mean,
+                                   const float* __restrict__ sd, uint32_t cols, uint64_t n,
+                                   __nv_bfloat16* __restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = (uint32_t)(i % cols);
+    out[i] = __float2bfloat16_rn((x[i] - mean[c]) / sd[c]);
+  }
+}
+
+// ensemble moments of the de-standardized outputs: acc (+)= y, acc2 (+)= y^2;
+// final: mean = acc / E, spread = sqrt(max(acc2 / E - mean^2, 0))
+__global__ void ensemble_kernel(const float* __restrict__ y, const float* __restrict__ mean,
+                                const float* __restrict__ sd, uint32_t cols, uint64_t n, float* __restrict__ acc,
+                                float* __restrict__ acc2, uint32_t first, uint32_t last, float inv_e) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = (uint32_t)(i % cols);
+    const float v = y[i] * sd[c] + mean[c];
+    float a = first ? v : acc[i] + v;
+    float a2 = first ? v * v : acc2[i] + v * v;
+    if (last) {
+      const float m = a * inv_e;
+      a2 = sqrtf(fmaxf(a2 * inv_e - m * m, 0.0f));
+      a = m;
+    }
+    acc[i] = a;
+    acc2[i] = a2;
+  }
+}
+
+// per row: the largest ensemble spread among outputs whose mean is >= level
+// (one warp per row)
+__global__ void row_spread_kernel(const float* __restrict__ mean, const float* __restrict__ sd, uint32_t cols,
+                                  uint32_t rows, float level, float* __restrict__ out) {
+  const uint32_t row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
+  if (row >= rows) return;
+  float m = 0.0f;
+  for (uint32_t c = lane; c < cols; c += 32) {
+    const uint64_t i = (uint64_t)row * cols + c;
+    if (mean[i] >= level) m = fmaxf(m, sd[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) out[row] = m;
+}
+
 }  // namespace
+
+cudaError_t launch_row_spread(const float* mean, const float* sd, uint32_t cols, uint32_t rows, float level,
+                              float* out, cudaStream_t s) {
+  if (rows == 0) return cudaSuccess;
+  row_spread_kernel<<<(rows + 7) / 8, 256, 0, s>>>(mean, sd, cols, rows, level, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_standardize(const float* x, const float* mean, const float* sd, uint32_t cols, uint64_t n,
+                               void* out, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  standardize_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+      x, mean, sd, cols, n, static_cast<__nv_bfloat16*>(out));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ensemble(const float* y, const float* mean, const float* sd, uint32_t cols, uint64_t n,
+                            float* acc, float* acc2, bool first, bool last, float inv_e, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  ensemble_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+      y, mean, sd, cols, n, acc, acc2, first ? 1u : 0u, last ? 1u : 0u, inv_e);
+  return cudaGetLastError();
+}
 
 size_t gemm_smem_bytes() { return (size_t)(kTileM + kMaxTileN) * tc::kChunkK * 2; }
 

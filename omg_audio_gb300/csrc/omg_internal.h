@@ -294,6 +294,12 @@ cudaError_t launch_adamw(float* W, float* m, float* v, const float* g, void* Wh,
 cudaError_t launch_to_bf16(const float* x, void* y, uint64_t n, cudaStream_t s);
 cudaError_t launch_gather_rows(const float* X, uint32_t cols, const uint32_t* idx, uint32_t rows, float* out,
                                void* out_bf16, cudaStream_t s);
+cudaError_t launch_standardize(const float* x, const float* mean, const float* sd, uint32_t cols, uint64_t n,
+                               void* out, cudaStream_t s);
+cudaError_t launch_ensemble(const float* y, const float* mean, const float* sd, uint32_t cols, uint64_t n,
+                            float* acc, float* acc2, bool first, bool last, float inv_e, cudaStream_t s);
+cudaError_t launch_row_spread(const float* mean, const float* sd, uint32_t cols, uint32_t rows, float level,
+                              float* out, cudaStream_t s);
 cudaError_t build_dome_fan(float4* fan, uint32_t n_fan, cudaStream_t s);
 
 }  // namespace omg

@@ -34,7 +34,7 @@ N_BANDS = 3
 N_OUT = N_TIMES * N_BANDS
 EDC_T0, EDC_T1 = 0.005, 2.0            # seconds: the EDC sample times span this range
 EDC_TIMES = np.geomspace(EDC_T0, EDC_T1, N_TIMES)
-EDC_FLOOR_DB = -100.0
+EDC_FLOOR_DB = -60.0               # below: noise of the finite ray count, and no use to the RT60
 APERTURE_W, APERTURE_H = 1.5, 2.0      # metres: one aperture centred on each side wall, from the floor
 C_SOUND = 343.0
 
@@ -76,6 +76,16 @@ class Mlp:
         self.ctx._check(lib().omg_surrogate_predict(self.ctx.h, self.id, _p(x), len(x), _p(mean), _p(std)),
                         "omg_surrogate_predict")
         return mean, std
+
+    def query(self, x, level: float):
+        """Ensemble mean and, per row, the largest spread among outputs whose
+        mean is >= level (omg_surrogate_query)."""
+        x = np.ascontiguousarray(x, np.float32)
+        mean = np.empty((len(x), self.cfg.n_out), np.float32)
+        spread = np.empty(len(x), np.float32)
+        self.ctx._check(lib().omg_surrogate_query(self.ctx.h, self.id, _p(x), len(x), _p(mean), _p(spread), level),
+                        "omg_surrogate_query")
+        return mean, spread
 
     def grad(self, x, y, member: int = 0):
         """Loss and [(dW, db)] of one member on standardized x, y."""
@@ -152,12 +162,19 @@ class Mlp:
 
 # ------------------------------------------------------------------ rooms
 @dataclass
-class Room:
-    size: np.ndarray          # (3,)
-    alpha: np.ndarray         # (6, 3) per surface, per band
-    openness: np.ndarray      # (4,) apertures on x-, x+, y-, y+
-    src: np.ndarray           # (3,)
-    lis: np.ndarray           # (3,)
+class Rooms:
+    """A set of shoebox rooms, column by column."""
+    size: np.ndarray          # (n, 3)
+    alpha: np.ndarray         # (n, 6, 3) per surface (x-, x+, y-, y+, z-, z+), per band
+    openness: np.ndarray      # (n, 4) apertures on x-, x+, y-, y+
+    src: np.ndarray           # (n, 3)
+    lis: np.ndarray           # (n, 3)
+
+    def __len__(self):
+        return len(self.size)
+
+    def take(self, idx) -> "Rooms":
+        return Rooms(self.size[idx], self.alpha[idx], self.openness[idx], self.src[idx], self.lis[idx])
 
 
 # the training family: sizes, absorption and openness ranges (inputs outside
@@ -168,63 +185,68 @@ ALPHA_LO, ALPHA_HI = 0.02, 0.4
 SCATTERING = 0.1
 
 
-def sample_rooms(n: int, seed: int) -> list:
+def sample_rooms(n: int, seed: int) -> Rooms:
     rng = np.random.default_rng(seed)
-    rooms = []
-    for _ in range(n):
-        size = rng.uniform(SIZE_LO, SIZE_HI)
-        alpha = rng.uniform(ALPHA_LO, ALPHA_HI, (6, N_BANDS))
-        n_ap = rng.integers(0, 5)
-        openness = np.zeros(4)
-        openness[rng.permutation(4)[:n_ap]] = rng.uniform(0.0, 1.0, n_ap)
-        # poses >= 1 m from every wall
-        src = rng.uniform(1.0, size - 1.0)
-        lis = rng.uniform(1.0, size - 1.0)
-        rooms.append(Room(size, alpha, openness, src, lis))
-    return rooms
+    size = rng.uniform(SIZE_LO, SIZE_HI, (n, 3))
+    alpha = rng.uniform(ALPHA_LO, ALPHA_HI, (n, 6, N_BANDS))
+    openness = rng.uniform(0.0, 1.0, (n, 4))
+    # 0 to 4 apertures per room
+    n_ap = rng.integers(0, 5, n)
+    rank = np.argsort(rng.random((n, 4)), axis=1)
+    openness = np.where(rank < n_ap[:, None], openness, 0.0)
+    # poses >= 1 m from every wall
+    src = 1.0 + rng.random((n, 3)) * (size - 2.0)
+    lis = 1.0 + rng.random((n, 3)) * (size - 2.0)
+    return Rooms(size, alpha, openness, src, lis)
 
 
 def aperture_boxes(size):
-    """One aperture per side wall (x-, x+, y-, y+): a panel box flush with the
-    wall, APERTURE_W wide (clipped to the wall), APERTURE_H high from the
-    floor (clipped)."""
-    sx, sy, sz = size
-    h = min(APERTURE_H, sz - 0.1)
-    out = []
+    """One aperture per side wall (x-, x+, y-, y+) of each room: a panel box
+    flush with the wall, APERTURE_W wide (clipped to the wall) and APERTURE_H
+    high from the floor (clipped). size (n, 3) -> mn (n, 4, 3), mx (n, 4, 3),
+    area (n, 4)."""
+    size = np.atleast_2d(size)
+    n = len(size)
+    h = np.minimum(APERTURE_H, size[:, 2] - 0.1)
+    mn, mx, area = np.zeros((n, 4, 3)), np.zeros((n, 4, 3)), np.zeros((n, 4))
     for k in range(4):
         axis = 0 if k < 2 else 1
         other = 1 - axis
-        span = (sy if axis == 0 else sx)
-        w = min(APERTURE_W, span - 0.2)
+        span = size[:, other]
+        w = np.minimum(APERTURE_W, span - 0.2)
         c = 0.5 * span
-        mn, mx = np.zeros(3), np.zeros(3)
-        wall = 0.0 if k % 2 == 0 else (sx if axis == 0 else sy)
+        wall = np.zeros(n) if k % 2 == 0 else size[:, axis]
         # a thin slab on the room side of the wall: it is met before the wall
-        mn[axis], mx[axis] = (wall - 0.05, wall + 0.001) if k % 2 == 0 else (wall - 0.001, wall + 0.05)
-        mn[other], mx[other] = c - 0.5 * w, c + 0.5 * w
-        mn[2], mx[2] = 0.0, h
-        out.append((mn, mx, w * h))
-    return out
+        if k % 2 == 0:
+            mn[:, k, axis], mx[:, k, axis] = wall - 0.05, wall + 0.001
+        else:
+            mn[:, k, axis], mx[:, k, axis] = wall - 0.001, wall + 0.05
+        mn[:, k, other], mx[:, k, other] = c - 0.5 * w, c + 0.5 * w
+        mn[:, k, 2], mx[:, k, 2] = 0.0, h
+        area[:, k] = w * h
+    return mn, mx, area
 
 
-def features(r: Room) -> np.ndarray:
-    sx, sy, sz = r.size
+def features(r: Rooms) -> np.ndarray:
+    """The 38 inputs of every room, (n, 38)."""
+    sx, sy, sz = r.size[:, 0], r.size[:, 1], r.size[:, 2]
     V = sx * sy * sz
-    areas = np.array([sy * sz, sy * sz, sx * sz, sx * sz, sx * sy, sx * sy])
-    S = areas.sum()
-    ap = aperture_boxes(r.size)
-    ap_area = np.array([a[2] for a in ap])
-    # Sabine: A_b = sum_s area_s alpha_sb, with each aperture area absorbing
-    # `openness` instead of the wall's alpha
-    A = (areas[:, None] * r.alpha).sum(0)
-    for k in range(4):
-        A += ap_area[k] * (r.openness[k] - r.alpha[k])
+    areas = np.stack([sy * sz, sy * sz, sx * sz, sx * sz, sx * sy, sx * sy], 1)
+    S = areas.sum(1)
+    _, _, ap = aperture_boxes(r.size)
+    # Sabine: A_b = sum_s area_s alpha_sb, each aperture area absorbing its
+    # openness instead of its wall's alpha
+    A = np.einsum("ns,nsb->nb", areas, r.alpha)
+    A += np.einsum("nk,nkb->nb", ap, r.openness[:, :, None] - r.alpha[:, :4, :])
     A = np.maximum(A, 1e-3)
-    sabine = 0.161 * V / A
-    d = np.linalg.norm(r.src - r.lis)
-    return np.concatenate([r.size, r.alpha.reshape(-1), r.openness, r.src / r.size, r.lis / r.size,
-                           [np.log(V), np.log(S), np.log(max(d, 1e-3))], sabine,
-                           [float((ap_area * r.openness).sum() / S)]]).astype(np.float32)
+    sabine = 0.161 * V[:, None] / A
+    d = np.maximum(np.linalg.norm(r.src - r.lis, axis=1), 1e-3)
+    return np.concatenate([r.size, r.alpha.reshape(len(r), -1), r.openness, r.src / r.size, r.lis / r.size,
+                           np.log(V)[:, None], np.log(S)[:, None], np.log(d)[:, None], sabine,
+                           ((ap * r.openness).sum(1) / S)[:, None]], axis=1).astype(np.float32)
+
+
+SABINE_COLS = slice(34, 37)
 
 
 def in_range(x: np.ndarray) -> np.ndarray:
@@ -239,67 +261,64 @@ def in_range(x: np.ndarray) -> np.ndarray:
 
 
 def edc_db(bins: np.ndarray, bin_dt: float) -> np.ndarray:
-    """EDC in dB (Schroeder backward integral, FP64) at EDC_TIMES, per band:
-    bins [n_bins x NB] -> [N_TIMES x NB], linear interpolation between bins."""
+    """EDC in dB (Schroeder backward integral, FP64) at EDC_TIMES, per band, for
+    one echogram [n_bins x NB] or many [n x n_bins x NB]; the curve is read at
+    the start of each bin and interpolated linearly; floor EDC_FLOOR_DB."""
     b = np.asarray(bins, np.float64)
-    tail = np.cumsum(b[::-1], axis=0)[::-1]
-    total = np.maximum(tail[0:1], 1e-300)
-    e = tail / total
-    t = (np.arange(len(b)) + 0.0) * bin_dt
-    out = np.empty((N_TIMES, b.shape[1]))
-    for k in range(b.shape[1]):
-        out[:, k] = np.interp(EDC_TIMES, t, e[:, k])
-    return np.maximum(10.0 * np.log10(np.maximum(out, 1e-30)), EDC_FLOOR_DB)
+    one = b.ndim == 2
+    if one:
+        b = b[None]
+    tail = np.cumsum(b[:, ::-1], axis=1)[:, ::-1]
+    e = tail / np.maximum(tail[:, 0:1], 1e-300)
+    t = np.arange(b.shape[1]) * bin_dt
+    j = np.clip(np.searchsorted(t, EDC_TIMES, side="right") - 1, 0, len(t) - 2)
+    w = ((EDC_TIMES - t[j]) / bin_dt)[None, :, None]
+    out = e[:, j] * (1.0 - w) + e[:, j + 1] * w
+    out = np.maximum(10.0 * np.log10(np.maximum(out, 1e-30)), EDC_FLOOR_DB)
+    return out[0] if one else out
 
 
 def rt60_from_edc(edc: np.ndarray) -> np.ndarray:
     """RT60 per band from an EDC on the EDC_TIMES grid: 60 dB over the time the
     curve takes from -5 to -25 dB (the reference's T20 form, tracer.rs:205-257),
-    crossings interpolated in time. edc: [..., N_TIMES, NB] -> [..., NB]."""
+    crossings interpolated in time. edc: [..., N_TIMES, NB] -> [..., NB]
+    (NaN where a crossing is missing)."""
     e = np.asarray(edc, np.float64)
-    shp = e.shape[:-2]
-    e2 = e.reshape(-1, N_TIMES, e.shape[-1])
-    out = np.full((e2.shape[0], e.shape[-1]), np.nan)
-    for i in range(e2.shape[0]):
-        for k in range(e.shape[-1]):
-            c = e2[i, :, k]
-            t5 = _cross(c, -5.0)
-            t25 = _cross(c, -25.0)
-            if t5 is not None and t25 is not None and t25 > t5:
-                out[i, k] = 60.0 * (t25 - t5) / 20.0
-    return out.reshape(*shp, e.shape[-1])
+    return 3.0 * (_cross(e, -25.0) - _cross(e, -5.0))
 
 
-def _cross(c, level):
-    idx = np.nonzero(c <= level)[0]
-    if len(idx) == 0:
-        return None
-    j = idx[0]
-    if j == 0:
-        return float(EDC_TIMES[0])
-    t0, t1, c0, c1 = EDC_TIMES[j - 1], EDC_TIMES[j], c[j - 1], c[j]
-    return float(t0 + (t1 - t0) * (level - c0) / (c1 - c0)) if c1 != c0 else float(t1)
+def _cross(e, level):
+    below = e <= level
+    has = below.any(axis=-2)
+    j = np.argmax(below, axis=-2)
+    jm = np.maximum(j - 1, 0)
+    c0 = np.take_along_axis(e, jm[..., None, :], axis=-2)[..., 0, :]
+    c1 = np.take_along_axis(e, j[..., None, :], axis=-2)[..., 0, :]
+    t0, t1 = EDC_TIMES[jm], EDC_TIMES[j]
+    den = np.where(c1 != c0, c1 - c0, 1.0)
+    t = np.where(j == 0, EDC_TIMES[0], np.where(c1 != c0, t0 + (t1 - t0) * (level - c0) / den, t1))
+    return np.where(has, t, np.nan)
 
 
-def trace_rooms(ctx, rooms: Sequence[Room], n_rays: int, seed: int, chunk: int = 4096):
-    """Echograms of the rooms from the GPU tracer (shoebox jobs with the
-    aperture panels), batched; returns (bins [n x n_bins x NB], reverb)."""
+def trace_rooms(ctx, rooms: Rooms, n_rays: int, seed: int, chunk: int = 8192):
+    """Echograms of the rooms from the GPU tracer: shoebox jobs with the
+    aperture panels, batched. Returns bins [n x n_bins x NB] and the reverb
+    parameters of every room."""
     from .engine import Job
-    from .tracer import ReverbParams  # noqa: F401
-    cfg = ctx.cfg
+    mn, mx, _ = aperture_boxes(rooms.size)
     bins_all, rv_all = [], []
     for c0 in range(0, len(rooms), chunk):
-        part = rooms[c0:c0 + chunk]
         jobs, panels = [], []
-        for k, r in enumerate(part):
-            walls = [Material(tuple(float(a) for a in r.alpha[w]), SCATTERING, (0.0,) * N_BANDS) for w in range(6)]
+        for i in range(c0, min(c0 + chunk, len(rooms))):
+            walls = [Material(tuple(float(a) for a in rooms.alpha[i, w]), SCATTERING, (0.0,) * N_BANDS)
+                     for w in range(6)]
             off = len(panels)
-            for (mn, mx, _), op in zip(aperture_boxes(r.size), r.openness):
-                panels.append((tuple(mn), tuple(mx), Material((float(op),) * N_BANDS, 0.0, (0.0,) * N_BANDS)))
-            jobs.append(Job(tuple(r.src), tuple(r.lis), n_rays, seed=seed + c0 + k, box_size=tuple(r.size),
-                            box_walls=walls, panel_offset=off, n_panels=4))
-        res = ctx.trace_batch(jobs, panels)
-        for e, rv in res:
+            for k in range(4):
+                op = float(rooms.openness[i, k])
+                panels.append((tuple(mn[i, k]), tuple(mx[i, k]), Material((op,) * N_BANDS, 0.0, (0.0,) * N_BANDS)))
+            jobs.append(Job(tuple(rooms.src[i]), tuple(rooms.lis[i]), n_rays, seed=seed + i,
+                            box_size=tuple(rooms.size[i]), box_walls=walls, panel_offset=off, n_panels=4))
+        for e, rv in ctx.trace_batch(jobs, panels):
             bins_all.append(e.bins.copy())
             rv_all.append(rv)
     return np.stack(bins_all), rv_all
@@ -313,29 +332,25 @@ class RoomSurrogate:
         self.net = Mlp(ctx, N_IN, hidden, n_hidden, N_OUT, members, seed)
         self.threshold_db = 3.0
 
-    def fit(self, rooms, edcs, epochs: int, batch: int = 4096, **kw) -> np.ndarray:
-        x = np.stack([features(r) for r in rooms])
+    def fit(self, rooms: Rooms, edcs, epochs: int, batch: int = 4096, **kw) -> np.ndarray:
+        x = features(rooms)
         y = np.asarray(edcs, np.float32).reshape(len(rooms), -1)
         self.net.set_data(x, y)
         return self.net.train(epochs, batch, **kw)
 
-    def predict(self, rooms):
-        """EDC [n x N_TIMES x NB] (dB), spread [same], usable mask."""
-        x = np.stack([features(r) for r in rooms])
-        mean, std = self.net.predict(x)
-        mean = mean.reshape(len(rooms), N_TIMES, N_BANDS)
-        std = std.reshape(len(rooms), N_TIMES, N_BANDS)
-        # the spread that matters: the curve above the -30 dB point the RT60 reads
-        sig = np.where(mean >= -30.0, std, 0.0).max(axis=(1, 2))
+    def predict(self, rooms: Rooms):
+        """EDC [n x N_TIMES x NB] (dB), per-room spread (dB) over the part of
+        the curve the RT60 reads (down to -30 dB), usable mask."""
+        x = features(rooms)
+        mean, sig = self.net.query(x, -30.0)
         ok = in_range(x) & (sig <= self.threshold_db)
-        return mean, std, ok
+        return mean.reshape(len(rooms), N_TIMES, N_BANDS), sig, ok
 
-    def answer(self, rooms, n_rays: int = 4096, seed: int = 1):
-        """EDCs for every room: the surrogate's where usable, the tracer's elsewhere."""
+    def answer(self, rooms: Rooms, n_rays: int = 4096, seed: int = 1):
+        """EDCs of every room: the surrogate's where usable, the tracer's elsewhere."""
         edc, _, ok = self.predict(rooms)
-        fallback = [i for i in range(len(rooms)) if not ok[i]]
-        if fallback:
-            bins, _ = trace_rooms(self.ctx, [rooms[i] for i in fallback], n_rays, seed)
-            for j, i in enumerate(fallback):
-                edc[i] = edc_db(bins[j], self.ctx.cfg.bin_dt)
+        fallback = np.nonzero(~ok)[0]
+        if len(fallback):
+            bins, _ = trace_rooms(self.ctx, rooms.take(fallback), n_rays, seed)
+            edc[fallback] = edc_db(bins, self.ctx.cfg.bin_dt)
         return edc, ok
