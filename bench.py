@@ -244,6 +244,97 @@ def surrogate_leg(args, device):
     }
 
 
+def run_workload(args):
+    """The other configurations, one JSON line each (not the headline):
+    rooms256 = 256 independent uneven rooms in one batch (lognormal triangle
+    counts 12-20k, rays 512-65536, 3 or 8 bands, 0.5-4 s at 1 ms);
+    city = the 1 M-triangle procedural city, 16 sources x 1 M rays x 8 bands,
+    4 s at 1 ms, plus the 512-ray dome fan of 1024 street listeners."""
+    import torch
+    torch.cuda.set_device(0)
+    from omg_audio_gb300 import build as B
+    B.build()
+    from omg_audio_gb300 import Context, DomeProbe, Job, MeshBuilder, TraceConfig, _lib
+    from omg_audio_gb300 import workloads as W
+    bvh = _lib.BVH_LBVH if args.bvh == "lbvh" else _lib.BVH_SAH
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    t0 = time.perf_counter()
+    if args.workload == "rooms256":
+        rooms = W.room_batch(seed=3, n_rooms=256)
+        ctx = Context(TraceConfig(timeout_ms=120000, tie_mode=1, n_bins=4000, max_time=4.0, max_bounces=200,
+                                  energy_floor=1e-6))
+        scenes, jobs = [], []
+        for k, r in enumerate(rooms):
+            mb = MeshBuilder()
+            r.recorder.replay(mb)
+            sc = ctx.upload_builder(mb, r.n_bands, bvh)
+            scenes.append(sc)
+            jobs.append(Job(r.src, r.lis, r.n_rays, seed=100 + k, scene=sc, n_bands=r.n_bands, n_bins=r.n_bins,
+                            max_time=r.max_time))
+        desc = ("rooms256: 256 rooms, triangles lognormal (median 2k, 12-20k), rays lognormal 512-65536 "
+                f"({sum(j.n_rays for j in jobs)} in all), bands 3 or 8, 0.5-4 s at 1 ms, one batch")
+        dome = None
+        prims = sum(sc.info()["prims"] for sc in scenes)
+    else:
+        case = W.city(seed=5)
+        ctx = Context(TraceConfig(timeout_ms=300000, tie_mode=1, n_bands=case.n_bands, n_bins=4000, bin_dt=0.001,
+                                  max_time=4.0, max_bounces=200, energy_floor=1e-6))
+        mb = MeshBuilder()
+        case.recorder.replay(mb)
+        scene = ctx.upload_builder(mb, case.n_bands, bvh)
+        prims = scene.info()["prims"]
+        jobs = [Job(tuple(s_), tuple(l_), args.city_rays, seed=500 + k, scene=scene)
+                for k, (s_, l_) in enumerate(zip(case.sources, case.listeners))]
+        dome = DomeProbe(ctx, scene, (), n_fan=512)
+        desc = (f"city: {case.recorder.n_tris} triangles ({prims} primitives), 16 sources x {args.city_rays} rays "
+                f"x 8 bands, 4 s at 1 ms, 200 bounces, floor 1e-6, + 512-ray dome fans of "
+                f"{len(case.dome_eyes)} listeners")
+    setup_s = time.perf_counter() - t0
+    ctx.set_stream(stream.cuda_stream)
+    batch = ctx.batch(jobs)
+    tune = batch.autotune(reps=1) if args.autotune else batch.shape()
+    for _ in range(max(args.warmup, 1)):
+        batch.launch()
+    torch.cuda.synchronize()
+    ms, dms = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            batch.launch(1)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+            if dome is not None:
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                dome.submit(case.dome_eyes, n_rays=512, stream=stream.cuda_stream, want=2)
+                b.record(stream)
+                torch.cuda.synchronize()
+                dres = dome.collect()
+                dms.append(a.elapsed_time(b))
+    batch.launch()
+    res = batch.read()
+    segs = batch.segments()
+    line = {"metric": "ray-segments/s", "workload": args.workload, "desc": desc, "prims": prims,
+            "bvh": args.bvh, "setup_s": setup_s, "steps": args.steps, "trace_ms": float(np.mean(ms)),
+            "segments": segs, "value": segs / (float(np.mean(ms)) * 1e-3), "unit": "ray-segments/s",
+            "autotune": tune, "clocks": clk.summary(),
+            "rt60_range": [float(np.nanmin([np.min(rv.rt60) for _, rv in res])),
+                           float(np.nanmax([np.max(rv.rt60) for _, rv in res]))]}
+    if dome is not None:
+        dseg = dres["segments"]["escape_events"] + dres["segments"]["through_calls"]
+        line["dome"] = {"eyes": len(case.dome_eyes), "ms": float(np.mean(dms)), "segments": dseg,
+                        "segments_per_s": dseg / (float(np.mean(dms)) * 1e-3),
+                        "sky_escape_frac": float(np.mean(dres["escape"]))}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -423,9 +514,14 @@ def main():
                     help="launch shape as JSON (omg_tune_result fields), instead of the autotuner")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the launch-shape autotuner (it runs once, before the warm-up)")
+    ap.add_argument("--workload", choices=["multiroom", "rooms256", "city"], default="multiroom",
+                    help="multiroom: the headline (default); rooms256 and city print their own line")
+    ap.add_argument("--city-rays", type=int, default=1 << 20, help="rays per source of the city workload")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "multiroom":
+        return run_workload(args)
     return run_ours(args)
 
 

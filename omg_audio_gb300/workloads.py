@@ -55,6 +55,20 @@ class Recorder:
         self.max_edge.append(self._coarse)
         self._pending_surf = 0
 
+    def add_quads(self, q, mats, new_surface, max_edge: float):
+        """Many quads at once: q (n, 12) corner coordinates, per-quad material,
+        begin_surface counts before each quad, one tessellation limit."""
+        q = np.asarray(q, np.float32).reshape(-1, 12)
+        self.quads.extend(list(q))
+        self.mats.extend(int(m) for m in np.broadcast_to(np.asarray(mats), (len(q),)))
+        ns = np.asarray(new_surface).astype(int)
+        if self._pending_surf and len(ns):
+            ns = ns.copy()
+            ns[0] += self._pending_surf
+            self._pending_surf = 0
+        self.new_surface.extend(ns.tolist())
+        self.max_edge.extend([float(max_edge)] * len(q))
+
     @property
     def n_tris(self) -> int:
         return 2 * len(self.quads)
@@ -304,3 +318,94 @@ def _abox(rec, mn, mx, m):
     rec.quad((ax, by, az), (bx, by, az), (bx, by, bz), (ax, by, bz), m)
     rec.quad((ax, ay, az), (bx, ay, az), (bx, by, az), (ax, by, az), m)
     rec.quad((ax, ay, bz), (ax, by, bz), (bx, by, bz), (bx, ay, bz), m)
+
+
+# ------------------------------------------------------------------ config 5
+@dataclass
+class CityCase:
+    recorder: Recorder
+    sources: np.ndarray          # (16, 3)
+    listeners: np.ndarray        # (16, 3), one per source
+    dome_eyes: np.ndarray        # (n_eyes, 3)
+    buildings: np.ndarray        # (n, 6): footprint min x, y, size x, y, height, floor height
+    n_bands: int
+
+
+def _grid_quads(p0, u, v, nu, nv):
+    """nu x nv cells of the parallelogram p0 + [0,1] u + [0,1] v: (nu nv, 4, 3)
+    corners (p, p + u/nu, p + u/nu + v/nv, p + v/nv)."""
+    i, j = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    i, j = i.reshape(-1, 1), j.reshape(-1, 1)
+    du, dv = np.asarray(u) / nu, np.asarray(v) / nv
+    a = np.asarray(p0) + i * du + j * dv
+    return np.stack([a, a + du, a + du + dv, a + dv], axis=1)
+
+
+def city(seed: int = 5, nx: int = 20, ny: int = 10, pitch: float = 60.0, cell: float = 1.5, slab_cell: float = 3.0,
+         floors=(5, 28), window_frac: float = 0.4, n_bands: int = 8, n_sources: int = 16,
+         n_dome: int = 1024, jitter: float = 0.01) -> CityCase:
+    """Procedural city: nx x ny buildings (subdivided boxes: facades in
+    `cell`-wide panels with a `window_frac` share left open as aperture holes,
+    floor slabs and a roof in `slab_cell` cells) on a subdivided ground plane;
+    every vertex jittered N(0, jitter) m. 20 x 10 buildings give about 1 M
+    triangles. Sources, their listeners and the dome eyes stand in the streets
+    at 1.5 m."""
+    rng = np.random.default_rng(seed)
+    rec = Recorder()
+    facade = rec.material(Material(tuple(float(v) for v in rng.uniform(0.02, 0.1, n_bands)), 0.2,
+                                   tuple([0.0] * n_bands)))
+    slab = rec.material(Material(tuple(float(v) for v in rng.uniform(0.01, 0.05, n_bands)), 0.1,
+                                 tuple([0.0] * n_bands)))
+    ground = rec.material(Material(tuple(float(v) for v in rng.uniform(0.02, 0.15, n_bands)), 0.3,
+                                   tuple([0.0] * n_bands)))
+    blocks = []
+    quads, mats, surf = [], [], []
+
+    def add(q, m):
+        n = len(q)
+        quads.append(q.reshape(n, 12))
+        mats.append(np.full(n, m))
+        s_ = np.zeros(n, int)
+        s_[0] = 1
+        surf.append(s_)
+
+    for bx in range(nx):
+        for by in range(ny):
+            w, d = rng.uniform(15.0, 45.0, 2)
+            x0 = bx * pitch + (pitch - w) / 2
+            y0 = by * pitch + (pitch - d) / 2
+            nf = int(rng.integers(floors[0], floors[1] + 1))
+            fh = 3.5
+            h = nf * fh
+            blocks.append((x0, y0, w, d, h, fh))
+            corners = [(x0, y0), (x0 + w, y0), (x0 + w, y0 + d), (x0, y0 + d)]
+            for k in range(4):
+                (ax, ay), (cx, cy) = corners[k], corners[(k + 1) % 4]
+                length = float(np.hypot(cx - ax, cy - ay))
+                nu = max(1, int(round(length / cell)))
+                q = _grid_quads((ax, ay, 0.0), (cx - ax, cy - ay, 0.0), (0.0, 0.0, h), nu, nf)
+                keep = rng.random(len(q)) >= window_frac   # open cells are aperture holes
+                add(q[keep], facade)
+            for f in range(1, nf + 1):
+                z = f * fh
+                nu, nv = max(1, int(round(w / slab_cell))), max(1, int(round(d / slab_cell)))
+                add(_grid_quads((x0, y0, z), (w, 0.0, 0.0), (0.0, d, 0.0), nu, nv), slab)
+    gx, gy = nx * pitch, ny * pitch
+    add(_grid_quads((0.0, 0.0, 0.0), (gx, 0.0, 0.0), (0.0, gy, 0.0), int(gx / 10), int(gy / 10)), ground)
+    q = np.concatenate(quads)
+    q = q + rng.normal(0.0, jitter, q.shape).astype(np.float32)
+    rec.add_quads(q, np.concatenate(mats), np.concatenate(surf), 4.0)
+
+    def street_points(n):
+        # on the street lines between blocks, 1.5 m up
+        i = rng.integers(0, nx, n)
+        j = rng.integers(0, ny, n)
+        along = rng.random(n)
+        xs = np.where(rng.random(n) < 0.5, i * pitch + along * pitch, i * pitch + 1.0)
+        ys = np.where(xs == i * pitch + 1.0, j * pitch + along * pitch, j * pitch + 1.0)
+        return np.stack([xs, ys, np.full(n, 1.5)], 1).astype(np.float32)
+
+    src = street_points(n_sources)
+    lis = street_points(n_sources)
+    eyes = street_points(n_dome)
+    return CityCase(rec, src, lis, eyes, np.array(blocks, np.float32), n_bands)
