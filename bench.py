@@ -261,7 +261,19 @@ def run_workload(args):
     torch.cuda.set_stream(stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     t0 = time.perf_counter()
-    if args.workload == "rooms256":
+    oracle_jobs = []   # (mesh recorder or box, src, lis, n_rays, seed, n_bands, n_bins, max_time) for the CPU leg
+    if args.workload == "shoebox12":
+        case = W.shoebox12(seed=1)
+        ctx = Context(TraceConfig(timeout_ms=60000, tie_mode=1, **CFG))
+        mb = MeshBuilder()
+        case.recorder.replay(mb)
+        sc = ctx.upload_builder(mb, 3, bvh)
+        jobs = [Job(case.src, case.lis, N_RAYS, seed=11, scene=sc)]
+        oracle_jobs = [(case.recorder, case.src, case.lis, N_RAYS, 11, 3, CFG["n_bins"], CFG["max_time"])]
+        desc = "shoebox12: 10 x 7 x 4 m room as 12 triangles, 4096 rays x 3 bands, 2000 x 1 ms bins, 200 bounces"
+        dome = None
+        prims = sc.info()["prims"]
+    elif args.workload == "rooms256":
         rooms = W.room_batch(seed=3, n_rooms=256)
         ctx = Context(TraceConfig(timeout_ms=120000, tie_mode=1, n_bins=4000, max_time=4.0, max_bounces=200,
                                   energy_floor=1e-6))
@@ -273,6 +285,8 @@ def run_workload(args):
             scenes.append(sc)
             jobs.append(Job(r.src, r.lis, r.n_rays, seed=100 + k, scene=sc, n_bands=r.n_bands, n_bins=r.n_bins,
                             max_time=r.max_time))
+            if k < 16:
+                oracle_jobs.append((r.recorder, r.src, r.lis, r.n_rays, 100 + k, r.n_bands, r.n_bins, r.max_time))
         desc = ("rooms256: 256 rooms, triangles lognormal (median 2k, 12-20k), rays lognormal 512-65536 "
                 f"({sum(j.n_rays for j in jobs)} in all), bands 3 or 8, 0.5-4 s at 1 ms, one batch")
         dome = None
@@ -288,6 +302,8 @@ def run_workload(args):
         jobs = [Job(tuple(s_), tuple(l_), args.city_rays, seed=500 + k, scene=scene)
                 for k, (s_, l_) in enumerate(zip(case.sources, case.listeners))]
         dome = DomeProbe(ctx, scene, (), n_fan=512)
+        oracle_jobs = [(case.recorder, tuple(case.sources[0]), tuple(case.listeners[0]), 4096, 500, case.n_bands,
+                        4000, 4.0)]
         desc = (f"city: {case.recorder.n_tris} triangles ({prims} primitives), 16 sources x {args.city_rays} rays "
                 f"x 8 bands, 4 s at 1 ms, 200 bounces, floor 1e-6, + 512-ray dome fans of "
                 f"{len(case.dome_eyes)} listeners")
@@ -326,6 +342,41 @@ def run_workload(args):
             "autotune": tune, "clocks": clk.summary(),
             "rt60_range": [float(np.nanmin([np.min(rv.rt60) for _, rv in res])),
                            float(np.nanmax([np.max(rv.rt60) for _, rv in res]))]}
+    # CPU leg: the f32 oracle (the reference's algorithm over the reference's
+    # SAH tree) on a sample, all host threads and one; its traversal counters
+    # give the reference's bytes per segment on this configuration
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    seg = nodes = prims_t = hits = 0
+    sec = sec1 = seg1 = 0.0
+    for rec, src, lis, n_rays, seed, nb, n_bins, tmax in oracle_jobs:
+        ob = O.MeshBuilder()
+        rec.replay(ob, lambda m: O.Material.make(m.absorption, m.scattering, m.transmission))
+        mesh = ob.build("f32")
+        P = O.params(tie_mode=1, n_bands=nb, n_bins=n_bins, bin_dt=0.001, max_time=tmax, max_bounces=200,
+                     energy_floor=1e-6)
+        t0 = time.perf_counter()
+        _, _, st = O.trace_mesh(mesh, src, lis, n_rays, energy=[1.0] * nb, P=P, seed=seed, threads=threads)
+        sec += time.perf_counter() - t0
+        seg += st["segments"]
+        nodes += st["node_reads"]
+        prims_t += st["prim_tests"]
+        hits += st["receiver_hits"]
+        t0 = time.perf_counter()
+        _, _, s1 = O.trace_mesh(mesh, src, lis, n_rays, energy=[1.0] * nb, P=P, seed=seed, threads=1,
+                                ray_end=min(n_rays, 256))
+        sec1 += time.perf_counter() - t0
+        seg1 += s1["segments"]
+    if seg:
+        nbm = max(r[5] for r in oracle_jobs)
+        bseg = 32.0 * nodes / seg + 48.0 * prims_t / seg + 4.0 * (nbm + 3) * hits / seg
+        peak, peak_kind = peaks()
+        line["cpu_baseline"] = {"value": seg / sec, "unit": "ray-segments/s", "cores": threads, "kind": "port",
+                                "one_thread": seg1 / sec1,
+                                "sample": f"{len(oracle_jobs)} job(s) of the workload (f32 oracle)"}
+        line["roofline"] = {"bound": "hbm", "bytes_per_segment": bseg, "achieved": line["value"] * bseg / 1e9,
+                            "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                            "frac": line["value"] * bseg / 1e9 / peak}
     if dome is not None:
         dseg = dres["segments"]["escape_events"] + dres["segments"]["through_calls"]
         line["dome"] = {"eyes": len(case.dome_eyes), "ms": float(np.mean(dms)), "segments": dseg,
@@ -514,7 +565,7 @@ def main():
                     help="launch shape as JSON (omg_tune_result fields), instead of the autotuner")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the launch-shape autotuner (it runs once, before the warm-up)")
-    ap.add_argument("--workload", choices=["multiroom", "rooms256", "city"], default="multiroom",
+    ap.add_argument("--workload", choices=["multiroom", "shoebox12", "rooms256", "city"], default="multiroom",
                     help="multiroom: the headline (default); rooms256 and city print their own line")
     ap.add_argument("--city-rays", type=int, default=1 << 20, help="rays per source of the city workload")
     args = ap.parse_args()
