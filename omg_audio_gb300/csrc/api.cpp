@@ -65,6 +65,8 @@ int32_t sync_scene_table(omg_ctx* ctx) {
     d.n_bands = s.n_bands;
     d.nodes4 = s.n_nodes4 ? s.nodes4.p : nullptr;
     d.nodes4c = s.n_nodes4 ? s.nodes4c.p : nullptr;
+    d.nodes_f = s.nodes_f.p;
+    for (int a = 0; a < 3; a++) d.fast_m[a] = s.fast_m[a];
     d.root4 = s.root4;
     d.n_nodes4 = s.n_nodes4;
   }

@@ -84,6 +84,12 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
     CK(S->nodes.alloc(S->n_nodes * 4));
     if (S->n_nodes)
       CK(cudaMemcpy(S->nodes.p, dev_nodes.data(), dev_nodes.size() * 4, cudaMemcpyHostToDevice));
+    if (S->n_nodes) {
+      std::vector<float> grown;
+      grow_nodes_for_fma(dev_nodes, grown, S->fast_m);
+      CK(S->nodes_f.alloc(S->n_nodes * 4));
+      CK(cudaMemcpy(S->nodes_f.p, grown.data(), grown.size() * 4, cudaMemcpyHostToDevice));
+    }
     std::vector<float> dev_nodes4;
     uint32_t need = 0;
     S->root4 = flatten_bvh4(S->ref_boxes, S->ref_ab, dev_nodes4, &need);
@@ -144,6 +150,21 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
         std::memcpy(&t, &o[7], 4);
         S->prim_mat[i] = (uint16_t)m;
         S->prim_tri[i] = t;
+      }
+      // grown boxes for the near-tie walks: the bound from the primitives
+      float mx[3] = {0.0f, 0.0f, 0.0f};
+      for (uint32_t i = 0; i < S->n_prims; i++) {
+        const float* g = &S->prim_geo[9 * i];
+        for (int a = 0; a < 3; a++) {
+          const float p0 = g[a], p1 = g[a] + g[3 + a], p2 = g[a] + g[6 + a];
+          mx[a] = std::max(mx[a], std::max(std::fabs(p0), std::max(std::fabs(p1), std::fabs(p2))));
+        }
+      }
+      for (int a = 0; a < 3; a++) S->fast_m[a] = mx[a] + 1.0f;
+      if (S->root >= 0 && S->n_nodes) {
+        CK(S->nodes_f.alloc((size_t)S->n_nodes * 4));
+        CK(grow_nodes(S->nodes.p, S->nodes_f.p, S->n_nodes, S->fast_m, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
       }
     }
   }

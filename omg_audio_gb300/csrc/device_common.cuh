@@ -107,6 +107,26 @@ __device__ __forceinline__ bool ray_aabb(float lx, float ly, float lz, float hx,
   return t0 <= t1;
 }
 
+// Slab test with t = fma(l, inv, -o inv) (oi = o inv) and min/max
+// instructions, on boxes grown by DScene::nodes_f's margin. For an origin
+// with |o_a| <= 7 M_a it accepts every box ray_aabb accepts on the ungrown
+// box and returns an entry distance no larger: the rounding of t differs from
+// ray_aabb's by at most 4 u (|lo_a| + |o_a|) |inv_a| <= 2^-22 8 M_a |inv_a|
+// (u = 2^-24), no more than the margin 2^-19 M_a moves a face; a NaN from an
+// infinite inv leaves its axis open. Used only where the visit order does not
+// decide the hit (the near-tie rule), so the result is ray_aabb's.
+__device__ __forceinline__ bool ray_aabb_fma(float lx, float ly, float lz, float hx, float hy, float hz, float oix,
+                                             float oiy, float oiz, float ix, float iy, float iz, float tmax,
+                                             float& tout) {
+  const float ax = __fmaf_rn(lx, ix, -oix), bx = __fmaf_rn(hx, ix, -oix);
+  const float ay = __fmaf_rn(ly, iy, -oiy), by = __fmaf_rn(hy, iy, -oiy);
+  const float az = __fmaf_rn(lz, iz, -oiz), bz = __fmaf_rn(hz, iz, -oiz);
+  const float t0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), 0.0f));
+  const float t1 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fminf(fmaxf(az, bz), tmax));
+  tout = t0;
+  return t0 <= t1;
+}
+
 // mesh.rs:436-456 — Möller–Trumbore, both faces, reference epsilons.
 __device__ __forceinline__ bool ray_tri(const float4& p0, const float4& p1, const float4& p2, float ox, float oy,
                                         float oz, float dx, float dy, float dz, float& tout) {

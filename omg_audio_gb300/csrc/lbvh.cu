@@ -348,4 +348,33 @@ cudaError_t lbvh_build(const float4* prims_in, uint32_t n, float4* prims_out, fl
   return herr ? cudaErrorInvalidValue : cudaSuccess;
 }
 
+
+namespace {
+// Child boxes of every binary node grown by 2^-19 m[a] on each side, rounded
+// outward (DScene::nodes_f).
+__global__ void grow_nodes_kernel(const float4* __restrict__ in, float4* __restrict__ out, uint32_t n, float mx,
+                                  float my, float mz) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float g[3] = {ldexpf(mx, -19), ldexpf(my, -19), ldexpf(mz, -19)};
+  float v[16];
+  for (int i = 0; i < 4; i++) {
+    const float4 q = in[4 * k + i];
+    v[4 * i] = q.x; v[4 * i + 1] = q.y; v[4 * i + 2] = q.z; v[4 * i + 3] = q.w;
+  }
+  for (int c = 0; c < 2; c++)
+    for (int a = 0; a < 3; a++) {
+      v[6 * c + a] = __fsub_rd(v[6 * c + a], g[a]);
+      v[6 * c + 3 + a] = __fadd_ru(v[6 * c + 3 + a], g[a]);
+    }
+  for (int i = 0; i < 4; i++) out[4 * k + i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+}  // namespace
+
+cudaError_t grow_nodes(const float4* nodes, float4* out, uint32_t n_nodes, const float m[3], cudaStream_t s) {
+  if (n_nodes == 0) return cudaSuccess;
+  grow_nodes_kernel<<<(n_nodes + 255) / 256, 256, 0, s>>>(nodes, out, n_nodes, m[0], m[1], m[2]);
+  return cudaGetLastError();
+}
+
 }  // namespace omg

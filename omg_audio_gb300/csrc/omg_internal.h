@@ -61,6 +61,12 @@ struct DScene {
   // children over 4 lanes: 32 B per child, child k of node n at float4 index
   // 8 n + 2 k: (lo.x, lo.y, lo.z, hi.x), (hi.y, hi.z, ref bits, 0).
   const float4* nodes4c;
+  // `nodes` with every child box grown by 2^-19 M_a on each side (M_a: the
+  // scene's largest |coordinate| along axis a, plus 1 m), for the fused
+  // multiply-add slab test of near-tie walks whose origin lies within
+  // |o_a| <= 7 M_a (device_common.cuh:ray_aabb_fma); null: exact test only.
+  const float4* nodes_f;
+  float fast_m[3];
 };
 constexpr int32_t kEmpty4 = 0x7FFFFFFE;
 
@@ -230,6 +236,8 @@ cudaError_t launch_reverb(const DReverbJob* rj, uint32_t n_jobs, uint32_t max_bi
 cudaError_t lbvh_build(const float4* prims_in, uint32_t n_prims, float4* prims_out, float4* nodes_out,
                        int32_t* root_ref, void* scratch, size_t scratch_bytes, cudaStream_t s);
 size_t lbvh_scratch_bytes(uint32_t n_prims);
+// DScene::nodes_f from `nodes` on the device (m: the bound of |coordinate| per axis)
+cudaError_t grow_nodes(const float4* nodes, float4* out, uint32_t n_nodes, const float m[3], cudaStream_t s);
 
 // dome.cu
 struct DDomePanel {

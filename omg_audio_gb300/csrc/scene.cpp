@@ -427,6 +427,29 @@ int32_t flatten_bvh4(const std::vector<float>& ref_boxes, const std::vector<uint
   return 0;
 }
 
+void grow_nodes_for_fma(const std::vector<float>& dev_nodes, std::vector<float>& out, float m[3]) {
+  const size_t n = dev_nodes.size() / 16;
+  // child box c of node k: lo at 16k + 6c + {0,1,2}, hi at 16k + 6c + {3,4,5}
+  float mx[3] = {0.0f, 0.0f, 0.0f};
+  for (size_t k = 0; k < n; k++)
+    for (int c = 0; c < 2; c++)
+      for (int j = 0; j < 6; j++) {
+        const float v = std::fabs(dev_nodes[16 * k + 6 * c + j]);
+        if (std::isfinite(v)) mx[j % 3] = std::max(mx[j % 3], v);
+      }
+  for (int a = 0; a < 3; a++) m[a] = mx[a] + 1.0f;
+  out = dev_nodes;
+  for (size_t k = 0; k < n; k++)
+    for (int c = 0; c < 2; c++)
+      for (int a = 0; a < 3; a++) {
+        const float grow = std::ldexp(m[a], -19);
+        float& lo = out[16 * k + 6 * c + a];
+        float& hi = out[16 * k + 6 * c + 3 + a];
+        lo = std::nextafter(lo - grow, -INFINITY);
+        hi = std::nextafter(hi + grow, INFINITY);
+      }
+}
+
 // mesh.rs:458-461 per original triangle; .w carries the material id bits.
 void tri_normals(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
                  std::vector<float>& out) {

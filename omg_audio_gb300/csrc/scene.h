@@ -56,6 +56,11 @@ int32_t flatten_bvh2(const std::vector<float>& ref_boxes, const std::vector<uint
 // walk of it can need.
 int32_t flatten_bvh4(const std::vector<float>& ref_boxes, const std::vector<uint32_t>& ref_ab,
                      std::vector<float>& dev_nodes, uint32_t* max_stack);
+// The binary nodes (flatten_bvh2 layout) with every child box grown for the
+// fused multiply-add slab test: by 2^-19 m[a] on each side, rounded outward,
+// where m[a] bounds |coordinate| along axis a of the scene (filled here: the
+// largest |box coordinate| plus 1 m).
+void grow_nodes_for_fma(const std::vector<float>& dev_nodes, std::vector<float>& out, float m[3]);
 void tri_normals(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
                  std::vector<float>& out);
 DMat make_dmat(const omg_material& m, uint32_t nb);

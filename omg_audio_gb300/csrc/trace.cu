@@ -34,6 +34,7 @@ struct Walk {
   uint32_t s_best, tri_best;
   int prim_best;
   float ix, iy, iz;
+  bool fast;             // origin within the grown boxes' margin (else every box counts as hit)
   uint32_t budget;
   int* stack_ref;
   float* stack_t;
@@ -56,7 +57,8 @@ __device__ __forceinline__ int walk_pop(Walk& w) {
 }
 
 template <bool TIE>
-__device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float dx, float dy, float dz, bool wide) {
+__device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float ox, float oy, float oz, float dx, float dy,
+                                           float dz, bool wide) {
   // the 4-wide tree (when asked for, and the scene has one) where the
   // near-tie rule lets the visit order differ
   w.cur = S.n_prims ? ((TIE && wide && S.nodes4) ? S.root4 : S.root) : kDone;
@@ -71,6 +73,8 @@ __device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float dx, f
   w.ix = __frcp_rn(dx);
   w.iy = __frcp_rn(dy);
   w.iz = __frcp_rn(dz);
+  // the margin 2^-19 M_a covers the slab test's rounding for |o_a| <= 7 M_a
+  w.fast = fabsf(ox) <= 7.0f * S.fast_m[0] && fabsf(oy) <= 7.0f * S.fast_m[1] && fabsf(oz) <= 7.0f * S.fast_m[2];
   w.budget = 2u * S.n_nodes + S.n_prims + 64u;
 }
 
@@ -87,6 +91,90 @@ __device__ __forceinline__ bool walk4_steps(Walk& w, const DScene& S, float ox, 
                       w.t_cull, w.prim_best, w.s_best, w.tri_best, w.stack_ref, w.stack_t, w.sp, err);
   }
   return w.cur == kDone;
+}
+
+// The near-tie walk (TIE = true): speculative while-while over the grown
+// boxes with the fused multiply-add slab test. A ray whose origin lies beyond
+// the boxes' margin (|o_a| > 7 M_a: never in a trace that starts inside the
+// scene) takes every box as hit and walks the whole tree: slow, still exact.
+__device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, float oy, float oz, float dx,
+                                          float dy, float dz, int steps, uint32_t* err) {
+  // speculative while-while: descend, postponing one leaf, until every lane of
+  // the warp holds a leaf; then test leaves
+  const float4* __restrict__ tnodes = S.nodes_f;
+  const float4* __restrict__ prims = S.prims;
+  while (steps > 0 && w.cur >= 0 && w.cur != kDone) {
+    steps--;
+    if (w.budget-- == 0u) {
+      atomicOr(err, 4u);
+      w.cur = kDone;
+      w.leaf = 0;
+      return true;
+    }
+    const float4 n0 = __ldg(tnodes + 4 * w.cur + 0);
+    const float4 n1 = __ldg(tnodes + 4 * w.cur + 1);
+    const float4 n2 = __ldg(tnodes + 4 * w.cur + 2);
+    const float4 n3 = __ldg(tnodes + 4 * w.cur + 3);
+    const float tmax = w.have ? w.t_cull : FLT_MAX;
+    float ta, tb;
+    bool h0, h1;
+    {
+      const float oix = ox * w.ix, oiy = oy * w.iy, oiz = oz * w.iz;
+      h0 = ray_aabb_fma(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, oix, oiy, oiz, w.ix, w.iy, w.iz, tmax, ta);
+      h1 = ray_aabb_fma(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, oix, oiy, oiz, w.ix, w.iy, w.iz, tmax, tb);
+      if (!w.fast) {
+        h0 = h1 = true;
+        ta = tb = 0.0f;
+      }
+    }
+    const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+    if (h0 && h1) {
+      int nr, fr;
+      float nt, ft;
+      if (ta <= tb) { nr = c0; nt = ta; fr = c1; ft = tb; }
+      else { nr = c1; nt = tb; fr = c0; ft = ta; }
+      if (w.sp < STACK_DEPTH) {
+        w.stack_ref[w.sp] = fr;
+        w.stack_t[w.sp] = ft;
+        w.sp++;
+      } else {
+        atomicOr(err, 1u);
+      }
+      w.cur = nr;   // nt <= tmax = t_cull: never culled here
+    } else if (h0) {
+      w.cur = c0;
+    } else if (h1) {
+      w.cur = c1;
+    } else {
+      w.cur = walk_pop<true>(w);
+    }
+    if (w.cur < 0 && w.leaf == 0) {
+      w.leaf = w.cur;
+      w.cur = walk_pop<true>(w);
+    }
+    if (__all_sync(__activemask(), w.leaf < 0 || w.cur == kDone)) break;
+  }
+  if (w.leaf == 0 && w.cur < 0) {
+    w.leaf = w.cur;
+    w.cur = walk_pop<true>(w);
+  }
+  while (w.leaf < 0 && steps > 0) {
+    steps--;
+    if (w.budget-- == 0u) {
+      atomicOr(err, 4u);
+      w.cur = kDone;
+      w.leaf = 0;
+      return true;
+    }
+    leaf_test<true>(prims, w.leaf, ox, oy, oz, dx, dy, dz, w.have, w.t_best, w.t_cull, w.prim_best, w.s_best,
+                   w.tri_best);
+    w.leaf = 0;
+    if (w.cur < 0) {
+      w.leaf = w.cur;
+      w.cur = walk_pop<true>(w);
+    }
+  }
+  return w.cur == kDone && w.leaf == 0;
 }
 
 // Up to `steps` node visits / leaf tests; returns true when the walk is done.
@@ -142,72 +230,7 @@ __device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, f
     }
     return w.cur == kDone;
   }
-  // speculative while-while: descend, postponing one leaf, until every lane of
-  // the warp holds a leaf; then test leaves
-  while (steps > 0 && w.cur >= 0 && w.cur != kDone) {
-    steps--;
-    if (w.budget-- == 0u) {
-      atomicOr(err, 4u);
-      w.cur = kDone;
-      w.leaf = 0;
-      return true;
-    }
-    const float4 n0 = __ldg(nodes + 4 * w.cur + 0);
-    const float4 n1 = __ldg(nodes + 4 * w.cur + 1);
-    const float4 n2 = __ldg(nodes + 4 * w.cur + 2);
-    const float4 n3 = __ldg(nodes + 4 * w.cur + 3);
-    const float tmax = w.have ? w.t_cull : FLT_MAX;
-    float ta, tb;
-    const bool h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ox, oy, oz, w.ix, w.iy, w.iz, tmax, ta);
-    const bool h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ox, oy, oz, w.ix, w.iy, w.iz, tmax, tb);
-    const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-    if (h0 && h1) {
-      int nr, fr;
-      float nt, ft;
-      if (ta <= tb) { nr = c0; nt = ta; fr = c1; ft = tb; }
-      else { nr = c1; nt = tb; fr = c0; ft = ta; }
-      if (w.sp < STACK_DEPTH) {
-        w.stack_ref[w.sp] = fr;
-        w.stack_t[w.sp] = ft;
-        w.sp++;
-      } else {
-        atomicOr(err, 1u);
-      }
-      w.cur = (w.have && nt > w.t_cull) ? walk_pop<TIE>(w) : nr;
-    } else if (h0) {
-      w.cur = (w.have && ta > w.t_cull) ? walk_pop<TIE>(w) : c0;
-    } else if (h1) {
-      w.cur = (w.have && tb > w.t_cull) ? walk_pop<TIE>(w) : c1;
-    } else {
-      w.cur = walk_pop<TIE>(w);
-    }
-    if (w.cur < 0 && w.leaf == 0) {
-      w.leaf = w.cur;
-      w.cur = walk_pop<TIE>(w);
-    }
-    if (__all_sync(__activemask(), w.leaf < 0 || w.cur == kDone)) break;
-  }
-  if (w.leaf == 0 && w.cur < 0) {
-    w.leaf = w.cur;
-    w.cur = walk_pop<TIE>(w);
-  }
-  while (w.leaf < 0 && steps > 0) {
-    steps--;
-    if (w.budget-- == 0u) {
-      atomicOr(err, 4u);
-      w.cur = kDone;
-      w.leaf = 0;
-      return true;
-    }
-    leaf_test<TIE>(prims, w.leaf, ox, oy, oz, dx, dy, dz, w.have, w.t_best, w.t_cull, w.prim_best, w.s_best,
-                   w.tri_best);
-    w.leaf = 0;
-    if (w.cur < 0) {
-      w.leaf = w.cur;
-      w.cur = walk_pop<TIE>(w);
-    }
-  }
-  return w.cur == kDone && w.leaf == 0;
+  return walk_spec(w, S, ox, oy, oz, dx, dy, dz, steps, err);
 }
 
 // The tracer. Each lane runs a small state machine so that a lane whose
@@ -274,7 +297,7 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
       have = box_hit(J, job_mats, px, py, pz, dx, dy, dz, h);
       phase = SHADE;
     } else {
-      walk_begin<TIE>(w, scenes[J.scene], dx, dy, dz, wide);
+      walk_begin<TIE>(w, scenes[J.scene], px, py, pz, dx, dy, dz, wide);
       phase = WALK;
     }
   };
@@ -468,7 +491,7 @@ __global__ void __launch_bounds__(256, 4) trace_wl_kernel(const DJob* __restrict
     ox = P.x; oy = P.y; oz = P.z;
     dx = D.x; dy = D.y; dz = D.z;
     wsc = scenes + J.scene;
-    walk_begin<TIE>(w, *wsc, dx, dy, dz, wide);
+    walk_begin<TIE>(w, *wsc, ox, oy, oz, dx, dy, dz, wide);
     rid = r;
   };
   // ended rays (and the park signal), parked rays to the next epoch's queue
