@@ -279,7 +279,7 @@ typedef struct omg_tune_result {
     uint32_t walk_steps;         /* traversal steps per lane per loop iteration (0 = whole walk) */
     uint32_t shade_min;          /* lanes of a warp that shade together (1..32; 0 reads as 1) */
     uint32_t mode;               /* persistent kernel: 0 per-lane state machine, 1 warp-local wavefront
-                                    (walks refill lane by lane; rays shade 32 at a time), 2 the same with
+                                    (walks refill lane by lane; rays shade wl_shade_min at a time), 2 the same with
                                     each walk split over 4 lanes of a 4-wide tree (tie_mode 1 and
                                     host-built trees; otherwise mode 0 runs) */
     uint32_t tail_mode;          /* persistent kernel of epochs after the first (same values) */
@@ -288,6 +288,8 @@ typedef struct omg_tune_result {
     uint32_t wf_tail;            /* hand over to the persistent kernel at <= this many live rays */
     uint32_t epochs;             /* persistent-kernel epochs, <= 32 (0 = one launch) */
     uint32_t park_pct;           /* an epoch parks its rays once <= this % of them remain */
+    uint32_t wl_shade_min;       /* modes 1 and 2: rays a warp shades together once that many wait
+                                    (1..32, 0 reads as 32; every waiting ray once none walks) */
     float ms;                    /* autotune: mean time of the clear + trace part */
 } omg_tune_result;
 int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t batch_id, uint32_t reps, omg_tune_result* best);

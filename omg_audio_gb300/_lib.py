@@ -70,7 +70,8 @@ class omg_dome_bin(C.Structure):
 class omg_tune_result(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("refill_min", C.c_uint32),
                 ("walk_steps", C.c_uint32), ("shade_min", C.c_uint32), ("mode", C.c_uint32), ("tail_mode", C.c_uint32), ("wide", C.c_uint32), ("wf_rounds", C.c_uint32), ("wf_tail", C.c_uint32),
-                ("epochs", C.c_uint32), ("park_pct", C.c_uint32), ("ms", C.c_float)]
+                ("epochs", C.c_uint32), ("park_pct", C.c_uint32), ("wl_shade_min", C.c_uint32),
+                ("ms", C.c_float)]
 
 
 class omg_mlp_config(C.Structure):

@@ -775,14 +775,16 @@ void shape_to_result(const LaunchShape& sh, float ms, omg_tune_result* r) {
   r->mode = sh.mode;
   r->tail_mode = sh.tail_mode;
   r->wide = sh.wide;
+  r->wl_shade_min = sh.wl_shade_min;
   r->ms = ms;
 }
 
 }  // namespace
 
-// Three stages: the persistent kernel's shape alone (one launch), then epoch
-// counts and park thresholds with that shape, then wavefront round counts and
-// hand-over thresholds in front of the best of those.
+// Four stages: the persistent kernel's shape alone (one launch), then epoch
+// counts and park thresholds with that shape, then the wavefront kernels'
+// shading group (when the best shape runs one), then wavefront round counts
+// and hand-over thresholds in front of the best of those.
 int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_result* best) {
   if (!ctx || !best) return OMG_E_INVALID;
   auto it = ctx->batches.find(id);
@@ -800,6 +802,7 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
   const uint32_t epoch_counts[] = {2, 3, 4, 8};
   const uint32_t park_pcts[] = {5, 10, 20, 40};
   const uint32_t tail_modes[] = {0, 2};
+  const uint32_t wl_shades[] = {1, 4, 8, 16};
   cudaEvent_t e0, e1;
   cudaStream_t cs;
   CK(cudaEventCreate(&e0));
@@ -857,6 +860,16 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
         sh.tail_mode = tm;
         rc = try_shape(sh);
       }
+  // the shading group of the wavefront kernels (modes 1 and 2), where the
+  // best shape so far runs one of them
+  const LaunchShape grouped = best_shape;
+  if (grouped.mode != 0 || (grouped.epochs > 1 && grouped.tail_mode != 0))
+    for (uint32_t ws : wl_shades) {
+      if (rc) continue;
+      LaunchShape sh = grouped;
+      sh.wl_shade_min = ws;
+      rc = try_shape(sh);
+    }
   const LaunchShape chained = best_shape;
   for (uint32_t nr : rounds)
     for (uint32_t tl : tails) {
@@ -885,7 +898,7 @@ int32_t omg_batch_set_shape(omg_ctx* ctx, uint32_t id, const omg_tune_result* sh
   if (shape->block_threads == 0 || shape->block_threads % 32 != 0 || shape->block_threads > 256 ||
       shape->blocks_per_sm == 0 || shape->block_threads * shape->blocks_per_sm > 2048 || shape->refill_min == 0 ||
       shape->refill_min > 32 || shape->wf_rounds > 4096 || shape->epochs > kMaxEpochs || shape->park_pct > 100 ||
-      shape->shade_min > 32 || shape->mode > 2 || shape->tail_mode > 2)
+      shape->shade_min > 32 || shape->mode > 2 || shape->tail_mode > 2 || shape->wl_shade_min > 32)
     return OMG_E_INVALID;
   BatchRec& B = *it->second;
   LaunchShape sh;
@@ -901,6 +914,7 @@ int32_t omg_batch_set_shape(omg_ctx* ctx, uint32_t id, const omg_tune_result* sh
   sh.mode = shape->mode;
   sh.tail_mode = shape->tail_mode;
   sh.wide = shape->wide ? 1u : 0u;
+  sh.wl_shade_min = shape->wl_shade_min == 0 ? 32u : shape->wl_shade_min;
   B.shape = sh;
   int32_t rc = build_graphs(ctx, B);
   if (rc) return rc;

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
                                                             const DPanelGroup* __restrict__ groups,
                                                             float* __restrict__ acc, DLaunch* __restrict__ hdr,
                                                             uint32_t* __restrict__ job_segments, int walk_budget,
-                                                            EpochArgs ea) {
+                                                            uint32_t shade_min, EpochArgs ea) {
   __shared__ uint32_t s_shade[8][kQ];
   __shared__ uint32_t s_walk[8][kQ];
   __shared__ int s_sref[kGroupsPerBlock][STACK_DEPTH];
@@ -148,8 +148,9 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
     }
     unsigned walking = __ballot_sync(FULL, leader && rid != kNone);
 
-    // ---- shading pass, one ray per lane: 32 rays, or whatever waits once nothing can walk
-    if (sh_cnt >= 32u || (sh_cnt && !walking && !wk_cnt && (exhausted || parking))) {
+    // ---- shading pass, one ray per lane: once shade_min rays wait (at most 32 shade together), or
+    // whatever waits once nothing can walk
+    if (sh_cnt >= shade_min || (sh_cnt && !walking && !wk_cnt && (exhausted || parking))) {
       const uint32_t m = sh_cnt < 32u ? sh_cnt : 32u;
       bool alive = false, ended = false;
       uint32_t r = kNone;
@@ -332,12 +333,13 @@ cudaError_t launch_trace_coop(const DJob* jobs, uint32_t n_jobs, uint32_t total_
   uint32_t blocks = (uint32_t)(want < need ? want : need);
   if (blocks == 0) blocks = 1;
   const int steps = shape.walk_steps == 0 ? 1000000 : (int)shape.walk_steps;
+  const uint32_t shade_min = shape.wl_shade_min == 0 ? 32u : (shape.wl_shade_min > 32 ? 32u : shape.wl_shade_min);
   if (max_nb <= 3)
     trace_coop_kernel<3><<<blocks, kThreads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, groups,
-                                                     acc, hdr, job_segments, steps, ea);
+                                                     acc, hdr, job_segments, steps, shade_min, ea);
   else
     trace_coop_kernel<8><<<blocks, kThreads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, groups,
-                                                     acc, hdr, job_segments, steps, ea);
+                                                     acc, hdr, job_segments, steps, shade_min, ea);
   return cudaGetLastError();
 }
 

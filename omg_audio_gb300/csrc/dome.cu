@@ -1,10 +1,11 @@
 // Ambient-dome fan on the GPU (crates/omg-scene/src/dome.rs:293-478).
 //
-// One thread per (listener, fan ray): the specular escape (trace_escape,
-// dome.rs:330-382: <= max_events mesh hits or pane crossings, 80 m horizon)
-// and, when the escape is not near-full, the straight-through mass-law seep
-// (trace_through, dome.rs:390-422, over segment_hits, mesh.rs:546-604). A
-// second kernel bins the rays of each listener in fan order (dome.rs:452-458,
+// One thread per (listener, fan ray) traces the specular escape
+// (trace_escape, dome.rs:330-382: <= max_events mesh hits or pane crossings,
+// 80 m horizon); one warp per ray then adds, when the escape is not
+// near-full, the straight-through mass-law seep (trace_through,
+// dome.rs:390-422, over segment_hits, mesh.rs:546-604). A third kernel bins
+// the rays of each listener in fan order (dome.rs:452-458,
 // the same f32 sums in the same order), applies the per-listener EMA and
 // writes the 9 bins. The fan is deterministic, so the result is too.
 #include "device_common.cuh"
@@ -94,124 +95,205 @@ __device__ bool trace_escape(const DScene& S, const DDomeLaunch& L, float px, fl
   return false;
 }
 
-struct Cross {
-  float t;
-  uint32_t tri;
-  uint32_t mat;
+// One warp's shared memory for the straight-through segment of one fan ray.
+constexpr uint32_t kThroughWarps = 4;        // rays (warps) per block
+constexpr uint32_t kWarpStack = 512;         // pending node refs of one warp's walk
+constexpr uint32_t kMaxThroughRounds = 1u << 20;
+struct ThroughSmem {
+  int ref[kWarpStack];
+  unsigned long long key[kWarpStack];        // the ref's depth-first position (below)
+  float t[kMaxCross];                        // crossings as found
+  uint32_t prim[kMaxCross];
+  unsigned long long ckey[kMaxCross];
+  float st[kMaxCross];                       // crossings sorted
+  uint32_t sprim[kMaxCross];
+  uint32_t n;
 };
 
-// mesh.rs:546-604: every crossing strictly inside a->b, in the reference's
-// visit order (right subtree first), stably sorted, same-t clusters merged to
-// the lowest surface id. Returns the count (kMaxCross + 1 = overflow).
-__device__ uint32_t segment_hits(const DScene& S, float ax, float ay, float az, float bx, float by, float bz,
-                                 Cross* out) {
-  if (S.n_prims == 0) return 0;
-  float dx = bx - ax, dy = by - ay, dz = bz - az;
-  const float len = sqrtf(dx * dx + dy * dy + dz * dz);
-  if (len < 1e-6f) return 0;
-  const float il = __frcp_rn(len);
-  dx = dx * il;
-  dy = dy * il;
-  dz = dz * il;
-  const float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
-  uint32_t n = 0;
-  bool overflow = false;
-  int stack[STACK_DEPTH];
-  int sp = 0;
-  stack[sp++] = S.root;
-  while (sp > 0) {
-    const int cur = stack[--sp];
-    if (cur >= 0) {
-      const float4 n0 = __ldg(S.nodes + 4 * cur + 0);
-      const float4 n1 = __ldg(S.nodes + 4 * cur + 1);
-      const float4 n2 = __ldg(S.nodes + 4 * cur + 2);
-      const float4 n3 = __ldg(S.nodes + 4 * cur + 3);
-      float ta, tb;
-      const bool h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ax, ay, az, ix, iy, iz, len, ta);
-      const bool h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ax, ay, az, ix, iy, iz, len, tb);
-      // the reference pushes left then right and pops right first
-      if (h0) {
-        if (sp < STACK_DEPTH) stack[sp++] = __float_as_int(n3.x);
-        else overflow = true;
-      }
-      if (h1) {
-        if (sp < STACK_DEPTH) stack[sp++] = __float_as_int(n3.y);
-        else overflow = true;
-      }
-    } else {
-      const uint32_t code = ~(uint32_t)cur;
-      const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
-      for (uint32_t i = start; i < end; i++) {
-        const float4 p0 = __ldg(S.prims + 3 * i + 0);
-        const float4 p1 = __ldg(S.prims + 3 * i + 1);
-        const float4 p2 = __ldg(S.prims + 3 * i + 2);
-        float t;
-        if (ray_tri(p0, p1, p2, ax, ay, az, dx, dy, dz, t)) {
-          const float tt = t / len;
-          if (tt > 1e-4f && tt < 1.0f - 1e-4f) {
-            if (n < kMaxCross) out[n++] = Cross{tt, __float_as_uint(p1.w), __float_as_uint(p0.w)};
-            else overflow = true;
-          }
-        }
-      }
-    }
-  }
-  if (overflow) return kMaxCross + 1;
-  // stable insertion sort by t
-  for (uint32_t i = 1; i < n; i++) {
-    const Cross c = out[i];
-    uint32_t j = i;
-    while (j > 0 && out[j - 1].t > c.t) {
-      out[j] = out[j - 1];
-      j--;
-    }
-    out[j] = c;
-  }
-  const float tol = 1e-4f / fmaxf(len, 1.0f);
-  uint32_t w = 0;
-  for (uint32_t i = 0; i < n; i++) {
-    if (w > 0 && fabsf(out[i].t - out[w - 1].t) < tol) {
-      if (S.tri_surface[out[i].tri] < S.tri_surface[out[w - 1].tri]) {
-        out[w - 1].tri = out[i].tri;
-        out[w - 1].mat = out[i].mat;
-      }
-    } else {
-      out[w++] = out[i];
-    }
-  }
-  return w;
-}
-
-// dome.rs:384-422
-__device__ void trace_through(const DScene& S, const DDomeLaunch& L, float ex, float ey, float ez, float dx,
-                              float dy, float dz, float tp[MAXB]) {
+// Straight-through seep of one fan ray (trace_through, dome.rs:390-422) by a
+// whole warp. The crossings of the 50 m segment (segment_hits,
+// mesh.rs:546-604) are collected by a walk in which every lane takes one
+// pending ref per round (children whose box the segment meets are pushed
+// warp-aggregated, leaves test their primitives), so the any-hit walk, which
+// visits every node the segment meets, runs 32 nodes wide instead of one.
+//
+// The reference sorts the crossings by t with a stable sort over its
+// depth-first visiting order (child b before child a) and then merges
+// clusters within 1e-4 / max(len, 1) keeping the lowest surface id (the
+// first one on equal ids). Each ref therefore carries its depth-first
+// position: bit 63 - d set for the a child at depth d (d < 58) above a
+// 6-bit depth, so that ordering crossings by (t, key, primitive) reproduces
+// the reference's order, and the merge and the transmission product then run
+// in that order, uniformly across the warp.
+__device__ void through_warp(const DScene& S, const DDomeLaunch& L, ThroughSmem& W, uint32_t lane, float ex,
+                             float ey, float ez, float dx, float dy, float dz, float tp[MAXB]) {
+  constexpr unsigned FULL = 0xffffffffu;
   const uint32_t nb = L.nb;
-  const float bx = ex + dx * 50.0f, by = ey + dy * 50.0f, bz = ez + dz * 50.0f;
+  const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
   for (int b = 0; b < MAXB; b++) tp[b] = 1.0f;
+  const float bx = ex + dx * 50.0f, by = ey + dy * 50.0f, bz = ez + dz * 50.0f;
   if (bz < -0.05f) {
 #pragma unroll
     for (int b = 0; b < MAXB; b++) tp[b] = 0.0f;
     return;
   }
-  Cross hits[kMaxCross];
-  const uint32_t nh = segment_hits(S, ex, ey, ez, bx, by, bz, hits);
-  if (nh > kMaxCross) {
-    atomicOr(&L.hdr->error, 2u);
+  uint32_t n = 0;
+  uint32_t fail = 0;   // error bits: 1 walk overflow, 2 too many crossings
+  float len = 0.0f;
+  if (S.n_prims != 0) {
+    float sx = bx - ex, sy = by - ey, sz = bz - ez;
+    len = sqrtf(sx * sx + sy * sy + sz * sz);
+    if (len >= 1e-6f) {
+      const float il = __frcp_rn(len);
+      sx = sx * il;
+      sy = sy * il;
+      sz = sz * il;
+      const float ix = __frcp_rn(sx), iy = __frcp_rn(sy), iz = __frcp_rn(sz);
+      if (lane == 0) {
+        W.ref[0] = S.root;
+        W.key[0] = 0ull;
+        W.n = 0u;
+      }
+      __syncwarp();
+      uint32_t sp = 1, rounds = 0;
+      while (sp > 0) {
+        if (++rounds > kMaxThroughRounds) {
+          fail |= 1u;
+          break;
+        }
+        const uint32_t take = sp < 32u ? sp : 32u;
+        const uint32_t base = sp - take;
+        const bool act = lane < take;
+        int cur = 0;
+        unsigned long long key = 0ull;
+        if (act) {
+          cur = W.ref[base + lane];
+          key = W.key[base + lane];
+        }
+        __syncwarp();
+        sp = base;
+        bool h0 = false, h1 = false;
+        int c0 = 0, c1 = 0;
+        if (act && cur >= 0) {
+          const float4 n0 = __ldg(S.nodes + 4 * cur + 0);
+          const float4 n1 = __ldg(S.nodes + 4 * cur + 1);
+          const float4 n2 = __ldg(S.nodes + 4 * cur + 2);
+          const float4 n3 = __ldg(S.nodes + 4 * cur + 3);
+          float ta, tb;
+          h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ex, ey, ez, ix, iy, iz, len, ta);
+          h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ex, ey, ez, ix, iy, iz, len, tb);
+          c0 = __float_as_int(n3.x);
+          c1 = __float_as_int(n3.y);
+        }
+        const unsigned m0 = __ballot_sync(FULL, h0), m1 = __ballot_sync(FULL, h1);
+        const uint32_t tot = (uint32_t)(__popc(m0) + __popc(m1));
+        if (sp + tot > kWarpStack) {
+          fail |= 1u;
+          break;
+        }
+        const uint32_t d = (uint32_t)(key & 63ull);
+        const unsigned long long child = (key & ~63ull) | (unsigned long long)(d < 63u ? d + 1u : 63u);
+        const unsigned long long abit = d < 58u ? (1ull << (63u - d)) : 0ull;
+        const uint32_t pos = sp + (uint32_t)(__popc(m0 & lt) + __popc(m1 & lt));
+        if (h0) {
+          W.ref[pos] = c0;
+          W.key[pos] = child | abit;
+        }
+        if (h1) {
+          W.ref[pos + (h0 ? 1u : 0u)] = c1;
+          W.key[pos + (h0 ? 1u : 0u)] = child;
+        }
+        sp += tot;
+        if (act && cur < 0) {
+          const uint32_t code = ~(uint32_t)cur;
+          const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
+          for (uint32_t i = start; i < end; i++) {
+            const float4 p0 = __ldg(S.prims + 3 * i + 0);
+            const float4 p1 = __ldg(S.prims + 3 * i + 1);
+            const float4 p2 = __ldg(S.prims + 3 * i + 2);
+            float t;
+            if (ray_tri(p0, p1, p2, ex, ey, ez, sx, sy, sz, t)) {
+              const float tt = t / len;
+              if (tt > 1e-4f && tt < 1.0f - 1e-4f) {
+                const uint32_t k = atomicAdd(&W.n, 1u);
+                if (k < kMaxCross) {
+                  W.t[k] = tt;
+                  W.prim[k] = i;
+                  W.ckey[k] = key;
+                }
+              }
+            }
+          }
+        }
+        __syncwarp();
+      }
+      __syncwarp();
+      n = W.n;
+      if (n > kMaxCross) fail |= 2u;
+    }
+  }
+  if (fail) {
+    if (lane == 0) atomicOr(&L.hdr->error, fail);
 #pragma unroll
     for (int b = 0; b < MAXB; b++) tp[b] = 0.0f;
     return;
   }
-  for (uint32_t h = 0; h < nh; h++) {
-    const DMat& M = S.mats[hits[h].mat];
-#pragma unroll
-    for (int b = 0; b < MAXB; b++)
-      if ((uint32_t)b < nb) tp[b] = tp[b] * M.t2[b];
-    if (tp[0] < 1e-7f) {
-#pragma unroll
-      for (int b = 0; b < MAXB; b++) tp[b] = 0.0f;
-      return;
+  // rank sort by (t, depth-first key, primitive): every key is distinct
+  for (uint32_t e = lane; e < n; e += 32u) {
+    const float te = W.t[e];
+    const unsigned long long ke = W.ckey[e];
+    const uint32_t pe = W.prim[e];
+    uint32_t r = 0;
+    for (uint32_t q = 0; q < n; q++) {
+      const float tq = W.t[q];
+      const unsigned long long kq = W.ckey[q];
+      if (tq < te || (tq == te && (kq < ke || (kq == ke && W.prim[q] < pe)))) r++;
     }
+    W.st[r] = te;
+    W.sprim[r] = pe;
+  }
+  __syncwarp();
+  // same-t merge (lowest surface id wins, the cluster keeps its first t),
+  // then the mass-law product in crossing order
+  const float tol = 1e-4f / fmaxf(len, 1.0f);
+  bool open = false;
+  float anchor = 0.0f;
+  uint32_t wtri = 0, wmat = 0;
+  bool dead = false;
+  for (uint32_t q = 0; q <= n && !dead; q++) {
+    uint32_t tri = 0, mat = 0;
+    float tq = 0.0f;
+    const bool last = q == n;
+    if (!last) {
+      const uint32_t pq = W.sprim[q];
+      tq = W.st[q];
+      mat = __float_as_uint(__ldg(S.prims + 3 * pq + 0).w);
+      tri = __float_as_uint(__ldg(S.prims + 3 * pq + 1).w);
+      if (open && fabsf(tq - anchor) < tol) {
+        if (S.tri_surface[tri] < S.tri_surface[wtri]) {
+          wtri = tri;
+          wmat = mat;
+        }
+        continue;
+      }
+    }
+    if (open) {
+      const DMat& M = S.mats[wmat];
+#pragma unroll
+      for (int b = 0; b < MAXB; b++)
+        if ((uint32_t)b < nb) tp[b] = tp[b] * M.t2[b];
+      if (tp[0] < 1e-7f) dead = true;
+    }
+    anchor = tq;
+    wtri = tri;
+    wmat = mat;
+    open = true;
+  }
+  if (dead) {
+#pragma unroll
+    for (int b = 0; b < MAXB; b++) tp[b] = 0.0f;
+    return;
   }
   for (uint32_t k = 0; k < L.n_panels; k++) {
     float t;
@@ -223,8 +305,11 @@ __device__ void trace_through(const DScene& S, const DDomeLaunch& L, float ex, f
   }
 }
 
+// The specular escape of every (listener, fan ray), one thread each: its
+// transmission goes to ray_tp and its escape flag to ray_escape; the
+// straight-through kernel then completes the rays that need it.
 template <bool TIE>
-__global__ void dome_rays_kernel(DDomeLaunch L) {
+__global__ void dome_escape_kernel(DDomeLaunch L) {
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= L.n_eyes * L.n_rays) return;
   const uint32_t eye = gid / L.n_rays, j = gid % L.n_rays;
@@ -232,55 +317,91 @@ __global__ void dome_rays_kernel(DDomeLaunch L) {
   const uint32_t i = (uint32_t)((uint64_t)j * L.n_fan / L.n_rays);  // dome.rs:434
   const float4 f = L.fan[i];
   const float ex = L.eyes[3 * eye], ey = L.eyes[3 * eye + 1], ez = L.eyes[3 * eye + 2];
-  float bp[MAXB], tp[MAXB];
-  uint32_t events = 0, through = 0;
+  float bp[MAXB];
+  uint32_t events = 0;
   const bool esc = trace_escape<TIE>(S, L, ex, ey, ez, f.x, f.y, f.z, bp, events);
-  if (esc && bp[0] > 0.5f) {
-#pragma unroll
-    for (int b = 0; b < MAXB; b++) tp[b] = bp[b];
-  } else {
-    through = 1;
-    trace_through(S, L, ex, ey, ez, f.x, f.y, f.z, tp);
-    if (esc) {
-#pragma unroll
-      for (int b = 0; b < MAXB; b++) tp[b] = fmaxf(tp[b], bp[b]);
-    }
-  }
   float* o = L.ray_tp + (uint64_t)gid * L.nb;
-  for (uint32_t b = 0; b < L.nb; b++) o[b] = tp[b];
+  for (uint32_t b = 0; b < L.nb; b++) o[b] = bp[b];
   L.ray_escape[gid] = esc ? 1 : 0;
   atomicAdd(&L.events[0], events);
-  if (through) atomicAdd(&L.events[1], through);
 }
 
-// dome.rs:452-477 per listener: bins in fan order, EMA, directions.
-__global__ void dome_bins_kernel(DDomeLaunch L, float ema_alpha) {
+// dome.rs:432-446 per ray: a near-full escape stands; otherwise the
+// straight-through seep, combined with an escape by the per-band max. One
+// warp per ray.
+__global__ void __launch_bounds__(32 * kThroughWarps) dome_through_kernel(DDomeLaunch L) {
+  __shared__ ThroughSmem smem[kThroughWarps];
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  const uint64_t gid = (uint64_t)blockIdx.x * kThroughWarps + wib;
+  if (gid >= (uint64_t)L.n_eyes * L.n_rays) return;   // warp-uniform
+  const uint32_t nb = L.nb;
+  float* o = L.ray_tp + gid * nb;
+  const bool esc = L.ray_escape[gid] != 0;
+  float bp[MAXB];
+#pragma unroll
+  for (int b = 0; b < MAXB; b++) bp[b] = (uint32_t)b < nb ? o[b] : 0.0f;
+  if (esc && bp[0] > 0.5f) return;
+  const uint32_t eye = (uint32_t)(gid / L.n_rays), j = (uint32_t)(gid % L.n_rays);
+  const uint32_t i = (uint32_t)((uint64_t)j * L.n_fan / L.n_rays);
+  const float4 f = L.fan[i];
+  const float ex = L.eyes[3 * eye], ey = L.eyes[3 * eye + 1], ez = L.eyes[3 * eye + 2];
+  float tp[MAXB];
+  through_warp(*L.scene, L, smem[wib], lane, ex, ey, ez, f.x, f.y, f.z, tp);
+  if (esc) {
+#pragma unroll
+    for (int b = 0; b < MAXB; b++) tp[b] = fmaxf(tp[b], bp[b]);
+  }
+  __syncwarp();
+  if (lane == 0) {
+    for (uint32_t b = 0; b < nb; b++) o[b] = tp[b];
+    atomicAdd(&L.events[1], 1u);
+  }
+}
+
+// dome.rs:452-477 per listener: bins in fan order, EMA, directions. The
+// block stages the listener's rays (fan direction with its bin, transmission)
+// in shared memory, kDomeChunk at a time; thread k < 9 then sums bin k over
+// them in fan order (the same f32 sums in the same order as one loop).
+constexpr uint32_t kDomeChunk = 256;
+constexpr uint32_t kDomeBinThreads = 128;
+__global__ void __launch_bounds__(kDomeBinThreads) dome_bins_kernel(DDomeLaunch L, float ema_alpha) {
+  __shared__ float4 s_fan[kDomeChunk];
+  __shared__ float s_tp[kDomeChunk * MAXB];
   const uint32_t eye = blockIdx.x;
-  const uint32_t k = threadIdx.x;  // bin 0..8; lanes 9..31 only join the warp sync
+  const uint32_t k = threadIdx.x;  // bin 0..8; the other threads only stage
   const uint32_t nb = L.nb;
   const bool primed = L.primed[eye] != 0u;
-  __syncwarp();
-  if (k < 9) {
-    float e[MAXB];
+  float e[MAXB];
 #pragma unroll
-    for (int b = 0; b < MAXB; b++) e[b] = 0.0f;
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    const float nr = (float)L.n_rays;
-    for (uint32_t j = 0; j < L.n_rays; j++) {
-      const uint32_t i = (uint32_t)((uint64_t)j * L.n_fan / L.n_rays);
-      const float4 f = L.fan[i];
-      if ((uint32_t)__float_as_int(f.w) != k) continue;
-      const float* tp = L.ray_tp + ((uint64_t)eye * L.n_rays + j) * nb;
-      if (tp[0] > 1e-9f) {
+  for (int b = 0; b < MAXB; b++) e[b] = 0.0f;
+  float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+  const float nr = (float)L.n_rays;
+  const float* tp_eye = L.ray_tp + (uint64_t)eye * L.n_rays * nb;
+  for (uint32_t j0 = 0; j0 < L.n_rays; j0 += kDomeChunk) {
+    const uint32_t m = L.n_rays - j0 < kDomeChunk ? L.n_rays - j0 : kDomeChunk;
+    for (uint32_t q = threadIdx.x; q < m; q += blockDim.x)
+      s_fan[q] = L.fan[(uint32_t)((uint64_t)(j0 + q) * L.n_fan / L.n_rays)];
+    for (uint32_t q = threadIdx.x; q < m * nb; q += blockDim.x) s_tp[q] = tp_eye[(uint64_t)j0 * nb + q];
+    __syncthreads();
+    if (k < 9) {
+      for (uint32_t q = 0; q < m; q++) {
+        const float4 f = s_fan[q];
+        if ((uint32_t)__float_as_int(f.w) != k) continue;
+        const float* tp = s_tp + q * nb;
+        if (tp[0] > 1e-9f) {
 #pragma unroll
-        for (int b = 0; b < MAXB; b++)
-          if ((uint32_t)b < nb) e[b] = e[b] + tp[b] / nr;
-        const float w = fmaxf(tp[1], tp[0] * 0.2f);
-        sx = sx + f.x * w;
-        sy = sy + f.y * w;
-        sz = sz + f.z * w;
+          for (int b = 0; b < MAXB; b++)
+            if ((uint32_t)b < nb) e[b] = e[b] + tp[b] / nr;
+          const float w = fmaxf(tp[1], tp[0] * 0.2f);
+          sx = sx + f.x * w;
+          sy = sy + f.y * w;
+          sz = sz + f.z * w;
+        }
       }
     }
+    __syncthreads();
+  }
+  if (k < 9) {
     const float alpha = primed ? ema_alpha : 1.0f;
     float* ema = L.ema + ((uint64_t)eye * 9 + k) * nb;
     for (uint32_t b = 0; b < nb; b++) {
@@ -296,16 +417,16 @@ __global__ void dome_bins_kernel(DDomeLaunch L, float ema_alpha) {
       dxo = 0.0f; dyo = 0.0f; dzo = 1.0f;
     } else {
       const float az = ((float)k + 0.5f) * TAU_F / 8.0f - PI_F;
-      double s, c;
-      sincos((double)az, &s, &c);
-      dxo = (float)c; dyo = (float)s; dzo = 0.0f;
+      double sn, cs;
+      sincos((double)az, &sn, &cs);
+      dxo = (float)cs; dyo = (float)sn; dzo = 0.0f;
     }
     float* od = L.out_dir + ((uint64_t)eye * 9 + k) * 3;
     od[0] = dxo;
     od[1] = dyo;
     od[2] = dzo;
   }
-  __syncwarp();
+  __syncthreads();
   if (k == 0) L.primed[eye] = 1u;
 }
 
@@ -342,9 +463,10 @@ cudaError_t build_dome_fan(float4* fan, uint32_t n, cudaStream_t s) {
 cudaError_t launch_dome(const DDomeLaunch& L, cudaStream_t s) {
   const uint64_t total = (uint64_t)L.n_eyes * L.n_rays;
   if (total == 0) return cudaSuccess;
-  if (L.tie) dome_rays_kernel<true><<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);
-  else dome_rays_kernel<false><<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);
-  dome_bins_kernel<<<L.n_eyes, 32, 0, s>>>(L, 0.35f);
+  if (L.tie) dome_escape_kernel<true><<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);
+  else dome_escape_kernel<false><<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);
+  dome_through_kernel<<<(uint32_t)((total + kThroughWarps - 1) / kThroughWarps), 32 * kThroughWarps, 0, s>>>(L);
+  dome_bins_kernel<<<L.n_eyes, kDomeBinThreads, 0, s>>>(L, 0.35f);
   return cudaGetLastError();
 }
 

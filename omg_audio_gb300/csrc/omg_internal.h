@@ -144,13 +144,14 @@ struct LaunchShape {
   uint32_t tail_mode = 0;       // the persistent kernel of epochs after the first
   uint32_t wide = 0;            // persistent walks on the 4-wide tree (near-tie rule only)
   // mode 2: the persistent kernel walks each ray with 4 lanes (one child of a
-  // 4-wide node each) and shades 32 rays at a time (near-tie rule, every
+  // 4-wide node each) and shades wl_shade_min rays at a time (near-tie rule, every
   // mesh scene of the batch host-built)
   uint32_t wf_iters = 0;        // wavefront rounds before the persistent kernel takes over (0: none)
   uint32_t wf_tail = 0;         // ... or as soon as at most this many rays are alive
   uint32_t epochs = 0;          // persistent-kernel epochs (0: one launch that never parks)
   uint32_t park_pct = 50;       // an epoch parks its rays once at most this % of them remain
   uint32_t park_min = 4096;     // epochs of at most this many rays run to the end
+  uint32_t wl_shade_min = 32;   // modes 1 and 2: rays a warp shades together once that many wait
 };
 
 // Wavefront state (wavefront.cu). One record per ray of the batch, indexed by

@@ -437,10 +437,12 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
 // The tracer as a wavefront inside each warp. A lane walks one ray at a time;
 // when its walk ends, the ray id goes to the warp's shading queue and the lane
 // takes the next ray to walk from the warp's walk queue (or the global ray
-// queue). Once 32 rays wait in the shading queue (or nothing is left to walk)
-// the whole warp shades them together, from their saved state, and the
-// survivors join the walk queue. Walks thus refill lane by lane, and the long
-// shading code always runs with full warps. A warp owns at most 63 rays
+// queue). Once shade_min rays wait in the shading queue (32 by default; or
+// nothing is left to walk) the whole warp shades up to 32 of them together,
+// from their saved state, and the survivors join the walk queue. Walks thus
+// refill lane by lane, and the long shading code runs with full warps (a
+// smaller shade_min trades that for shorter waits when few rays are left). A
+// warp owns at most 63 rays
 // between two fetches from the ray queue (fetching only once its walk queue
 // is empty, with at most 31 waiting for shading and 32 walking), so each
 // queue holds 64 ids.
@@ -455,7 +457,7 @@ __global__ void __launch_bounds__(256, 4) trace_wl_kernel(const DJob* __restrict
                                                           const DPanelGroup* __restrict__ groups,
                                                           float* __restrict__ acc, DLaunch* __restrict__ hdr,
                                                           uint32_t* __restrict__ job_segments, int walk_budget,
-                                                          bool wide, EpochArgs ea) {
+                                                          uint32_t shade_min, bool wide, EpochArgs ea) {
   constexpr unsigned FULL = 0xffffffffu;
   constexpr uint32_t kNone = 0xFFFFFFFFu;
   constexpr uint32_t kQ = 64;
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(256, 4) trace_wl_kernel(const DJob* __restrict
     unsigned walking = __ballot_sync(FULL, rid != kNone);
 
     // ---- shading pass: a full warp of rays, or whatever waits once nothing can walk
-    if (sh_cnt >= 32u || (sh_cnt && !walking && !wk_cnt && (exhausted || parking))) {
+    if (sh_cnt >= shade_min || (sh_cnt && !walking && !wk_cnt && (exhausted || parking))) {
       const uint32_t m = sh_cnt < 32u ? sh_cnt : 32u;
       bool alive = false, ended = false;
       uint32_t r = kNone;
@@ -667,11 +669,12 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
   const uint32_t shade_min = shape.shade_min == 0 ? 1u : (shape.shade_min > 32 ? 32u : shape.shade_min);
   // the warp-local wavefront needs the per-ray records and at most 8 warps a block
   const bool wl = shape.mode == 1 && ea.st.pos && threads <= 256;
+  const uint32_t wl_shade = shape.wl_shade_min == 0 ? 32u : (shape.wl_shade_min > 32 ? 32u : shape.wl_shade_min);
   const bool wide = shape.wide != 0;
 #define OMG_TRACE_LAUNCH(NB, TIE)                                                                         \
   if (wl)                                                                                                      \
     trace_wl_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels,    \
-                                                        groups, acc, hdr, job_segments, steps, wide, ea);            \
+                                                        groups, acc, hdr, job_segments, steps, wl_shade, wide, ea);  \
   else                                                                                                         \
     trace_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, groups, \
                                                      acc, hdr, job_segments, refill, steps, shade_min, wide, ea)

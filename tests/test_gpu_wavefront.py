@@ -42,10 +42,14 @@ SHAPES = [dict(mode=0, wf_rounds=0, wf_tail=0, epochs=0),
           dict(mode=2, wf_rounds=0, wf_tail=0, epochs=0, walk_steps=3),
           dict(mode=2, wf_rounds=0, wf_tail=0, epochs=6, park_pct=50, walk_steps=0),
           dict(mode=2, wf_rounds=4, wf_tail=0, epochs=3, park_pct=60, walk_steps=8),
-          dict(mode=0, tail_mode=2, wf_rounds=0, wf_tail=0, epochs=2, park_pct=30, walk_steps=0)]
+          dict(mode=0, tail_mode=2, wf_rounds=0, wf_tail=0, epochs=2, park_pct=30, walk_steps=0),
+          dict(mode=0, tail_mode=2, wf_rounds=0, wf_tail=0, epochs=2, park_pct=30, walk_steps=0, wl_shade_min=1),
+          dict(mode=1, wf_rounds=0, wf_tail=0, epochs=3, park_pct=50, walk_steps=0, wl_shade_min=4),
+          dict(mode=2, wf_rounds=0, wf_tail=0, epochs=0, walk_steps=0, wl_shade_min=8)]
 for _s in SHAPES:
     _s.setdefault("wide", 0)
     _s.setdefault("tail_mode", _s["mode"])
+    _s.setdefault("wl_shade_min", 32)
 
 
 def _launches(shape):
