@@ -344,6 +344,48 @@ int32_t omg_dome_collect(omg_ctx* ctx, uint32_t probe_id, omg_dome_bin* out, flo
  * trace_through calls (dome.rs:390-422), summed over listeners. */
 int32_t omg_dome_segments(omg_ctx* ctx, uint32_t probe_id, uint64_t* escape_events, uint64_t* through_calls);
 
+/* -------------------------------------------------------------- late field */
+/* The consumer side of the seam (Sim::reverb_world / reverb_only,
+ * sim.rs:330-398) for many sim instances at once. Each slot keeps its
+ * averaged echogram (Sim::echo_avg) in device memory. A tick traces the
+ * slots the caller's gates fired for in ONE batched launch; then, on the
+ * device, each traced slot's echogram is blended in (Echogram::ema,
+ * tracer.rs:46-57, with the caller's weight) and its
+ * reverb (estimate_reverb) and late direction (late_direction,
+ * tracer.rs:59-77, from dir_from_s on, energy of the context's dir_band) are
+ * computed. Only the slot states travel back. The trace gate, the per-tick
+ * budget and the staleness compensation (sim.rs:38-75, 364-395) stay with the
+ * caller, which knows the poses.
+ * Slots share the context's n_bins and n_bands; a submitted job must use
+ * them. One tick is in flight per field: submit returns OMG_PENDING while the
+ * previous tick has not been polled to completion. */
+typedef struct omg_late_state {
+    float rt60[OMG_MAX_BANDS];   /* estimate_reverb of the averaged echogram */
+    float level[OMG_MAX_BANDS];
+    float dir[3];                /* unit direction of the late arrivals (1,0,0 when none) */
+    float anisotropy;            /* 0 diffuse .. 1 all from one direction */
+    uint32_t version;            /* updates blended in so far (0: never traced) */
+    uint32_t updated_tick;       /* the tick of the last update */
+} omg_late_state;
+int32_t omg_late_create(omg_ctx* ctx, uint32_t n_slots, float dir_from_s, uint32_t* field_id);
+int32_t omg_late_destroy(omg_ctx* ctx, uint32_t field_id);
+/* Enqueue one tick on the context stream: trace jobs[i] for slot slots[i]
+ * (distinct slots), then blend each into its slot with weight alpha[i]
+ * (NULL: 1 on the slot's first update, 0.3 after). Returns at once; *tick
+ * numbers the tick (1, 2, ...). n_jobs = 0 enqueues only the state read-back. */
+int32_t omg_late_submit(omg_ctx* ctx, uint32_t field_id, const uint32_t* slots, const omg_job* jobs,
+                        const float* alpha, uint32_t n_jobs, const omg_panel* panels, uint32_t n_panels,
+                        uint32_t* tick);
+/* OMG_PENDING until the last submitted tick is done; then every slot's state
+ * (n_slots records) and that tick's number. Without a tick in flight: the
+ * last states. */
+int32_t omg_late_poll(omg_ctx* ctx, uint32_t field_id, omg_late_state* states, uint32_t* tick);
+/* Forget a slot's history (a new sim instance in it): its next update
+ * replaces the echogram (alpha 1). Not while a tick is in flight. */
+int32_t omg_late_reset(omg_ctx* ctx, uint32_t field_id, uint32_t slot);
+/* A slot's averaged echogram (n_bins x n_bands, n_bins x 3). Not while a tick is in flight. */
+int32_t omg_late_read(omg_ctx* ctx, uint32_t field_id, uint32_t slot, float* bins, float* dirs);
+
 /* --------------------------------------------------------------- surrogate */
 /* No counterpart in the reference: the learned surrogate of the tracer. An
  * ensemble of `members` MLPs n_in -> hidden (x n_hidden, GELU) -> n_out,

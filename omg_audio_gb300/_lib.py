@@ -58,6 +58,11 @@ class omg_reverb(C.Structure):
     _fields_ = [("rt60", F8), ("level", F8), ("rt60_fit", F8), ("segments", C.c_uint64)]
 
 
+class omg_late_state(C.Structure):
+    _fields_ = [("rt60", F8), ("level", F8), ("dir", C.c_float * 3), ("anisotropy", C.c_float),
+                ("version", C.c_uint32), ("updated_tick", C.c_uint32)]
+
+
 class omg_dome_panel(C.Structure):
     _fields_ = [("axis", C.c_int32), ("plane", C.c_float), ("lat0", C.c_float), ("lat1", C.c_float),
                 ("z0", C.c_float), ("z1", C.c_float), ("glass", C.c_int32), ("trans", F8)]
@@ -138,6 +143,12 @@ SIGNATURES = {
     "omg_dome_submit": (I32, [P, U32, C.c_void_p, U32, C.c_void_p, U32, U32, U32, U32, C.c_void_p]),
     "omg_dome_collect": (I32, [P, U32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "omg_dome_segments": (I32, [P, U32, PU64, PU64]),
+    "omg_late_create": (I32, [P, U32, F, PU32]),
+    "omg_late_destroy": (I32, [P, U32]),
+    "omg_late_submit": (I32, [P, U32, P, P, P, U32, P, U32, PU32]),
+    "omg_late_poll": (I32, [P, U32, P, PU32]),
+    "omg_late_reset": (I32, [P, U32, U32]),
+    "omg_late_read": (I32, [P, U32, U32, P, P]),
     "omg_mlp_create": (I32, [P, C.POINTER(omg_mlp_config), PU32]),
     "omg_mlp_destroy": (I32, [P, U32]),
     "omg_mlp_set_data": (I32, [P, U32, P, P, U32]),

@@ -428,6 +428,39 @@ int32_t run_io(omg_ctx* ctx, BatchRec& B, float* bins, float* dirs, omg_reverb* 
   return OMG_OK;
 }
 
+// New per-job values into a batch whose job layout is unchanged: the job
+// array is refilled (it travels with each launch), materials and panels are
+// re-uploaded only when they differ, graphs are rebuilt on a shape change.
+int32_t refill_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                     uint32_t n_panels) {
+  std::vector<DMat> old_mats = B.job_mats;
+  std::vector<DPanel> old_panels = B.panels;
+  int32_t rc = fill_batch(ctx, B, jobs, n_jobs, panels, n_panels);
+  if (rc) return rc;
+  // materials and panels change rarely: re-upload only when they differ
+  bool mats_same = old_mats.size() == B.job_mats.size() &&
+                   std::memcmp(old_mats.data(), B.job_mats.data(), old_mats.size() * sizeof(DMat)) == 0;
+  bool pan_same = old_panels.size() == B.panels.size() &&
+                  std::memcmp(old_panels.data(), B.panels.data(), old_panels.size() * sizeof(DPanel)) == 0;
+  if (!mats_same && !B.job_mats.empty()) ctx->last_h2d += B.job_mats.size() * sizeof(DMat);
+  if (!pan_same && !B.panels.empty()) ctx->last_h2d += B.panels.size() * sizeof(DPanel);
+  if (!mats_same && !B.job_mats.empty())
+    CK(cudaMemcpyAsync(B.d_job_mats.p, B.job_mats.data(), B.job_mats.size() * sizeof(DMat),
+                       cudaMemcpyHostToDevice, ctx->stream));
+  if (!pan_same && !B.panels.empty()) {
+    CK(cudaMemcpyAsync(B.d_panels.p, B.panels.data(), B.panels.size() * sizeof(DPanel), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(B.d_groups.p, B.groups.data(), B.groups.size() * sizeof(DPanelGroup),
+                       cudaMemcpyHostToDevice, ctx->stream));
+  }
+  // the context's launch shape changed since the graphs were recorded
+  if (std::memcmp(&B.shape, &ctx->shape, sizeof(LaunchShape)) != 0) {
+    B.shape = ctx->shape;
+    if ((rc = build_graphs(ctx, B))) return rc;
+  }
+  return OMG_OK;
+}
+
 // Synchronous one-shot through the context's cached batch (rebuilt only when
 // the job layout changes; per-call values travel in the job array).
 int32_t one_shot(omg_ctx* ctx, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels, uint32_t n_panels,
@@ -442,33 +475,8 @@ int32_t one_shot(omg_ctx* ctx, const omg_job* jobs, uint32_t n_jobs, const omg_p
       return rc;
     }
   } else {
-    BatchRec& B = *ctx->cached;
-    std::vector<DMat> old_mats = B.job_mats;
-    std::vector<DPanel> old_panels = B.panels;
-    std::vector<DPanelGroup> old_groups = B.groups;
-    int32_t rc = fill_batch(ctx, B, jobs, n_jobs, panels, n_panels);
+    int32_t rc = refill_batch(ctx, *ctx->cached, jobs, n_jobs, panels, n_panels);
     if (rc) return rc;
-    // materials and panels change rarely: re-upload only when they differ
-    bool mats_same = old_mats.size() == B.job_mats.size() &&
-                     std::memcmp(old_mats.data(), B.job_mats.data(), old_mats.size() * sizeof(DMat)) == 0;
-    bool pan_same = old_panels.size() == B.panels.size() &&
-                    std::memcmp(old_panels.data(), B.panels.data(), old_panels.size() * sizeof(DPanel)) == 0;
-    if (!mats_same && !B.job_mats.empty()) ctx->last_h2d += B.job_mats.size() * sizeof(DMat);
-    if (!pan_same && !B.panels.empty()) ctx->last_h2d += B.panels.size() * sizeof(DPanel);
-    if (!mats_same && !B.job_mats.empty())
-      CK(cudaMemcpyAsync(B.d_job_mats.p, B.job_mats.data(), B.job_mats.size() * sizeof(DMat),
-                         cudaMemcpyHostToDevice, ctx->stream));
-    if (!pan_same && !B.panels.empty()) {
-      CK(cudaMemcpyAsync(B.d_panels.p, B.panels.data(), B.panels.size() * sizeof(DPanel), cudaMemcpyHostToDevice,
-                         ctx->stream));
-      CK(cudaMemcpyAsync(B.d_groups.p, B.groups.data(), B.groups.size() * sizeof(DPanelGroup),
-                         cudaMemcpyHostToDevice, ctx->stream));
-    }
-    // the context's launch shape changed since the graphs were recorded
-    if (std::memcmp(&B.shape, &ctx->shape, sizeof(LaunchShape)) != 0) {
-      B.shape = ctx->shape;
-      if ((rc = build_graphs(ctx, B))) return rc;
-    }
   }
   return run_io(ctx, *ctx->cached, bins, dirs, reverb);
 }
@@ -488,6 +496,23 @@ void job_from_world(omg_job& j, uint32_t scene_id, const omg_world_job& w, uint3
 }
 
 }  // namespace
+
+namespace omg {
+
+int32_t batch_prepare(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                      uint32_t n_panels) {
+  return prepare_batch(ctx, B, jobs, n_jobs, panels, n_panels);
+}
+int32_t batch_refill(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                     uint32_t n_panels) {
+  return refill_batch(ctx, B, jobs, n_jobs, panels, n_panels);
+}
+uint64_t batch_layout(const omg_job* jobs, uint32_t n_jobs, uint32_t n_panels, const omg_params& P) {
+  return batch_signature(jobs, n_jobs, n_panels, P);
+}
+int32_t batch_flags(omg_ctx* ctx, const BatchRec& B) { return check_kernel_flags(ctx, B); }
+
+}  // namespace omg
 
 // ====================================================================== C ABI
 extern "C" {

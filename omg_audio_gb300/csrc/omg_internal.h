@@ -232,6 +232,19 @@ struct DReverbJob {
 };
 cudaError_t launch_reverb(const DReverbJob* rj, uint32_t n_jobs, uint32_t max_bins, const float* bins,
                           omg_reverb* out, const uint32_t* job_segments, cudaStream_t s);
+// late.cu: blend each traced slot's fresh echogram (a batch output at
+// fresh + fresh_off) into the slot's average, then its reverb (rj: the slots'
+// echograms in avg, one per update) and state.
+struct DLateUpdate {
+  uint32_t slot;
+  uint32_t tick;
+  uint64_t fresh_off;
+  float alpha;          // EMA weight of the fresh echogram
+  uint32_t pad;
+};
+cudaError_t launch_late_update(const DLateUpdate* up, uint32_t n_up, const float* fresh, float* avg,
+                               uint32_t* version, const DReverbJob* rj, omg_reverb* rev, omg_late_state* state,
+                               uint32_t n_bins, uint32_t nb, uint32_t from_bin, uint32_t dir_band, cudaStream_t s);
 // lbvh.cu: build the node array for prims already in device memory; reorders
 // prims into leaf order (prims_out) and returns the root ref.
 cudaError_t lbvh_build(const float4* prims_in, uint32_t n_prims, float4* prims_out, float4* nodes_out,

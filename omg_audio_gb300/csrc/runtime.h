@@ -133,6 +133,7 @@ struct Ticket {
 
 struct DomeRec;
 struct MlpRec;
+struct LateRec;
 
 }  // namespace omg
 
@@ -156,6 +157,8 @@ struct omg_ctx {
   uint32_t next_probe = 1;
   std::map<uint32_t, std::shared_ptr<omg::MlpRec>> mlps;   // surrogate networks
   uint32_t next_mlp = 1;
+  std::map<uint32_t, std::shared_ptr<omg::LateRec>> lates;  // late fields
+  uint32_t next_late = 1;
   // raycast query scratch
   omg::DevBuf<float> q_o, q_d, q_t;
   omg::DevBuf<uint32_t> q_tri;
@@ -174,6 +177,15 @@ int32_t fail(omg_ctx* ctx, cudaError_t e, const char* where);
 uint32_t timeout_of(const omg_ctx* ctx);
 int32_t wait_event(omg_ctx* ctx, cudaEvent_t ev, uint32_t timeout_ms);
 int32_t sync_scene_table(omg_ctx* ctx);
+// api.cpp: a batch record for `jobs` (allocations, uploads, launch graphs);
+// the same record refilled with new per-job values when the job layout
+// (batch_layout) is unchanged; the kernels' error flags of its last read-back.
+int32_t batch_prepare(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                      uint32_t n_panels);
+int32_t batch_refill(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jobs, const omg_panel* panels,
+                     uint32_t n_panels);
+uint64_t batch_layout(const omg_job* jobs, uint32_t n_jobs, uint32_t n_panels, const omg_params& P);
+int32_t batch_flags(omg_ctx* ctx, const BatchRec& B);
 constexpr uint32_t kMaxScenes = 4096;     // scene ids 1 .. kMaxScenes-1
 bool valid_material(const omg_material& m, uint32_t nb);
 bool finite3(const float* v);

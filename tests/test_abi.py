@@ -48,6 +48,7 @@ def test_struct_sizes_match_the_header(built_lib):
     assert C.sizeof(_lib.omg_material) == 68
     assert C.sizeof(_lib.omg_panel) == 24 + 68
     assert C.sizeof(_lib.omg_reverb) == 3 * 32 + 8
+    assert C.sizeof(_lib.omg_late_state) == 2 * 32 + 16 + 8
 
 
 def test_mesh_builder_matches_oracle_on_cpu(built_lib, oracle):
