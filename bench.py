@@ -256,7 +256,7 @@ def run_workload(args):
     B.build()
     from omg_audio_gb300 import Context, DomeProbe, Job, MeshBuilder, TraceConfig, _lib
     from omg_audio_gb300 import workloads as W
-    bvh = _lib.BVH_LBVH if args.bvh == "lbvh" else _lib.BVH_SAH
+    bvh = {"sah": _lib.BVH_SAH, "lbvh": _lib.BVH_LBVH, "sah3": _lib.BVH_SAH3}[args.bvh]
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -409,7 +409,7 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
     mb = MeshBuilder()
     case.recorder.replay(mb)
-    bvh = _lib.BVH_LBVH if args.bvh == "lbvh" else _lib.BVH_SAH
+    bvh = {"sah": _lib.BVH_SAH, "lbvh": _lib.BVH_LBVH, "sah3": _lib.BVH_SAH3}[args.bvh]
     scene = ctx.upload_builder(mb, 3, bvh)
     jobs = [Job(src, lis, N_RAYS, seed=1000 + p, scene=scene, panel_offset=0, n_panels=len(case.panels))
             for p, (src, lis) in enumerate(case.pairs[:args.pairs])]
@@ -546,7 +546,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--bvh", choices=["sah", "lbvh"], default="sah")
+    ap.add_argument("--bvh", choices=["sah", "lbvh", "sah3"], default=None,
+                    help="sah: the reference's tree; sah3: three-axis binned SAH (default); lbvh: built on the "
+                         "GPU (the city's default: the host builds of its 1.9 M primitives take seconds)")
     ap.add_argument("--ref-pairs", type=int, default=64)
     ap.add_argument("--pairs", type=int, default=N_PAIRS, help="pairs traced per step (default: the workload's 64)")
     ap.add_argument("--profile", action="store_true", help="launches only (a small case under a profiler)")
@@ -565,6 +567,8 @@ def main():
                     help="multiroom: the headline (default); rooms256 and city print their own line")
     ap.add_argument("--city-rays", type=int, default=1 << 20, help="rays per source of the city workload")
     args = ap.parse_args()
+    if args.bvh is None:
+        args.bvh = "lbvh" if args.workload == "city" else "sah3"
     if args.impl == "reference":
         return run_reference(args)
     if args.workload != "multiroom":

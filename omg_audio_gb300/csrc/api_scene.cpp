@@ -45,7 +45,7 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
                           const uint16_t* tri_mat, const float* tri_max_edge, const uint16_t* tri_surf,
                           const omg_material* mats, uint32_t nm, uint32_t nb, uint32_t kind, uint32_t* scene_id) {
   if (!ctx || !scene_id || nb == 0 || nb > (uint32_t)MAXB || (nt && (!pos || !idx || !tri_mat)) || (nm && !mats) ||
-      (kind != OMG_BVH_SAH && kind != OMG_BVH_LBVH))
+      (kind != OMG_BVH_SAH && kind != OMG_BVH_LBVH && kind != OMG_BVH_SAH3))
     return OMG_E_INVALID;
   for (uint32_t t = 0; t < nt; t++) {
     if (tri_mat[t] >= nm) return OMG_E_INVALID;
@@ -72,8 +72,11 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
   std::vector<uint16_t> tsurf(nt, 0);
   if (tri_surf) tsurf.assign(tri_surf, tri_surf + nt);
 
-  if (kind == OMG_BVH_SAH) {
-    build_sah(S->prim_geo, S->prim_tri, S->prim_mat, S->ref_boxes, S->ref_ab);
+  if (kind == OMG_BVH_SAH || kind == OMG_BVH_SAH3) {
+    if (kind == OMG_BVH_SAH)
+      build_sah(S->prim_geo, S->prim_tri, S->prim_mat, S->ref_boxes, S->ref_ab);
+    else
+      build_sah3(S->prim_geo, S->prim_tri, S->prim_mat, S->ref_boxes, S->ref_ab);
     std::vector<float> dev_nodes;
     S->root = flatten_bvh2(S->ref_boxes, S->ref_ab, dev_nodes);
     S->n_nodes = (uint32_t)(dev_nodes.size() / 16);
@@ -252,8 +255,8 @@ int32_t omg_scene_info(omg_ctx* ctx, uint32_t id, uint32_t* n_nodes, uint32_t* n
   auto it = ctx->scenes.find(id);
   if (it == ctx->scenes.end()) return OMG_E_NOT_FOUND;
   const SceneRec& S = *it->second;
-  // reference-form node count for SAH trees (leaves included), device node count otherwise
-  if (n_nodes) *n_nodes = S.bvh_kind == OMG_BVH_SAH ? (uint32_t)(S.ref_ab.size() / 2) : S.n_nodes;
+  // reference-form node count for host-built trees (leaves included), device node count otherwise
+  if (n_nodes) *n_nodes = S.bvh_kind != OMG_BVH_LBVH ? (uint32_t)(S.ref_ab.size() / 2) : S.n_nodes;
   if (n_prims) *n_prims = S.n_prims;
   if (n_tris) *n_tris = S.n_tris;
   return OMG_OK;
@@ -265,7 +268,7 @@ int32_t omg_scene_export_bvh(omg_ctx* ctx, uint32_t id, float* node_boxes, uint3
   auto it = ctx->scenes.find(id);
   if (it == ctx->scenes.end()) return OMG_E_NOT_FOUND;
   const SceneRec& S = *it->second;
-  if (S.bvh_kind == OMG_BVH_SAH) {
+  if (S.bvh_kind != OMG_BVH_LBVH) {
     if (node_boxes) std::memcpy(node_boxes, S.ref_boxes.data(), S.ref_boxes.size() * 4);
     if (node_ab) std::memcpy(node_ab, S.ref_ab.data(), S.ref_ab.size() * 4);
   } else if (node_boxes || node_ab) {

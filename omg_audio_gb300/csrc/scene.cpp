@@ -1,5 +1,6 @@
 // Host-side scene preparation: mesh builder with vertex dedup, tessellation of
-// oversized triangles, the reference's binned-SAH BVH, and flattening into the
+// oversized triangles, the reference's binned-SAH BVH (and a three-axis binned
+// SAH tree for near-tie walks), and flattening into the
 // device layout (child-box BVH2, 48-byte primitives, per-triangle normals).
 //
 // Compiled with -ffp-contract=off: every f32 result here (midpoints, edges,
@@ -11,6 +12,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <memory>
 
 namespace omg {
 
@@ -298,6 +300,185 @@ void build_sah(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, st
     ref_ab[2 * i] = r.a;
     ref_ab[2 * i + 1] = r.b;
   }
+}
+
+// Binned SAH over all three axes (128 bins per axis, primitives binned by the
+// centre of their box), leaves of at most 4 primitives. The reference bins
+// only the widest centroid axis in 16 bins; on the 40-room scene this tree
+// needs a third fewer node visits and a fifth fewer triangle tests per
+// closest-hit query. The closest hit under the near-tie rule does not depend
+// on the tree. Below depth 36 the split is the SAH one; deeper (degenerate
+// inputs only) it is the object median of the widest axis, so a path never
+// exceeds 36 + log2(n) < 64 nodes (the traversal stack depth).
+namespace {
+struct BinBox {
+  float lo[3], hi[3];
+  void clear() {
+    for (int k = 0; k < 3; k++) {
+      lo[k] = std::numeric_limits<float>::max();
+      hi[k] = -std::numeric_limits<float>::max();
+    }
+  }
+  void grow(const BinBox& o) {
+    for (int k = 0; k < 3; k++) {
+      lo[k] = std::fmin(lo[k], o.lo[k]);
+      hi[k] = std::fmax(hi[k], o.hi[k]);
+    }
+  }
+  float half_area() const {
+    float e[3];
+    for (int k = 0; k < 3; k++) e[k] = std::fmax(hi[k] - lo[k], 0.0f);
+    return e[0] * e[1] + e[1] * e[2] + e[2] * e[0];
+  }
+};
+
+struct SweepPrim {
+  BinBox b;
+  float c[3];
+  uint32_t id;
+};
+
+struct Sah3Builder {
+  static constexpr int kBins = 128;
+  static constexpr int kMedianDepth = 36;
+  std::vector<SweepPrim>& P;
+  std::vector<BinBox> boxes;
+  std::vector<uint32_t> ab;
+  BinBox bins[3][kBins];
+  uint32_t counts[3][kBins];
+  float right_cost[kBins];
+
+  explicit Sah3Builder(std::vector<SweepPrim>& p) : P(p) {}
+
+  uint32_t node(size_t s, size_t e, int depth) {
+    BinBox bb, cb;
+    bb.clear();
+    cb.clear();
+    for (size_t i = s; i < e; i++) {
+      bb.grow(P[i].b);
+      for (int k = 0; k < 3; k++) {
+        cb.lo[k] = std::fmin(cb.lo[k], P[i].c[k]);
+        cb.hi[k] = std::fmax(cb.hi[k], P[i].c[k]);
+      }
+    }
+    const uint32_t idx = (uint32_t)boxes.size();
+    boxes.push_back(bb);
+    ab.push_back(0);
+    ab.push_back(0);
+    const size_t n = e - s;
+    if (n <= kLeafSize) {
+      ab[2 * idx] = kLeafBit | (uint32_t)s;
+      ab[2 * idx + 1] = (uint32_t)n;
+      return idx;
+    }
+    int best_axis = -1, best_cut = -1;
+    if (depth < kMedianDepth) {
+      float best = std::numeric_limits<float>::max();
+      for (int a = 0; a < 3; a++) {
+        const float w = cb.hi[a] - cb.lo[a];
+        if (!(w > 1e-6f)) continue;
+        const float scale = (float)kBins / w;
+        for (int k = 0; k < kBins; k++) {
+          bins[a][k].clear();
+          counts[a][k] = 0;
+        }
+        for (size_t i = s; i < e; i++) {
+          const int k = std::min(kBins - 1, (int)((P[i].c[a] - cb.lo[a]) * scale));
+          bins[a][k].grow(P[i].b);
+          counts[a][k]++;
+        }
+        BinBox acc;
+        acc.clear();
+        uint32_t cnt = 0;
+        for (int k = kBins - 1; k >= 1; k--) {
+          acc.grow(bins[a][k]);
+          cnt += counts[a][k];
+          right_cost[k - 1] = cnt ? acc.half_area() * (float)cnt : 0.0f;
+        }
+        acc.clear();
+        cnt = 0;
+        for (int k = 0; k < kBins - 1; k++) {
+          acc.grow(bins[a][k]);
+          cnt += counts[a][k];
+          if (cnt == 0 || cnt == n) continue;
+          const float cost = acc.half_area() * (float)cnt + right_cost[k];
+          if (cost < best) {
+            best = cost;
+            best_axis = a;
+            best_cut = k;
+          }
+        }
+      }
+    }
+    size_t mid;
+    if (best_axis >= 0) {
+      const int a = best_axis;
+      const float scale = (float)kBins / (cb.hi[a] - cb.lo[a]), lo = cb.lo[a];
+      auto it = std::partition(P.begin() + s, P.begin() + e, [&](const SweepPrim& p) {
+        return std::min(kBins - 1, (int)((p.c[a] - lo) * scale)) <= best_cut;
+      });
+      mid = (size_t)(it - P.begin());
+    } else {
+      // object median of the widest centroid axis
+      int a = 0;
+      for (int k = 1; k < 3; k++)
+        if (cb.hi[k] - cb.lo[k] > cb.hi[a] - cb.lo[a]) a = k;
+      mid = s + n / 2;
+      std::nth_element(P.begin() + s, P.begin() + mid, P.begin() + e,
+                       [&](const SweepPrim& x, const SweepPrim& y) {
+                         return x.c[a] < y.c[a] || (x.c[a] == y.c[a] && x.id < y.id);
+                       });
+    }
+    if (mid <= s || mid >= e) mid = s + n / 2;
+    const uint32_t l = node(s, mid, depth + 1);
+    const uint32_t r = node(mid, e, depth + 1);
+    ab[2 * idx] = l;
+    ab[2 * idx + 1] = r;
+    return idx;
+  }
+};
+}  // namespace
+
+void build_sah3(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, std::vector<uint16_t>& prim_mat,
+                std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab) {
+  const size_t n = prim_tri.size();
+  ref_boxes.clear();
+  ref_ab.clear();
+  if (n == 0) return;
+  std::vector<SweepPrim> P(n);
+  for (size_t i = 0; i < n; i++) {
+    const float* g = &prim_geo[9 * i];
+    for (int k = 0; k < 3; k++) {
+      const float x0 = g[k], x1 = g[k] + g[3 + k], x2 = g[k] + g[6 + k];
+      P[i].b.lo[k] = std::fmin(std::fmin(x0, x1), x2);
+      P[i].b.hi[k] = std::fmax(std::fmax(x0, x1), x2);
+      P[i].c[k] = (P[i].b.lo[k] + P[i].b.hi[k]) * 0.5f;
+    }
+    P[i].id = (uint32_t)i;
+  }
+  std::unique_ptr<Sah3Builder> B(new Sah3Builder(P));
+  B->boxes.reserve(2 * n / kLeafSize + 8);
+  B->ab.reserve(4 * n / kLeafSize + 16);
+  B->node(0, n, 0);
+  std::vector<float> geo(prim_geo.size());
+  std::vector<uint32_t> tri(n);
+  std::vector<uint16_t> mat(n);
+  for (size_t i = 0; i < n; i++) {
+    std::memcpy(&geo[9 * i], &prim_geo[9 * (size_t)P[i].id], 9 * sizeof(float));
+    tri[i] = prim_tri[P[i].id];
+    mat[i] = prim_mat[P[i].id];
+  }
+  prim_geo.swap(geo);
+  prim_tri.swap(tri);
+  prim_mat.swap(mat);
+  ref_boxes.resize(B->boxes.size() * 6);
+  for (size_t i = 0; i < B->boxes.size(); i++) {
+    float* o = &ref_boxes[6 * i];
+    const BinBox& b = B->boxes[i];
+    o[0] = b.lo[0]; o[1] = b.lo[1]; o[2] = b.lo[2];
+    o[3] = b.hi[0]; o[4] = b.hi[1]; o[5] = b.hi[2];
+  }
+  ref_ab.swap(B->ab);
 }
 
 // Flatten the reference node array into the device BVH2: one device node per

@@ -47,6 +47,10 @@ void tessellate(const float* pos, const uint32_t* idx, uint32_t n_tris, const ui
                 std::vector<uint16_t>& prim_mat);
 void build_sah(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, std::vector<uint16_t>& prim_mat,
                std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab);
+// Binned SAH over all three axes (128 bins, leaves <= 4), same output form as
+// build_sah; for walks under the near-tie rule, whose hit is tree-independent.
+void build_sah3(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, std::vector<uint16_t>& prim_mat,
+                std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab);
 // Returns the root ref; dev_nodes gets 16 floats per internal node.
 int32_t flatten_bvh2(const std::vector<float>& ref_boxes, const std::vector<uint32_t>& ref_ab,
                      std::vector<float>& dev_nodes);

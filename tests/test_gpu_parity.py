@@ -102,7 +102,7 @@ def test_scene_builder_and_sah_tree_match_the_oracle(ctx, oracle):
 
 
 @pytest.mark.parametrize("tie", [0, 1], ids=["first-found", "surface-tie"])
-@pytest.mark.parametrize("bvh", [_lib.BVH_SAH, _lib.BVH_LBVH], ids=["sah", "lbvh"])
+@pytest.mark.parametrize("bvh", [_lib.BVH_SAH, _lib.BVH_LBVH, _lib.BVH_SAH3], ids=["sah", "lbvh", "sah3"])
 def test_closest_hit_tri_ids(ctx, ctx_tie, oracle, bvh, tie):
     """Mesh::raycast on segments logged from oracle traces of the 50k-primitive
     scene. tie 0 (the reference's rule): the GPU equals the f32 oracle (same t;

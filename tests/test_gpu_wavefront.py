@@ -13,10 +13,12 @@ wavefront, cooperative 4-lane walks) alone and in epochs, on the binary and
 the 4-wide tree, a hand-over after a few rounds, a hand-over at a live-ray
 threshold, and rounds to the last ray.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
-from omg_audio_gb300 import Context, Job, MeshBuilder, TraceConfig
+from omg_audio_gb300 import Context, Job, MeshBuilder, TraceConfig, _lib
 from omg_audio_gb300 import workloads as W
 
 from test_gpu_parity import gpu_scene, oparams, rel_bins
@@ -166,3 +168,24 @@ def test_autotuned_shape_keeps_the_result(mixed):
         assert rv.segments == segs
         assert rel_bins(e.bins, ob) <= 1e-5
     b.destroy()
+
+
+@pytest.mark.parametrize("shape", [SHAPES[0], SHAPES[8], SHAPES[13], SHAPES[14], SHAPES[18]],
+                         ids=["m0", "m1", "m1-wide", "m2", "m0-tail2"])
+def test_three_axis_sah_tree_keeps_the_result(mixed, shape):
+    """The same jobs over the three-axis binned-SAH tree (OMG_BVH_SAH3): under
+    the near-tie rule the closest hit does not depend on the tree, so segment
+    counts and histograms equal the oracle's as on the reference's tree."""
+    ctx, jobs, panels, ref = mixed
+    case = W.multiroom(seed=2)
+    big3 = gpu_scene(ctx, case.recorder, _lib.BVH_SAH3)
+    big = jobs[0].scene
+    jobs3 = [dataclasses.replace(j, scene=big3) if j.scene is big else j for j in jobs]
+    b = ctx.batch(jobs3, panels)
+    b.set_shape(**shape)
+    b.launch()
+    for k, ((e, rv), (ob, segs)) in enumerate(zip(b.read(), ref)):
+        assert rv.segments == segs, (k, rv.segments, segs)
+        assert rel_bins(e.bins, ob) <= 1e-5, k
+    b.destroy()
+    big3.release()
