@@ -389,6 +389,71 @@ int32_t omg_late_reset(omg_ctx* ctx, uint32_t field_id, uint32_t slot);
 /* A slot's averaged echogram (n_bins x n_bands, n_bins x 3). Not while a tick is in flight. */
 int32_t omg_late_read(omg_ctx* ctx, uint32_t field_id, uint32_t slot, float* bins, float* dirs);
 
+/* ------------------------------------------------------------- wire formats */
+/* The web bridge's flat trace jobs, as the wasm build queues them for its GPU
+ * driver and the driver reads them (crates/omg-web/src/lib.rs:150-202 and
+ * 365-416; web/gpu.js:181-199 packJob, 420-437 pumpWorldLate), traced here as
+ * ONE batch instead of one dispatch per job. Word values are converted as the
+ * driver's Uint32Array stores do (JavaScript ToUint32: truncate, modulo 2^32).
+ * Box job, 57 f32: [0] sim id, [1] n_rays, [2] seed, [3..6] room size,
+ *   [6..9] source, [9..12] listener, [12..15] band energy, [15..57] 6 walls
+ *   (x-,x+,y-,y+,z-,z+) x (absorption x3, scattering, transmission x3).
+ * World job, 1034 f32 (10 + 64 x 16): [0] sim id, [1] n_rays, [2] seed,
+ *   [3..6] source, [6..9] listener, [9] n_panels (<= 64), [10..] panels of
+ *   16 f32: min xyz, scattering, max xyz, 0, absorption xyz, 0,
+ *   transmission xyz, 0; unit band energy (gpu.js:434).
+ * echo: per job the injection record of lib.rs:158/204-218: n_bins x 3 bin
+ *   energies, then n_bins x 3 direction sums (1800 f32 at the reference's
+ *   300 bins). ids (nullable): the jobs' sim ids. reverb (nullable): one per job.
+ * The context must run 3 bands (the formats' NBANDS); n_floats must be a
+ * whole number of jobs. */
+#define OMG_WEB_BOX_JOB_F32S 57
+#define OMG_WEB_BOX_JOB_VERSION 2        /* lib.rs:158 GPU_JOB_VERSION */
+#define OMG_WEB_WORLD_MAX_PANELS 64
+#define OMG_WEB_WORLD_JOB_F32S (10 + OMG_WEB_WORLD_MAX_PANELS * 16)
+#define OMG_WEB_WORLD_JOB_VERSION 3      /* lib.rs:377 WLATE_VERSION */
+int32_t omg_trace_web_box_jobs(omg_ctx* ctx, const float* jobs, uint32_t n_floats, float* echo, uint32_t* ids,
+                               omg_reverb* reverb);
+int32_t omg_trace_web_world_jobs(omg_ctx* ctx, uint32_t scene_id, const float* jobs, uint32_t n_floats,
+                                 float* echo, uint32_t* ids, omg_reverb* reverb);
+
+/* The simulation -> renderer contract in its flat f32 form (ParamBlock,
+ * crates/omg-core/src/params.rs:57-141): [0] version, [1] n_taps,
+ * [2..8] reverb rt60[3], level[3], [8] remote flag, [9..24] remote rt60[3],
+ * send[3], sh[9], then 9 f32 per tap: key, delay_s, dir[3], gains[3], 0.
+ * Host-only (no device work). */
+#define OMG_PARAM_FLAT_HEADER 24
+#define OMG_PARAM_FLAT_PER_TAP 9
+typedef struct omg_tap {         /* params.rs:7-16 */
+    uint32_t key;
+    float delay_s;
+    float dir[3];
+    float gains[3];
+} omg_tap;
+typedef struct omg_param_block { /* params.rs:57-66, taps passed beside it */
+    uint64_t version;
+    float rt60[3];               /* ReverbParams (params.rs:18-29) */
+    float level[3];
+    int32_t has_remote;          /* RemoteReverb (params.rs:44-55) present */
+    float remote_rt60[3];
+    float remote_send[3];
+    float remote_sh[9];
+} omg_param_block;
+/* ParamBlock::flat_len (params.rs:75-77). */
+uint32_t omg_param_block_flat_len(uint32_t n_taps);
+/* ParamBlock::write_flat (params.rs:79-106): out_len >= flat_len(n_taps). */
+int32_t omg_param_block_write_flat(const omg_param_block* pb, const omg_tap* taps, uint32_t n_taps, float* out,
+                                   uint32_t out_len);
+/* ParamBlock::read_flat (params.rs:108-141). *n_taps gets the block's tap
+ * count; taps beyond max_taps, or a block longer than len, give OMG_E_INVALID
+ * (the reference panics on a short slice). */
+int32_t omg_param_block_read_flat(const float* data, uint32_t len, omg_param_block* pb, omg_tap* taps,
+                                  uint32_t max_taps, uint32_t* n_taps);
+/* The reverb part of n ParamBlocks from late-field slot states (bands 0..2 of
+ * rt60 and level, as Sim writes estimate_reverb into its block,
+ * sim.rs:364-398); version = the slot's update count; no remote field. */
+int32_t omg_param_block_from_late(const omg_late_state* states, uint32_t n, omg_param_block* out);
+
 /* --------------------------------------------------------------- surrogate */
 /* No counterpart in the reference: the learned surrogate of the tracer. An
  * ensemble of `members` MLPs n_in -> hidden (x n_hidden, GELU) -> n_out,

@@ -79,6 +79,15 @@ class omg_tune_result(C.Structure):
                 ("ms", C.c_float)]
 
 
+class omg_tap(C.Structure):
+    _fields_ = [("key", C.c_uint32), ("delay_s", C.c_float), ("dir", F3), ("gains", F3)]
+
+
+class omg_param_block(C.Structure):
+    _fields_ = [("version", C.c_uint64), ("rt60", F3), ("level", F3), ("has_remote", C.c_int32),
+                ("remote_rt60", F3), ("remote_send", F3), ("remote_sh", C.c_float * 9)]
+
+
 class omg_mlp_config(C.Structure):
     _fields_ = [("n_in", C.c_uint32), ("hidden", C.c_uint32), ("n_hidden", C.c_uint32), ("n_out", C.c_uint32),
                 ("members", C.c_uint32), ("seed", C.c_uint32)]
@@ -160,9 +169,19 @@ SIGNATURES = {
     "omg_mlp_set_params": (I32, [P, U32, U32, P, U64]),
     "omg_tc_gemm": (I32, [P, P, P, P, U32, U32, U32]),
     "omg_trace_box_noalloc": (I32, [C.POINTER(omg_box_job), C.POINTER(omg_params), P, P, P]),
+    "omg_trace_web_box_jobs": (I32, [P, P, U32, P, P, P]),
+    "omg_trace_web_world_jobs": (I32, [P, U32, P, U32, P, P, P]),
+    "omg_param_block_flat_len": (U32, [U32]),
+    "omg_param_block_write_flat": (I32, [C.POINTER(omg_param_block), P, U32, P, U32]),
+    "omg_param_block_read_flat": (I32, [P, U32, C.POINTER(omg_param_block), P, U32, PU32]),
+    "omg_param_block_from_late": (I32, [P, U32, P]),
 }
 
 NOALLOC_MAX_CELLS = 45056
+WEB_BOX_JOB_F32S, WEB_BOX_JOB_VERSION = 57, 2
+WEB_WORLD_MAX_PANELS, WEB_WORLD_JOB_VERSION = 64, 3
+WEB_WORLD_JOB_F32S = 10 + WEB_WORLD_MAX_PANELS * 16
+PARAM_FLAT_HEADER, PARAM_FLAT_PER_TAP = 24, 9
 
 _lib = None
 

@@ -21,7 +21,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["trace.cu", "wavefront.cu", "coop.cu", "reverb.cu", "lbvh.cu", "dome.cu", "noalloc.cu", "mlp.cu", "late.cu"]
-CPP_SOURCES = ["api.cpp", "api_scene.cpp", "api_dome.cpp", "api_mlp.cpp", "api_late.cpp", "scene.cpp"]
+CPP_SOURCES = ["api.cpp", "api_scene.cpp", "api_dome.cpp", "api_mlp.cpp", "api_late.cpp", "api_wire.cpp", "scene.cpp"]
 
 
 def _sources():
