@@ -434,3 +434,88 @@ uint32_t orc_world_build(void* mbv, const RoomC* rooms, uint32_t n_rooms, const 
 extern "C" void orc_sincos_f32(const float* phi, uint32_t n, float* s, float* c) {
   for (uint32_t i = 0; i < n; i++) sincos_f32(phi[i], &s[i], &c[i]);
 }
+
+// ------------------------------------------------ world early reflections
+// crates/omg-core/src/pt_mesh.rs over an f32 oracle mesh (omg_oracle_early.hpp).
+#include "omg_oracle_early.hpp"
+
+namespace {
+struct EarlyHandle {
+  const Mesh<float>* mesh;
+  SurfaceTable table;
+  std::vector<std::pair<V3<float>, V3<float>>> boxes;
+};
+}  // namespace
+
+extern "C" {
+// SurfaceTable::build + append_box per furniture box (early_world.rs:114-120);
+// the boxes are also discovery's overlay reflectors.
+void* orc_early_new(void* meshv, const BoxPanelC* furn, uint32_t n_furn) {
+  MeshHandle* h = (MeshHandle*)meshv;
+  if (h->real != 0) return nullptr;
+  EarlyHandle* e = new EarlyHandle();
+  e->mesh = &h->mf;
+  e->table.build(h->mf);
+  for (uint32_t i = 0; i < n_furn; i++) {
+    e->table.append_box(furn[i].mn, furn[i].mx, furn[i].m);
+    e->boxes.push_back({from_f<float>(furn[i].mn), from_f<float>(furn[i].mx)});
+  }
+  return e;
+}
+void orc_early_free(void* e) { delete (EarlyHandle*)e; }
+uint32_t orc_early_base_overlay(void* e) { return ((EarlyHandle*)e)->table.base_overlay; }
+uint32_t orc_early_n_surfaces(void* e) { return (uint32_t)((EarlyHandle*)e)->table.surfaces.size(); }
+
+// mesh_chains (pt_mesh.rs:382-457); use_boxes = 0 runs it with no overlay
+// boxes (the furniture switch off). Returns the chain count; writes <= cap.
+uint32_t orc_early_discover(void* ev, const float* lis, uint32_t n_rays, uint32_t rot, int use_boxes,
+                            uint16_t* chains, uint8_t* orders, uint32_t cap) {
+  EarlyHandle* e = (EarlyHandle*)ev;
+  std::vector<MChain> out;
+  static const std::vector<std::pair<V3<float>, V3<float>>> none;
+  mesh_chains(*e->mesh, use_boxes ? e->boxes : none, e->table.base_overlay, from_f<float>(lis), n_rays, rot, out);
+  for (size_t i = 0; i < out.size() && i < cap; i++) {
+    for (int k = 0; k < M_MAX_ORDER; k++) chains[3 * i + k] = out[i].c[k];
+    orders[i] = out[i].order;
+  }
+  return (uint32_t)out.size();
+}
+
+// mesh_record (pt_mesh.rs:186-337) for every (source, chain) pair, source
+// major; out: 7 floats per pair (delay_s, dir[3], gains[3]), valid: 1 when the
+// pair solves. threads > 1 splits the sources over std::threads.
+void orc_early_solve(void* ev, const uint16_t* src_ids, const float* src_pos, uint32_t n_src, const uint16_t* chains,
+                     const uint8_t* orders, uint32_t n_chains, const float* lis, const Aabb* extras, uint32_t n_extras,
+                     float* out, uint8_t* valid, int threads) {
+  EarlyHandle* e = (EarlyHandle*)ev;
+  std::vector<Aabb> ex(extras, extras + n_extras);
+  const V3<float> L = from_f<float>(lis);
+  auto run = [&](uint32_t s0, uint32_t s1) {
+    std::vector<SegHit> buf;
+    for (uint32_t s = s0; s < s1; s++) {
+      for (uint32_t c = 0; c < n_chains; c++) {
+        MeshRecord r;
+        const size_t k = (size_t)s * n_chains + c;
+        const bool ok = mesh_record(*e->mesh, e->table, chains + 3 * c, orders[c], src_ids[s],
+                                    from_f<float>(src_pos + 3 * s), L, ex, buf, &r);
+        valid[k] = ok ? 1 : 0;
+        float* o = out + 7 * k;
+        if (ok) {
+          o[0] = r.delay_s;
+          for (int q = 0; q < 3; q++) { o[1 + q] = r.dir[q]; o[4 + q] = r.gains[q]; }
+        } else {
+          for (int q = 0; q < 7; q++) o[q] = 0.0f;
+        }
+      }
+    }
+  };
+  const uint32_t nt = (uint32_t)std::max(1, std::min<int>(threads, (int)std::max<uint32_t>(n_src, 1)));
+  if (nt <= 1) {
+    run(0, n_src);
+    return;
+  }
+  std::vector<std::thread> ts;
+  for (uint32_t t = 0; t < nt; t++) ts.emplace_back(run, n_src * t / nt, n_src * (t + 1) / nt);
+  for (auto& t : ts) t.join();
+}
+}

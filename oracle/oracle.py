@@ -26,9 +26,9 @@ BUILD_CMD = ["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-shared"
 
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "omg_oracle.cpp")
-    hdr = os.path.join(HERE, "omg_oracle.hpp")
+    hdrs = [os.path.join(HERE, f) for f in ("omg_oracle.hpp", "omg_oracle_early.hpp")]
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+            and os.path.getmtime(LIB_PATH) >= max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in hdrs])):
         return LIB_PATH
     subprocess.check_call(BUILD_CMD)
     return LIB_PATH
@@ -123,6 +123,16 @@ def lib():
         L.orc_dome_fan.argtypes = [U32, I, P]
         L.orc_pcg_draws.argtypes = [U32, U32, U32, P]
         L.orc_xorshift_draws.argtypes = [U64, U32, P]
+        L.orc_early_new.argtypes = [P, P, U32]
+        L.orc_early_new.restype = P
+        L.orc_early_free.argtypes = [P]
+        L.orc_early_base_overlay.argtypes = [P]
+        L.orc_early_base_overlay.restype = U32
+        L.orc_early_n_surfaces.argtypes = [P]
+        L.orc_early_n_surfaces.restype = U32
+        L.orc_early_discover.argtypes = [P, P, U32, U32, I, P, P, U32]
+        L.orc_early_discover.restype = U32
+        L.orc_early_solve.argtypes = [P, P, P, U32, P, P, U32, P, P, U32, P, P, I]
         _lib = L
     return _lib
 
@@ -459,3 +469,71 @@ def sincos_f32(phi: np.ndarray):
     L.orc_sincos_f32.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
     L.orc_sincos_f32(_p(phi), len(phi), _p(s), _p(c))
     return s, c
+
+
+# ----------------------------------------------------- world early reflections
+class AabbC(C.Structure):
+    """crates/omg-core/src/pt.rs:31-35."""
+    _fields_ = [("mn", C.c_float * 3), ("mx", C.c_float * 3), ("transmission", C.c_float * 3)]
+
+
+def aabbs(extras):
+    """(min, max, transmission3) triples -> a ctypes array (or None)."""
+    if not extras:
+        return None
+    arr = (AabbC * len(extras))()
+    for i, (mn, mx, tr) in enumerate(extras):
+        for k in range(3):
+            arr[i].mn[k] = mn[k]
+            arr[i].mx[k] = mx[k]
+            arr[i].transmission[k] = tr[k]
+    return arr
+
+
+class Early:
+    """pt_mesh.rs over an f32 oracle mesh: SurfaceTable (+ furniture faces),
+    mesh_chains discovery, mesh_record solves."""
+
+    def __init__(self, mesh: "Mesh", furniture=()):
+        assert mesh.real == "f32"
+        self.mesh = mesh      # keeps the mesh alive
+        parr, n = _panels_arr(list(furniture))
+        self.h = lib().orc_early_new(mesh.h, C.cast(parr, C.c_void_p) if parr is not None else None, n)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_early_free(self.h)
+            self.h = None
+
+    @property
+    def base_overlay(self) -> int:
+        return int(lib().orc_early_base_overlay(self.h))
+
+    @property
+    def n_surfaces(self) -> int:
+        return int(lib().orc_early_n_surfaces(self.h))
+
+    def discover(self, listener, n_rays=768, rot=0, use_boxes=True, cap=1 << 16):
+        """mesh_chains: list of (chain tuple, order) in first-found order."""
+        ch = np.zeros((cap, 3), np.uint16)
+        od = np.zeros(cap, np.uint8)
+        n = lib().orc_early_discover(self.h, _p(_f3(listener)), n_rays, rot, int(use_boxes), _p(ch), _p(od), cap)
+        n = min(n, cap)
+        return [(tuple(int(v) for v in ch[i]), int(od[i])) for i in range(n)]
+
+    def solve(self, sources, chains, listener, extras=(), threads=1):
+        """mesh_record for every (source, chain) pair, source-major.
+        sources: (id, pos) pairs; chains: (chain3, order) pairs.
+        Returns (records (n_src, n_chain, 7) = delay, dir3, gains3; valid bool (n_src, n_chain))."""
+        ns, nc = len(sources), len(chains)
+        ids = np.array([s[0] for s in sources], np.uint16)
+        pos = np.array([s[1] for s in sources], np.float32).reshape(-1, 3)
+        ch = np.array([c[0] for c in chains], np.uint16).reshape(-1, 3)
+        od = np.array([c[1] for c in chains], np.uint8)
+        out = np.zeros((ns, nc, 7), np.float32)
+        valid = np.zeros((ns, nc), np.uint8)
+        ex = aabbs(list(extras))
+        lib().orc_early_solve(self.h, _p(ids), _p(pos), ns, _p(ch), _p(od), nc, _p(_f3(listener)),
+                              C.cast(ex, C.c_void_p) if ex is not None else None, len(extras), _p(out), _p(valid),
+                              threads)
+        return out, valid.astype(bool)

@@ -1,10 +1,13 @@
-"""Extract the reference's walkthrough world (rooms and doors) as JSON data.
+"""Extract the reference's walkthrough world (rooms, doors, furniture) as JSON data.
 
 Reads crates/omg-scene/src/walkthrough.rs of the reference checkout (text
 only, nothing is executed) and writes tests/golden/walkthrough_world.json:
-the room table of `rooms()` (walkthrough.rs:44-226) and the door table of
-`doors()` (walkthrough.rs:275-307), with wall materials by preset name. The
-dome tests of dome.rs:496-654 run on this world.
+the room table of `rooms()` (walkthrough.rs:44-226), the door table of
+`doors()` (walkthrough.rs:275-307), with wall materials by preset name, and
+the furniture of `furniture(room)` / `furniture_mats(room)` with
+FURN_REFLECTOR_MIN_VOL (walkthrough.rs:535-672). The dome tests of
+dome.rs:496-654 and the world early-reflection tests (the reference's
+solve_parity.rs world) run on this world.
 
     python tests/golden/make_walkthrough_fixture.py /path/to/reference
 """
@@ -45,15 +48,55 @@ def parse(src: str):
     return rooms, doors
 
 
+def parse_furniture(src: str):
+    consts = {m.group(1): int(m.group(2)) for m in re.finditer(r"pub const (\w+): usize = (\d+);", src)}
+    fb = src[src.index("pub fn furniture(room: usize)"):src.index("pub const FURN_REFLECTOR_MIN_VOL")]
+    num = r"(-?[\d.]+)"
+    tconst = {m.group(1): [float(v) for v in m.group(2).split(",")]
+              for m in re.finditer(r"const (\w+): \[f32; 3\] = \[([^\]]+)\];", fb)}
+    tables = {}
+    for m in re.finditer(r"static (\w+): \[omg_core::pt::Aabb; \d+\] = \[(.*?)\];", fb, re.S):
+        boxes = []
+        for b in re.finditer(r"boxy\(" + r",\s*".join([num] * 6) + r",\s*(\w+)\)", m.group(2)):
+            v = [float(b.group(i)) for i in range(1, 7)]
+            boxes.append(dict(min=v[:3], max=v[3:], transmission=tconst[b.group(7)]))
+        tables[m.group(1)] = boxes
+    rooms_f = {consts[a]: tables[b] for a, b in re.findall(r"(\w+) => &(\w+_F),", fb)}
+    mb = src[src.index("pub fn furniture_mats(room: usize)"):]
+    mb = mb[:mb.index("\n}\n") + 3]
+    mconst = {}
+    for m in re.finditer(r"const (\w+): Material = Material \{\s*absorption: \[([^\]]+)\],\s*scattering: ([\d.]+),"
+                         r"\s*transmission: \[([^\]]+)\],\s*\};", mb):
+        mconst[m.group(1)] = dict(absorption=[float(v) for v in m.group(2).split(",")], scattering=float(m.group(3)),
+                                  transmission=[float(v) for v in m.group(4).split(",")])
+    mtables = {}
+    for m in re.finditer(r"static (\w+): \[Material; (\d+)\] =\s*\[(.*?)\];", mb, re.S):
+        body = re.sub(r"//[^\n]*", "", m.group(3))
+        rep = re.match(r"\s*(\w+); (\d+)\s*$", body)
+        names = [rep.group(1)] * int(rep.group(2)) if rep else [x.strip() for x in body.split(",") if x.strip()]
+        assert len(names) == int(m.group(2)), m.group(1)
+        mtables[m.group(1)] = [mconst[n] for n in names]
+    rooms_m = {consts[a]: mtables[b] for a, b in re.findall(r"(\w+) => &(\w+_M),", mb)}
+    out = {}
+    for r, boxes in rooms_f.items():
+        mats = rooms_m[r]
+        assert len(mats) == len(boxes), r
+        out[str(r)] = [dict(b, material=m) for b, m in zip(boxes, mats)]
+    vol = float(re.search(r"pub const FURN_REFLECTOR_MIN_VOL: f32 = ([\d.]+);", src).group(1))
+    return out, vol
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     src = open(os.path.join(ref, "crates/omg-scene/src/walkthrough.rs")).read()
     rooms, doors = parse(src)
+    furniture, min_vol = parse_furniture(src)
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "walkthrough_world.json")
     with open(out, "w") as fh:
-        json.dump({"source": "crates/omg-scene/src/walkthrough.rs rooms() and doors()", "rooms": rooms,
-                   "doors": doors}, fh, indent=1)
-    print(out, len(rooms), "rooms", len(doors), "doors")
+        json.dump({"source": "crates/omg-scene/src/walkthrough.rs rooms(), doors(), furniture(), furniture_mats()",
+                   "rooms": rooms, "doors": doors, "furniture": furniture,
+                   "furn_reflector_min_vol": min_vol}, fh, indent=1)
+    print(out, len(rooms), "rooms", len(doors), "doors", sum(len(v) for v in furniture.values()), "furniture")
 
 
 if __name__ == "__main__":
