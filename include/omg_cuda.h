@@ -389,6 +389,60 @@ int32_t omg_late_reset(omg_ctx* ctx, uint32_t field_id, uint32_t slot);
 /* A slot's averaged echogram (n_bins x n_bands, n_bins x 3). Not while a tick is in flight. */
 int32_t omg_late_read(omg_ctx* ctx, uint32_t field_id, uint32_t slot, float* bins, float* dirs);
 
+/* ---------------------------------------------- world early reflections */
+/* Specular surface chains over the world mesh (crates/omg-core/src/pt_mesh.rs):
+ * discovery from the listener (mesh_chains, :382-457; the WorldDiscovery seam,
+ * omg-scene/src/early_world.rs:18-26, kernel K3 in the reference's GPU plan)
+ * and the exact per-(source, chain) solve with transmission along every leg
+ * (mesh_record, :186-337; the WorldSolve seam, early_world.rs:36-48, kernel
+ * K4). A chain lists authored surface ids listener-first; surfaces at or above
+ * the table's base_overlay are the faces of the furniture boxes, 6 per box in
+ * the order x-min, x-max, y-min, y-max, z-min, z-max (SurfaceTable::append_box,
+ * pt_mesh.rs:86-109). Closest hits follow the reference's first-found order
+ * (tie_mode 0 semantics) whatever the context's tie_mode; over the reference's
+ * tree (OMG_BVH_SAH) they are the reference's hits exactly. */
+#define OMG_CHAIN_MAX_ORDER 3
+#define OMG_NO_SURF 0xFFFFu
+typedef struct omg_chain {       /* MChain (pt_mesh.rs:111) */
+    uint16_t surf[OMG_CHAIN_MAX_ORDER];  /* OMG_NO_SURF beyond order */
+    uint16_t order;              /* 0 = the direct path */
+} omg_chain;
+typedef struct omg_aabb {        /* pt.rs:31-35: a transient blocker (door leaf, pane, furniture) */
+    float mn[3];
+    float mx[3];
+    float transmission[3];       /* per-band amplitude through it */
+} omg_aabb;
+typedef struct omg_mesh_record { /* MeshRecord (pt_mesh.rs:113-121) */
+    uint16_t source;
+    uint16_t chain[OMG_CHAIN_MAX_ORDER];
+    uint32_t order;
+    float delay_s;
+    float dir[3];                /* from the listener toward the image source */
+    float gains[3];              /* per-band amplitude */
+    uint32_t key;                /* MeshRecord::key (pt_mesh.rs:123-134) */
+    uint32_t valid;              /* 0: the pair does not solve (mesh_record -> None) */
+} omg_mesh_record;
+/* SurfaceTable::build over an uploaded scene plus append_box per furniture box
+ * (early_world.rs:114-120); the boxes also reflect discovery rays. Scenes of at
+ * most 2^16 - 1 surfaces (ids are u16). */
+int32_t omg_early_create(omg_ctx* ctx, uint32_t scene_id, const omg_panel* furniture, uint32_t n_furniture,
+                         uint32_t* early_id);
+int32_t omg_early_destroy(omg_ctx* ctx, uint32_t early_id);
+int32_t omg_early_info(omg_ctx* ctx, uint32_t early_id, uint32_t* base_overlay, uint32_t* n_surfaces);
+/* WorldDiscovery::discover / mesh_chains: n_rays fan rays from the listener,
+ * fan rotation rot, up to 3 specular bounces each; the unique chains in the
+ * reference's first-found order (ray, then bounce). use_boxes = 0 leaves the
+ * furniture out (the furniture switch off). *n_out = the number found; the
+ * first min(n_out, cap) are written. */
+int32_t omg_early_discover(omg_ctx* ctx, uint32_t early_id, const float listener[3], uint32_t n_rays,
+                           uint32_t rot, int32_t use_boxes, omg_chain* out, uint32_t cap, uint32_t* n_out);
+/* WorldSolve::solve_batch / mesh_record for every (source, chain) pair in one
+ * launch: out[s * n_chains + c]. extras: blockers every leg pays when it
+ * passes through them (mesh_record's `extras`). */
+int32_t omg_early_solve(omg_ctx* ctx, uint32_t early_id, const uint16_t* source_ids, const float* source_pos,
+                        uint32_t n_sources, const omg_chain* chains, uint32_t n_chains, const float listener[3],
+                        const omg_aabb* extras, uint32_t n_extras, omg_mesh_record* out);
+
 /* ------------------------------------------------------------- wire formats */
 /* The web bridge's flat trace jobs, as the wasm build queues them for its GPU
  * driver and the driver reads them (crates/omg-web/src/lib.rs:150-202 and

@@ -79,6 +79,19 @@ class omg_tune_result(C.Structure):
                 ("ms", C.c_float)]
 
 
+class omg_chain(C.Structure):
+    _fields_ = [("surf", C.c_uint16 * 3), ("order", C.c_uint16)]
+
+
+class omg_aabb(C.Structure):
+    _fields_ = [("mn", F3), ("mx", F3), ("transmission", F3)]
+
+
+class omg_mesh_record(C.Structure):
+    _fields_ = [("source", C.c_uint16), ("chain", C.c_uint16 * 3), ("order", C.c_uint32), ("delay_s", C.c_float),
+                ("dir", F3), ("gains", F3), ("key", C.c_uint32), ("valid", C.c_uint32)]
+
+
 class omg_tap(C.Structure):
     _fields_ = [("key", C.c_uint32), ("delay_s", C.c_float), ("dir", F3), ("gains", F3)]
 
@@ -169,6 +182,11 @@ SIGNATURES = {
     "omg_mlp_set_params": (I32, [P, U32, U32, P, U64]),
     "omg_tc_gemm": (I32, [P, P, P, P, U32, U32, U32]),
     "omg_trace_box_noalloc": (I32, [C.POINTER(omg_box_job), C.POINTER(omg_params), P, P, P]),
+    "omg_early_create": (I32, [P, U32, P, U32, PU32]),
+    "omg_early_destroy": (I32, [P, U32]),
+    "omg_early_info": (I32, [P, U32, PU32, PU32]),
+    "omg_early_discover": (I32, [P, U32, P, U32, U32, I32, P, U32, PU32]),
+    "omg_early_solve": (I32, [P, U32, P, P, U32, P, U32, P, P, U32, P]),
     "omg_trace_web_box_jobs": (I32, [P, P, U32, P, P, P]),
     "omg_trace_web_world_jobs": (I32, [P, U32, P, U32, P, P, P]),
     "omg_param_block_flat_len": (U32, [U32]),
@@ -182,6 +200,7 @@ WEB_BOX_JOB_F32S, WEB_BOX_JOB_VERSION = 57, 2
 WEB_WORLD_MAX_PANELS, WEB_WORLD_JOB_VERSION = 64, 3
 WEB_WORLD_JOB_F32S = 10 + WEB_WORLD_MAX_PANELS * 16
 PARAM_FLAT_HEADER, PARAM_FLAT_PER_TAP = 24, 9
+CHAIN_MAX_ORDER, NO_SURF = 3, 0xFFFF
 
 _lib = None
 

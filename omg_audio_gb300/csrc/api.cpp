@@ -43,6 +43,27 @@ bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1])
 
 // The device scene table has a fixed capacity for the context's lifetime:
 // captured graphs hold its address, so it is never reallocated.
+DScene scene_view(const SceneRec& s) {
+  DScene d;
+  std::memset(&d, 0, sizeof(d));
+  d.nodes = s.nodes.p;
+  d.prims = s.prims.p;
+  d.normals = s.normals.p;
+  d.mats = s.mats.p;
+  d.tri_surface = s.tri_surface.p;
+  d.root = s.root;
+  d.n_nodes = s.n_nodes;
+  d.n_prims = s.n_prims;
+  d.n_bands = s.n_bands;
+  d.nodes4 = s.n_nodes4 ? s.nodes4.p : nullptr;
+  d.nodes4c = s.n_nodes4 ? s.nodes4c.p : nullptr;
+  d.nodes_f = s.nodes_f.p;
+  for (int a = 0; a < 3; a++) d.fast_m[a] = s.fast_m[a];
+  d.root4 = s.root4;
+  d.n_nodes4 = s.n_nodes4;
+  return d;
+}
+
 int32_t sync_scene_table(omg_ctx* ctx) {
   if (ctx->scene_cap == 0) {
     CK(ctx->d_scenes.alloc(kMaxScenes));
@@ -51,25 +72,7 @@ int32_t sync_scene_table(omg_ctx* ctx) {
   }
   std::vector<DScene> table(ctx->scene_cap);
   std::memset(table.data(), 0, table.size() * sizeof(DScene));
-  for (auto& kv : ctx->scenes) {
-    SceneRec& s = *kv.second;
-    DScene& d = table[kv.first];
-    d.nodes = s.nodes.p;
-    d.prims = s.prims.p;
-    d.normals = s.normals.p;
-    d.mats = s.mats.p;
-    d.tri_surface = s.tri_surface.p;
-    d.root = s.root;
-    d.n_nodes = s.n_nodes;
-    d.n_prims = s.n_prims;
-    d.n_bands = s.n_bands;
-    d.nodes4 = s.n_nodes4 ? s.nodes4.p : nullptr;
-    d.nodes4c = s.n_nodes4 ? s.nodes4c.p : nullptr;
-    d.nodes_f = s.nodes_f.p;
-    for (int a = 0; a < 3; a++) d.fast_m[a] = s.fast_m[a];
-    d.root4 = s.root4;
-    d.n_nodes4 = s.n_nodes4;
-  }
+  for (auto& kv : ctx->scenes) table[kv.first] = scene_view(*kv.second);
   CK(cudaMemcpy(ctx->d_scenes.p, table.data(), table.size() * sizeof(DScene), cudaMemcpyHostToDevice));
   return OMG_OK;
 }

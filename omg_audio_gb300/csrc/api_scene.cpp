@@ -1,6 +1,8 @@
 // C ABI of the GB300 tracer (include/omg_cuda.h), part 2: mesh builder,
 // scene upload (reference SAH tree on the host or LBVH on the device), BVH
 // export, closest-hit queries, estimate_reverb.
+#include <limits>
+
 #include "runtime.h"
 
 using namespace omg;
@@ -71,6 +73,27 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
   for (uint32_t m = 0; m < nm; m++) dmats[m] = make_dmat(mats[m], nb);
   std::vector<uint16_t> tsurf(nt, 0);
   if (tri_surf) tsurf.assign(tri_surf, tri_surf + nt);
+  // the surface table's seed (SurfaceTable::build, pt_mesh.rs:51-78): the
+  // first triangle of each surface id gives its plane and material
+  S->materials.assign(mats, mats + nm);
+  for (uint32_t t = 0; t < nt; t++) {
+    const uint32_t sid = tsurf[t];
+    if (sid >= S->surf_seed.size()) {
+      SceneRec::SurfSeed blank{{0.0f, 0.0f, 1.0f}, std::numeric_limits<float>::max(), 0u, 0u};
+      S->surf_seed.resize(sid + 1, blank);
+    }
+    SceneRec::SurfSeed& q = S->surf_seed[sid];
+    if (!q.set) {
+      const float* n = &normals[4 * (size_t)t];
+      const float* p = &pos[3 * (size_t)idx[3 * t]];
+      q.n[0] = n[0];
+      q.n[1] = n[1];
+      q.n[2] = n[2];
+      q.d = n[0] * p[0] + n[1] * p[1] + n[2] * p[2];
+      q.mat = tri_mat[t];
+      q.set = 1u;
+    }
+  }
 
   if (kind == OMG_BVH_SAH || kind == OMG_BVH_SAH3) {
     if (kind == OMG_BVH_SAH)

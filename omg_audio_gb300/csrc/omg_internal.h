@@ -324,4 +324,41 @@ cudaError_t launch_row_spread(const float* mean, const float* sd, uint32_t cols,
                               float* out, cudaStream_t s);
 cudaError_t build_dome_fan(float4* fan, uint32_t n_fan, cudaStream_t s);
 
+// early.cu: world early reflections (pt_mesh.rs). One surface of the table
+// (pt_mesh.rs:30-41): plane n.x = d, per-band reflection and transmission
+// amplitudes, and for a furniture face its rect.
+struct alignas(16) DSurf {
+  float n[3];
+  float d;
+  float refl[3];
+  uint32_t rect;
+  float trans[3];
+  float pad0;
+  float fmin[3];
+  float pad1;
+  float fmax[3];
+  float pad2;
+};
+struct DEarly {
+  DScene S;                   // the mesh (its binary tree: first-found closest hits, segment walks)
+  const DSurf* surf;
+  uint32_t n_surf;
+  uint32_t base_overlay;
+  const float4* mtrans;       // per scene material: amplitude transmission of bands 0..2
+  const float4* boxes;        // furniture boxes: 2 float4 (min, max) each
+  uint32_t n_boxes;
+  float root_lo[3], root_hi[3];  // the tree's root box (segment_hits tests it first)
+  uint32_t* err;              // error bits: 1 stack, 2 crossing list, 4 walk budget, 8 hash table
+};
+// Discovery: n_rays fan rays -> 3 candidates each (cand_key 0 = none), the
+// first occurrence of every key (hash table tkey/tidx of tcap slots, cleared
+// to 0 / 0xFFFFFFFF) compacted in candidate order into out (<= cap), *n_out.
+cudaError_t launch_early_discover(const DEarly& E, const float lis[3], uint32_t n_rays, uint32_t rot, bool use_boxes,
+                                  const float* jitter, unsigned long long* cand_key, omg_chain* cand_chain,
+                                  uint32_t* cand_slot, unsigned long long* tkey, uint32_t* tidx, uint32_t tcap,
+                                  omg_chain* out, uint32_t cap, uint32_t* n_out, cudaStream_t s);
+cudaError_t launch_early_solve(const DEarly& E, const uint16_t* ids, const float* pos, uint32_t n_src,
+                               const omg_chain* chains, uint32_t n_chains, const float lis[3], const omg_aabb* extras,
+                               uint32_t n_extras, omg_mesh_record* out, cudaStream_t s);
+
 }  // namespace omg

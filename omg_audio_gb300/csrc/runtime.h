@@ -70,6 +70,16 @@ struct SceneRec {
   DevBuf<DMat> mats;
   DevBuf<uint16_t> tri_surface;
   // host copies for export / queries
+  std::vector<omg_material> materials;
+  // per authored surface id, its first triangle's plane and material
+  // (SurfaceTable::build, pt_mesh.rs:51-78): n[3], d, material, set
+  struct SurfSeed {
+    float n[3];
+    float d;
+    uint32_t mat;
+    uint32_t set;
+  };
+  std::vector<SurfSeed> surf_seed;
   std::vector<float> ref_boxes;
   std::vector<uint32_t> ref_ab;
   std::vector<float> prim_geo;
@@ -134,6 +144,7 @@ struct Ticket {
 struct DomeRec;
 struct MlpRec;
 struct LateRec;
+struct EarlyRec;
 
 }  // namespace omg
 
@@ -159,6 +170,8 @@ struct omg_ctx {
   uint32_t next_mlp = 1;
   std::map<uint32_t, std::shared_ptr<omg::LateRec>> lates;  // late fields
   uint32_t next_late = 1;
+  std::map<uint32_t, std::shared_ptr<omg::EarlyRec>> earlies;  // world early-reflection tables
+  uint32_t next_early = 1;
   // raycast query scratch
   omg::DevBuf<float> q_o, q_d, q_t;
   omg::DevBuf<uint32_t> q_tri;
@@ -177,6 +190,8 @@ int32_t fail(omg_ctx* ctx, cudaError_t e, const char* where);
 uint32_t timeout_of(const omg_ctx* ctx);
 int32_t wait_event(omg_ctx* ctx, cudaEvent_t ev, uint32_t timeout_ms);
 int32_t sync_scene_table(omg_ctx* ctx);
+// The device view of an uploaded scene (one entry of the scene table).
+DScene scene_view(const SceneRec& s);
 // api.cpp: a batch record for `jobs` (allocations, uploads, launch graphs);
 // the same record refilled with new per-job values when the job layout
 // (batch_layout) is unchanged; the kernels' error flags of its last read-back.

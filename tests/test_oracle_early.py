@@ -4,12 +4,14 @@ the mesh solver agrees with the analytic image sources in a box, doorways
 thread without portal code on the walkthrough world, and a furniture face
 reflects exactly. CPU only."""
 import itertools
+import json
+import os
 
 import numpy as np
 import pytest
 
 from omg_audio_gb300 import materials as M
-from walkthrough import load, oracle_world
+from walkthrough import HERE, oracle_world
 
 NO = 0xFFFF
 AIR = np.float32([1.0e-4, 5.0e-4, 3.0e-3])     # material.rs:76
@@ -159,11 +161,33 @@ def test_discovery_is_deterministic_and_rotates(oracle):
 
 def test_walkthrough_furniture_fixture():
     """walkthrough.rs:535-672: furniture rows parallel to their materials."""
-    d = __import__("json").load(open(__import__("walkthrough").os.path.join(
-        __import__("walkthrough").HERE, "golden", "walkthrough_world.json")))
+    with open(os.path.join(HERE, "golden", "walkthrough_world.json")) as fh:
+        d = json.load(fh)
     assert d["furn_reflector_min_vol"] == 0.25
     assert sum(len(v) for v in d["furniture"].values()) == 37
     for room, boxes in d["furniture"].items():
         for b in boxes:
             assert all(lo <= hi for lo, hi in zip(b["min"], b["max"]))
             assert b["transmission"] == b["material"]["transmission"]
+
+
+def test_reference_acceptance_world_is_not_degenerate(oracle):
+    """solve_parity.rs:24-61, 183: on the walkthrough world with its furniture
+    and two shut leaves, the oracle solves more than 200 of the pairs of three
+    listener spots x six sources."""
+    from walkthrough import furniture_world
+    O = oracle
+    furn, extras = furniture_world(lambda m: O.Material.make(m["absorption"], m["scattering"], m["transmission"]))
+    assert len(furn) > 10 and len(extras) == 39
+    E = O.Early(_walkthrough_mesh(O), furn)
+    srcs = [(8, (10.5, 20.5, 1.2)), (16, (2.0, 2.0, 1.0)), (24, (31.5, 18.0, 1.4)), (32, (7.0, 30.0, 1.7)),
+            (40, (18.0, 9.0, 2.2)), (48, (4.0, 25.0, 0.8))]
+    solved = 0
+    for lis in [(10.5, 20.5, 1.6), (4.4, 7.5, 1.6), (7.0, 27.0, 1.6)]:
+        cs = set()
+        for rot in range(6):
+            cs.update(E.discover(lis, 768, rot))
+        chains = [((NO, NO, NO), 0)] + sorted(cs)[:399]
+        _, valid = E.solve(srcs, chains, lis, extras, threads=8)
+        solved += int(valid.sum())
+    assert solved > 200, solved

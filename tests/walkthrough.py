@@ -52,3 +52,30 @@ def leaf_panels(doors):
         out.append(dict(axis=d["axis"], plane=float(plane), lat=(float(lo), float(lo + covered)),
                         z=(float(z0), float(z1)), glass=False, trans=t))
     return out
+
+
+def furniture_world(materials_of):
+    """The reference's solve_parity.rs world (solve_parity.rs:24-61): every
+    furniture box in world coordinates as an extras blocker, the pieces above
+    FURN_REFLECTOR_MIN_VOL as reflector boxes with their materials, and two
+    shut wood leaves. materials_of(dict) -> the caller's material object.
+    Returns (furniture [(min, max, material)], extras [(min, max, transmission)])."""
+    import numpy as np
+    f32 = np.float32
+    with open(os.path.join(HERE, "golden", "walkthrough_world.json")) as fh:
+        d = json.load(fh)
+    rooms = d["rooms"]
+    furn, extras = [], []
+    for ri, r in enumerate(rooms):
+        o = (f32(r["min"][0]), f32(r["min"][1]), f32(r["floor_z"]))
+        for b in d["furniture"].get(str(ri), []):
+            mn = tuple(float(f32(b["min"][k]) + o[k]) for k in range(3))
+            mx = tuple(float(f32(b["max"][k]) + o[k]) for k in range(3))
+            extras.append((mn, mx, tuple(b["transmission"])))
+            dd = [f32(f32(b["max"][k]) - f32(b["min"][k])) for k in range(3)]
+            if f32(f32(dd[0] * dd[1]) * dd[2]) > f32(d["furn_reflector_min_vol"]):
+                furn.append((mn, mx, materials_of(b["material"])))
+    leaf = M.WOOD_PANEL.transmission
+    extras.append(((6.9, 24.9, 0.0), (7.5, 25.1, 2.1), leaf))
+    extras.append(((3.9, 7.9, 0.0), (4.9, 8.1, 2.1), leaf))
+    return furn, extras
