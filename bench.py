@@ -14,6 +14,11 @@ jobs) are resident in HBM; the BVH (~3 MB) fits in L2, so L2 is flushed (a
 The near-tie rule (tie_mode 1: lowest surface id among hits within 1e-6
 relative t) is on, so the f32 result matches the FP64 oracle.
 
+Beside the headline, the line carries the learned surrogate against the
+tracer ("surrogate") and the world early reflections on the same scene
+("early": chain discovery and the batched exact solve of every source x chain
+pair, with the oracle's solve of a sample timed beside it).
+
 Rank 0 prints one JSON line. `--impl reference` times the CPU restatement of
 the reference tracer (the oracle port; the reference itself is Rust and has
 no toolchain here) on the host cores, on the same metric.
@@ -241,6 +246,64 @@ def surrogate_leg(args, device):
         "speedup": t_trace / t_pred, "surrogate_features_ms_per_room": 1e3 * t_feat / n,
         "timing": "wall clock of the calls with host buffers: trace_rooms (batched jobs, echograms down) vs "
                   "RoomSurrogate.predict (input features, omg_surrogate_query, decay curves down)",
+    }
+
+
+def early_leg(args, device, case):
+    """World early reflections on the 40-room scene (its reference SAH tree):
+    per listener, chain discovery (768 fan rays x 6 rotations) and the batched
+    exact solve of every (source, chain) pair for the 64 sources, through the C
+    ABI with host buffers; the oracle's single-thread solve of the same pairs
+    beside it, and the number of pairs whose result differs."""
+    from omg_audio_gb300 import Context, MeshBuilder, TraceConfig, _lib
+    from omg_audio_gb300.early import WorldEarly
+    from oracle import oracle as O
+    ctx = Context(TraceConfig(device=device, timeout_ms=60000))
+    mb = MeshBuilder()
+    case.recorder.replay(mb)
+    scene = ctx.upload_builder(mb, 3, _lib.BVH_SAH)
+    early = WorldEarly(ctx, scene)
+    oe = O.Early(oracle_mesh(case))
+    sources = [(8 * i, src) for i, (src, _) in enumerate(case.pairs)]
+    listeners = [lis for (_, lis) in case.pairs[:args.early_listeners]]
+    extras = [(mn, mx, m.transmission) for (mn, mx, m) in case.panels]
+    no = (_lib.NO_SURF,) * 3
+    disc_ms, solve_ms, cpu_s, pairs, solved, mismatch, cpu_pairs = [], [], 0.0, 0, 0, 0, 0
+    for li, lis in enumerate(listeners):
+        early.discover(lis, 768, 0)                       # warm-up
+        t0 = time.perf_counter()
+        found = set()
+        for rot in range(6):
+            found.update(early.discover(lis, 768, rot))
+        disc_ms.append(1e3 * (time.perf_counter() - t0) / 6)
+        chains = [(no, 0)] + sorted(found)[:399]
+        early.solve(sources, chains, lis, extras)         # warm-up
+        t0 = time.perf_counter()
+        rec = early.solve(sources, chains, lis, extras)
+        solve_ms.append(1e3 * (time.perf_counter() - t0))
+        pairs += rec.size
+        solved += int(rec["valid"].sum())
+        # the oracle on a sample of the sources, one thread
+        k = 8
+        t0 = time.perf_counter()
+        _, valid = oe.solve(sources[:k], chains, lis, extras, threads=1)
+        cpu_s += time.perf_counter() - t0
+        cpu_pairs += valid.size
+        mismatch += int(np.sum(valid != rec["valid"][:k].astype(bool)))
+    early.close()
+    scene.release()
+    ctx.close()
+    gpu_pairs_s = pairs / (1e-3 * float(np.sum(solve_ms)))
+    return {
+        "scene": "the 40-room scene (reference SAH tree), its panes as blockers",
+        "listeners": len(listeners), "sources": len(sources), "fan_rays": 768, "rotations": 6,
+        "chains_per_listener": round(pairs / len(sources) / len(listeners), 1),
+        "pairs": pairs, "solved": solved, "discover_ms_per_call": float(np.mean(disc_ms)),
+        "solve_ms_per_call": float(np.mean(solve_ms)), "solve_pairs_per_s": gpu_pairs_s,
+        "cpu_pairs_per_s": cpu_pairs / cpu_s, "cpu_threads": 1,
+        "cpu_sample": f"8 of {len(sources)} sources per listener (f32 oracle)",
+        "mismatched_pairs_in_cpu_sample": mismatch,
+        "timing": "wall clock of the calls with host buffers (chains and sources up, records down)",
     }
 
 
@@ -533,6 +596,8 @@ def run_ours(args):
         }
         if args.surrogate:
             line["surrogate"] = surrogate_leg(args, local)
+        if args.early_listeners > 0:
+            line["early"] = early_leg(args, local, case)
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()
@@ -554,6 +619,8 @@ def main():
     ap.add_argument("--profile", action="store_true", help="launches only (a small case under a profiler)")
     ap.add_argument("--no-surrogate", dest="surrogate", action="store_false",
                     help="skip the surrogate leg (train on tracer data, compare with the tracer)")
+    ap.add_argument("--early-listeners", type=int, default=8,
+                    help="listeners of the world early-reflection leg (0 skips it)")
     ap.add_argument("--surrogate-rooms", type=int, default=131072, help="training rooms (1 M: the full config)")
     ap.add_argument("--surrogate-epochs", type=int, default=60)
     ap.add_argument("--surrogate-test", type=int, default=16384, help="held-out rooms")
