@@ -545,7 +545,13 @@ def run_ours(args):
 
     # end to end through the C ABI with host buffers: the dome submitted (eyes
     # up, fans, bins down), the batch call on the same stream (jobs up, trace,
-    # echograms and reverb down), then the dome collected
+    # echograms and reverb down), then the dome collected. One untimed call
+    # first (it sets up the one-shot batch record); the reported time is the
+    # median over the steps (host-side stalls of a few hundred ms were seen on
+    # single calls), with the mean and the maximum beside it.
+    dome.submit(case.listeners, n_rays=DOME_RAYS, stream=stream.cuda_stream)
+    ctx.trace_batch(jobs, case.panels)
+    dome.collect()
     e2e_ms = []
     for k in range(max(1, args.steps)):
         flush.zero_()
@@ -558,7 +564,7 @@ def run_ours(args):
     h2d, d2h = ctx.io_bytes()
     d2h += 64 * 9 * (3 + 3) * 4 + 2 * 4 + 16
     h2d += 64 * 12
-    e2e = ws * (segments + dome_seg) / (float(np.mean(e2e_ms)) * 1e-3)
+    e2e = ws * (segments + dome_seg) / (float(np.median(e2e_ms)) * 1e-3)
 
     line = None
     if rank == 0:
@@ -581,7 +587,8 @@ def run_ours(args):
                        "dome": "the 64 fans after the trace, on its stream", "autotune": tune,
                        "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "ms_per_step": float(np.mean(e2e_ms))},
+                    "ms_per_step": float(np.median(e2e_ms)), "ms_mean": float(np.mean(e2e_ms)),
+                    "ms_max": float(np.max(e2e_ms)), "statistic": "median of the steps"},
             "gpu_launches": int(args.steps * (batch.kernel_count() + 3)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic(), "peak_kind": peak_kind,
@@ -612,8 +619,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--bvh", choices=["sah", "lbvh", "sah3"], default=None,
-                    help="sah: the reference's tree; sah3: three-axis binned SAH (default); lbvh: built on the "
-                         "GPU (the city's default: the host builds of its 1.9 M primitives take seconds)")
+                    help="sah: the reference's tree; sah3: three-axis binned SAH (default); lbvh: built on the GPU")
     ap.add_argument("--ref-pairs", type=int, default=64)
     ap.add_argument("--pairs", type=int, default=N_PAIRS, help="pairs traced per step (default: the workload's 64)")
     ap.add_argument("--profile", action="store_true", help="launches only (a small case under a profiler)")
@@ -635,7 +641,7 @@ def main():
     ap.add_argument("--city-rays", type=int, default=1 << 20, help="rays per source of the city workload")
     args = ap.parse_args()
     if args.bvh is None:
-        args.bvh = "lbvh" if args.workload == "city" else "sah3"
+        args.bvh = "sah3"
     if args.impl == "reference":
         return run_reference(args)
     if args.workload != "multiroom":

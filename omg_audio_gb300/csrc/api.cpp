@@ -41,8 +41,6 @@ bool valid_material(const omg_material& m, uint32_t nb) {
 
 bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
 
-// The device scene table has a fixed capacity for the context's lifetime:
-// captured graphs hold its address, so it is never reallocated.
 DScene scene_view(const SceneRec& s) {
   DScene d;
   std::memset(&d, 0, sizeof(d));
@@ -64,6 +62,8 @@ DScene scene_view(const SceneRec& s) {
   return d;
 }
 
+// The device scene table has a fixed capacity for the context's lifetime:
+// captured graphs hold its address, so it is never reallocated.
 int32_t sync_scene_table(omg_ctx* ctx) {
   if (ctx->scene_cap == 0) {
     CK(ctx->d_scenes.alloc(kMaxScenes));
