@@ -110,15 +110,19 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
     CK(S->nodes.alloc(S->n_nodes * 4));
     if (S->n_nodes)
       CK(cudaMemcpy(S->nodes.p, dev_nodes.data(), dev_nodes.size() * 4, cudaMemcpyHostToDevice));
+    const float pad = near_tie_pad(S->prim_geo);
     if (S->n_nodes) {
       std::vector<float> grown;
-      grow_nodes_for_fma(dev_nodes, grown, S->fast_m);
+      grow_nodes_for_fma(dev_nodes, grown, S->fast_m, pad);
       CK(S->nodes_f.alloc(S->n_nodes * 4));
       CK(cudaMemcpy(S->nodes_f.p, grown.data(), grown.size() * 4, cudaMemcpyHostToDevice));
     }
+    // the 4-wide tree serves near-tie walks only: its boxes are grown likewise
+    std::vector<float> grown_ref = S->ref_boxes;
+    grow_ref_boxes(grown_ref, S->fast_m, pad);
     std::vector<float> dev_nodes4;
     uint32_t need = 0;
-    S->root4 = flatten_bvh4(S->ref_boxes, S->ref_ab, dev_nodes4, &need);
+    S->root4 = flatten_bvh4(grown_ref, S->ref_ab, dev_nodes4, &need);
     S->n_nodes4 = (uint32_t)(dev_nodes4.size() / 32);
     // a tree whose walks could overflow the traversal stack keeps the binary walk
     if (need >= (uint32_t)STACK_DEPTH) S->n_nodes4 = 0;
@@ -189,7 +193,7 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
       for (int a = 0; a < 3; a++) S->fast_m[a] = mx[a] + 1.0f;
       if (S->root >= 0 && S->n_nodes) {
         CK(S->nodes_f.alloc((size_t)S->n_nodes * 4));
-        CK(grow_nodes(S->nodes.p, S->nodes_f.p, S->n_nodes, S->fast_m, ctx->stream));
+        CK(grow_nodes(S->nodes.p, S->nodes_f.p, S->n_nodes, S->fast_m, near_tie_pad(S->prim_geo), ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
       }
     }

@@ -30,19 +30,42 @@ constexpr int kDoneC = 0x7FFFFFFF;
 constexpr uint32_t kMaxLoopC = 1u << 22;    // warp loop guard (error 8)
 constexpr int kGroupsPerBlock = 64;         // 256 threads / 4
 
-// The near-tie rule between two candidate hits: true when a wins. A clearly
-// nearer hit wins; within the 1e-6 relative window the lower surface id, then
-// original triangle id, then primitive index wins (a total order, so every
-// lane of a group reduces to the same winner).
-__device__ __forceinline__ bool tie_better(bool ah, float at, uint32_t as, uint32_t atr, int ap, bool bh, float bt,
-                                           uint32_t bs, uint32_t btr, int bp) {
-  if (!bh) return ah;
-  if (!ah) return false;
-  if (at < bt * (1.0f - kTieRel)) return true;
-  if (bt < at * (1.0f - kTieRel)) return false;
-  if (as != bs) return as < bs;
-  if (atr != btr) return atr < btr;
-  return ap < bp;
+// Two lanes' near-tie states merged (TieState, device_common.cuh): the union
+// of the hits both have seen. The nearer t_min sets the window; a winner
+// outside it drops out, and if its lane had seen hits inside the window that
+// it no longer knows, the merged state is ambiguous. Winners compare by
+// (surface, triangle, t, primitive), a total order, so every lane of a group
+// reduces to the same state. In fixed mode the window is final and only the
+// lowest key counts.
+__device__ __forceinline__ void tie_merge(bool& ah, float& at, uint32_t& as, uint32_t& atr, int& ap, float& amin,
+                                          bool& aamb, bool bh, float bt, uint32_t bs, uint32_t btr, int bp,
+                                          float bmin, bool bamb, bool fixed) {
+  if (!bh) return;
+  bool take_b;
+  if (!ah) {
+    take_b = true;
+    amin = bmin;
+    aamb = bamb;
+  } else {
+    const bool b_less = tie_key_less(bs, btr, bt, as, atr, at) || (bs == as && btr == atr && bt == at && bp < ap);
+    if (fixed) {
+      take_b = b_less;
+    } else {
+      const float tmin = fminf(amin, bmin);
+      const float win = tmin * (1.0f + kTieRel);
+      const bool ain = at <= win, bin = bt <= win;
+      aamb = aamb || bamb || (!ain && amin <= win) || (!bin && bmin <= win);
+      take_b = (ain && bin) ? b_less : bin;
+      amin = tmin;
+    }
+  }
+  if (take_b) {
+    ah = true;
+    at = bt;
+    as = bs;
+    atr = btr;
+    ap = bp;
+  }
 }
 
 template <int NB>
@@ -85,8 +108,9 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
   int cur = kDoneC, sp = 0;
   bool have = false;
   float t_best = FLT_MAX, t_cull = FLT_MAX;
-  uint32_t s_best = 0, tri_best = 0, budget = 0;
-  int prim_best = -1;
+  uint32_t s_best = 0, tri_best = 0, budget = 0, budget0 = 0;
+  int prim_best = -1, root = kDoneC;
+  TieState ts = tie_begin();
 
   auto start_walk = [&](uint32_t r) {
     const DJob& J = jobs[find_job(jobs, n_jobs, r)];
@@ -101,7 +125,9 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
     // the walk ends at its first step without reading a node
     const bool walkable = J.geom == OMG_GEOM_MESH && S.n_prims != 0u && nodes != nullptr;
     cur = walkable ? S.root4 : kDoneC;
-    budget = walkable ? S.n_nodes4 + 1u : 1u;   // every node is entered at most once
+    root = cur;
+    budget0 = walkable ? S.n_nodes4 + 1u : 1u;   // every node is entered at most once per pass
+    budget = budget0;
     sp = 0;
     have = false;
     t_best = FLT_MAX;
@@ -109,6 +135,7 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
     s_best = 0;
     tri_best = 0;
     prim_best = -1;
+    ts = tie_begin();
     rid = r;
   };
   auto epoch_tally = [&](bool ended, bool parked, uint32_t r) {
@@ -229,8 +256,7 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
         const float4* c = nodes + 8 * cur + 2 * sub;
         const float4 a = __ldg(c), b = __ldg(c + 1);
         ref = __float_as_int(b.z);
-        hit = ref != kEmpty4 &&
-              ray_aabb(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz, have ? t_cull : FLT_MAX, tk);
+        hit = ref != kEmpty4 && ray_aabb(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz, t_cull, tk);
       }
       // leaves: each lane tests its hit leaf from the group's best, then the
       // group keeps the best of its lanes under the near-tie rule
@@ -240,7 +266,8 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
         float lt = t_best, lc = t_cull;
         uint32_t ls = s_best, ltr = tri_best;
         int lp = prim_best;
-        if (leaf) leaf_test<true>(prims, ref, ox, oy, oz, dx, dy, dz, lh, lt, lc, lp, ls, ltr);
+        TieState lts = ts;
+        if (leaf) leaf_test<true>(prims, ref, ox, oy, oz, dx, dy, dz, lh, lt, lc, lp, ls, ltr, lts);
 #pragma unroll
         for (int m = 1; m <= 2; m <<= 1) {
           const bool oh = __shfl_xor_sync(FULL, (int)lh, m) != 0;
@@ -248,9 +275,9 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
           const uint32_t os = __shfl_xor_sync(FULL, ls, m);
           const uint32_t otr = __shfl_xor_sync(FULL, ltr, m);
           const int op = __shfl_xor_sync(FULL, lp, m);
-          if (tie_better(oh, ot, os, otr, op, lh, lt, ls, ltr, lp)) {
-            lh = oh; lt = ot; ls = os; ltr = otr; lp = op;
-          }
+          const float omin = __shfl_xor_sync(FULL, lts.t_min, m);
+          const bool oamb = __shfl_xor_sync(FULL, (int)lts.amb, m) != 0;
+          tie_merge(lh, lt, ls, ltr, lp, lts.t_min, lts.amb, oh, ot, os, otr, op, omin, oamb, ts.fixed);
         }
         if (wk) {
           have = lh;
@@ -258,11 +285,13 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
           s_best = ls;
           tri_best = ltr;
           prim_best = lp;
-          t_cull = lh ? lt * (1.0f + kTieRel) : FLT_MAX;
+          ts.t_min = lts.t_min;
+          ts.amb = lts.amb;
+          if (!ts.fixed) t_cull = lh ? ts.t_min * (1.0f + kTieRel) : FLT_MAX;
         }
       }
       // internal children still in reach, ranked by (entry distance, child)
-      const bool in = hit && ref >= 0 && !(have && tk > t_cull);
+      const bool in = hit && ref >= 0 && !(tk > t_cull);
       const unsigned vm = __ballot_sync(FULL, in) & (0xFu << gbase);
       const int nv = __popc(vm);
       int rank = 0;
@@ -296,9 +325,20 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
           cur = kDoneC;
           while (sp > 0) {
             sp--;
-            if (have && sst[sp] > t_cull) continue;
+            if (sst[sp] > t_cull) continue;
             cur = sref[sp];
             break;
+          }
+          if (cur == kDoneC && ts.amb && !ts.fixed) {
+            // an ambiguous near-tie window: walk again with the final one
+            ts.fixed = true;
+            t_cull = ts.t_min * (1.0f + kTieRel);
+            have = false;
+            t_best = FLT_MAX;
+            prim_best = -1;
+            sp = 0;
+            budget = budget0;
+            cur = root;
           }
         }
       }

@@ -112,9 +112,14 @@ __device__ __forceinline__ bool ray_aabb(float lx, float ly, float lz, float hx,
 // with |o_a| <= 7 M_a it accepts every box ray_aabb accepts on the ungrown
 // box and returns an entry distance no larger: the rounding of t differs from
 // ray_aabb's by at most 4 u (|lo_a| + |o_a|) |inv_a| <= 2^-22 8 M_a |inv_a|
-// (u = 2^-24), no more than the margin 2^-19 M_a moves a face; a NaN from an
-// infinite inv leaves its axis open. Used only where the visit order does not
-// decide the hit (the near-tie rule), so the result is ray_aabb's.
+// (u = 2^-24), no more than the margin 2^-19 M_a moves a face. It needs
+// finite products: a direction component of 0 (inv infinite) can give
+// inf - inf on one face and -inf on the other and close an axis the ray runs
+// along, so walks with |d_a| < 2^-60 on any axis (or an origin beyond the
+// margin) use ray_aabb on the grown boxes instead, which is exact for them
+// and, the boxes being grown, accepts every box the ungrown test accepts.
+// Used only where the visit order does not decide the hit (the near-tie
+// rule), so the result is ray_aabb's.
 __device__ __forceinline__ bool ray_aabb_fma(float lx, float ly, float lz, float hx, float hy, float hz, float oix,
                                              float oiy, float oiz, float ix, float iy, float iz, float tmax,
                                              float& tout) {
@@ -158,18 +163,73 @@ __device__ __forceinline__ bool ray_tri(const float4& p0, const float4& p1, cons
 // Visit order, culling (t_enter >= best) and the strict `<` on hits are the
 // reference's, so over the reference tree the same triangle wins every tie.
 //
-// TIE = true resolves near-ties deterministically instead: a hit within a
-// relative t-gap of 1e-6 of the best replaces it only when its authored
-// surface id (then its original triangle id) is lower. Coplanar copies of a
-// shared wall, authored once per room with different materials, then resolve
-// the same way at any precision (the rule segment_hits applies to crossings,
-// mesh.rs:583-602). Nodes are culled only beyond best * (1 + 1e-6).
+// TIE = true resolves near-ties deterministically instead. Among all hits of
+// the ray, let t_min be the nearest; every hit within t_min * (1 + 1e-6) is a
+// near-tie of it, and the winner is the one of them with the lowest authored
+// surface id, then original triangle id, then t. Coplanar copies of a shared
+// wall, authored once per room with different materials, then resolve the
+// same way at any precision (the rule segment_hits applies to crossings,
+// mesh.rs:583-602). The winner depends only on the set of hits, so every
+// tree, walk order and lane split finds the same one.
+//
+// A walk keeps, besides the winner so far, the exact t_min so far; nodes are
+// culled beyond t_min * (1 + 1e-6). When a nearer hit shrinks the window so
+// that the winner so far falls out of it while an earlier hit may still lie
+// inside, the walk cannot know that hit any more: it flags `amb` and is then
+// walked once more in `fixed` mode, with the final window, taking the lowest
+// key among the hits inside it. That second walk is rare (three hits within
+// about 1e-6 of each other) and short (everything beyond the window is culled).
 constexpr float kTieRel = 1e-6f;
+
+struct TieState {
+  float t_min;   // nearest hit so far (FLT_MAX: none)
+  bool amb;      // the window shrank past a hit this walk no longer knows
+  bool fixed;    // second walk: the window is final (t_cull), take the lowest key in it
+};
+
+__device__ __forceinline__ TieState tie_begin() {
+  TieState z;
+  z.t_min = FLT_MAX;
+  z.amb = false;
+  z.fixed = false;
+  return z;
+}
+
+// (surface, triangle, t) of a below (s, tr, t) of b
+__device__ __forceinline__ bool tie_key_less(uint32_t as, uint32_t atr, float at, uint32_t bs, uint32_t btr, float bt) {
+  return as < bs || (as == bs && (atr < btr || (atr == btr && at < bt)));
+}
+
+// One hit (t, surface s, triangle tr) into a near-tie walk's state; true when
+// it becomes the winner so far. t_cull follows the window.
+__device__ __forceinline__ bool tie_take(float t, uint32_t s, uint32_t tr, bool have, float t_best, float& t_cull,
+                                         uint32_t s_best, uint32_t tri_best, TieState& ts) {
+  bool take;
+  if (ts.fixed) {
+    take = t <= t_cull && (!have || tie_key_less(s, tr, t, s_best, tri_best, t_best));
+  } else if (!have) {
+    take = true;
+    ts.t_min = t;
+  } else if (t < ts.t_min) {
+    const float win = t * (1.0f + kTieRel);
+    if (t_best <= win) {
+      take = tie_key_less(s, tr, t, s_best, tri_best, t_best);
+    } else {
+      if (ts.t_min <= win) ts.amb = true;
+      take = true;
+    }
+    ts.t_min = t;
+  } else {
+    take = t <= t_cull && tie_key_less(s, tr, t, s_best, tri_best, t_best);
+  }
+  if (!ts.fixed) t_cull = ts.t_min * (1.0f + kTieRel);
+  return take;
+}
 
 template <bool TIE>
 __device__ __forceinline__ bool leaf_test(const float4* __restrict__ prims, int leaf, float ox, float oy, float oz,
                                           float dx, float dy, float dz, bool& have, float& t_best, float& t_cull,
-                                          int& prim_best, uint32_t& s_best, uint32_t& tri_best) {
+                                          int& prim_best, uint32_t& s_best, uint32_t& tri_best, TieState& ts) {
   const uint32_t code = ~(uint32_t)leaf;
   const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
   for (uint32_t i = start; i < end; i++) {
@@ -178,27 +238,21 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ prims, int 
     const float4 p2 = __ldg(prims + 3 * i + 2);
     float t;
     if (ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) {
-      bool take;
       if (!TIE) {
-        take = !have || t < t_best;
-      } else if (!have || t < t_best * (1.0f - kTieRel)) {
-        take = true;
-      } else if (t <= t_cull) {
-        const uint32_t s = __float_as_uint(p2.w), tr = __float_as_uint(p1.w);
-        take = s < s_best || (s == s_best && tr < tri_best);
-      } else {
-        take = false;
-      }
-      if (take) {
-        have = true;
-        t_best = t;
-        prim_best = (int)i;
-        if (TIE) {
-          t_cull = t * (1.0f + kTieRel);
-          s_best = __float_as_uint(p2.w);
-          tri_best = __float_as_uint(p1.w);
-        } else {
+        if (!have || t < t_best) {
+          have = true;
+          t_best = t;
+          prim_best = (int)i;
           t_cull = t;
+        }
+      } else {
+        const uint32_t s = __float_as_uint(p2.w), tr = __float_as_uint(p1.w);
+        if (tie_take(t, s, tr, have, t_best, t_cull, s_best, tri_best, ts)) {
+          have = true;
+          t_best = t;
+          prim_best = (int)i;
+          s_best = s;
+          tri_best = tr;
         }
       }
     }
@@ -218,100 +272,118 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
   if (S.n_prims == 0) return false;
   constexpr int kDone = 0x7FFFFFFF;  // never a node index (< 2^28)
   const float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
-  const float4* __restrict__ nodes = S.nodes;
+  // near-tie walks use the grown boxes (DScene::nodes_f): they find every hit
+  // of every primitive, whatever the tree (the exact test on them)
+  const float4* __restrict__ nodes = (TIE && S.nodes_f) ? S.nodes_f : S.nodes;
   const float4* __restrict__ prims = S.prims;
   bool have = false;
   t_best = FLT_MAX;
-  float t_cull = FLT_MAX;            // TIE: best * (1 + 1e-6); else best
+  float t_cull = FLT_MAX;            // TIE: t_min * (1 + 1e-6); else best; FLT_MAX before the first hit
   uint32_t s_best = 0, tri_best = 0;
+  TieState ts = tie_begin();
   int stack_ref[STACK_DEPTH];
   float stack_t[STACK_DEPTH];
   int sp = 0;
   int cur = S.root;
   int leaf = 0;                      // postponed leaf (< 0), or 0
-  // every node and leaf is visited at most once per ray: a walk longer than
-  // this bound means a corrupt tree; stop and flag it rather than spin
+  // every node and leaf is visited at most once per ray and pass: a walk
+  // longer than this bound means a corrupt tree; stop and flag it rather than spin
   uint32_t budget = 2u * S.n_nodes + S.n_prims + 64u;
+  auto culled = [&](float t) { return TIE ? t > t_cull : (have && t >= t_best); };
   // next stacked entry that is not culled, or kDone
   auto pop = [&]() -> int {
     while (sp > 0) {
       sp--;
-      if (have && (TIE ? stack_t[sp] > t_cull : stack_t[sp] >= t_best)) continue;
+      if (culled(stack_t[sp])) continue;
       return stack_ref[sp];
     }
     return kDone;
   };
-  while (cur != kDone || leaf < 0) {
-    // ---- internal nodes
-    while (cur >= 0 && cur != kDone) {
-      if (budget-- == 0u) {
-        atomicOr(err, 4u);
-        return have;
-      }
-      const float4 n0 = __ldg(nodes + 4 * cur + 0);
-      const float4 n1 = __ldg(nodes + 4 * cur + 1);
-      const float4 n2 = __ldg(nodes + 4 * cur + 2);
-      const float4 n3 = __ldg(nodes + 4 * cur + 3);
-      const float tmax = have ? t_cull : FLT_MAX;
-      float ta, tb;
-      const bool h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ox, oy, oz, ix, iy, iz, tmax, ta);
-      const bool h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ox, oy, oz, ix, iy, iz, tmax, tb);
-      const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-      if (h0 && h1) {
-        int nr, fr;
-        float nt, ft;
-        if (ta <= tb) { nr = c0; nt = ta; fr = c1; ft = tb; }
-        else { nr = c1; nt = tb; fr = c0; ft = ta; }
-        if (sp < STACK_DEPTH) {
-          stack_ref[sp] = fr;
-          stack_t[sp] = ft;
-          sp++;
-        } else {
-          atomicOr(err, 1u);
-        }
-        cur = (have && (TIE ? nt > t_cull : nt >= t_best)) ? pop() : nr;
-      } else if (h0) {
-        cur = (have && (TIE ? ta > t_cull : ta >= t_best)) ? pop() : c0;
-      } else if (h1) {
-        cur = (have && (TIE ? tb > t_cull : tb >= t_best)) ? pop() : c1;
-      } else {
-        cur = pop();
-      }
-      if (TIE) {
-        if (cur < 0 && leaf == 0) {  // postpone the leaf, keep descending
-          leaf = cur;
-          cur = pop();
-        }
-        if (__all_sync(__activemask(), leaf < 0 || cur == kDone)) break;
-      }
-    }
-    // ---- leaves (the postponed one, then any leaf the stack yields next)
-    if (!TIE) {
-      if (cur == kDone) break;
-      if (budget-- == 0u) {
-        atomicOr(err, 4u);
-        return have;
-      }
-      leaf_test<TIE>(prims, cur, ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best);
-      cur = pop();
-    } else {
-      if (leaf == 0 && cur < 0) {  // a leaf reached outside the node loop (e.g. a leaf root)
-        leaf = cur;
-        cur = pop();
-      }
-      while (leaf < 0) {
+  while (true) {
+    while (cur != kDone || leaf < 0) {
+      // ---- internal nodes
+      while (cur >= 0 && cur != kDone) {
         if (budget-- == 0u) {
           atomicOr(err, 4u);
           return have;
         }
-        leaf_test<TIE>(prims, leaf, ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best);
-        leaf = 0;
-        if (cur < 0) {
+        const float4 n0 = __ldg(nodes + 4 * cur + 0);
+        const float4 n1 = __ldg(nodes + 4 * cur + 1);
+        const float4 n2 = __ldg(nodes + 4 * cur + 2);
+        const float4 n3 = __ldg(nodes + 4 * cur + 3);
+        const float tmax = t_cull;
+        float ta, tb;
+        const bool h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ox, oy, oz, ix, iy, iz, tmax, ta);
+        const bool h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ox, oy, oz, ix, iy, iz, tmax, tb);
+        const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+        if (h0 && h1) {
+          int nr, fr;
+          float nt, ft;
+          if (ta <= tb) { nr = c0; nt = ta; fr = c1; ft = tb; }
+          else { nr = c1; nt = tb; fr = c0; ft = ta; }
+          if (sp < STACK_DEPTH) {
+            stack_ref[sp] = fr;
+            stack_t[sp] = ft;
+            sp++;
+          } else {
+            atomicOr(err, 1u);
+          }
+          cur = culled(nt) ? pop() : nr;
+        } else if (h0) {
+          cur = culled(ta) ? pop() : c0;
+        } else if (h1) {
+          cur = culled(tb) ? pop() : c1;
+        } else {
+          cur = pop();
+        }
+        if (TIE) {
+          if (cur < 0 && leaf == 0) {  // postpone the leaf, keep descending
+            leaf = cur;
+            cur = pop();
+          }
+          if (__all_sync(__activemask(), leaf < 0 || cur == kDone)) break;
+        }
+      }
+      // ---- leaves (the postponed one, then any leaf the stack yields next)
+      if (!TIE) {
+        if (cur == kDone) break;
+        if (budget-- == 0u) {
+          atomicOr(err, 4u);
+          return have;
+        }
+        leaf_test<TIE>(prims, cur, ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best, ts);
+        cur = pop();
+      } else {
+        if (leaf == 0 && cur < 0) {  // a leaf reached outside the node loop (e.g. a leaf root)
           leaf = cur;
           cur = pop();
         }
+        while (leaf < 0) {
+          if (budget-- == 0u) {
+            atomicOr(err, 4u);
+            return have;
+          }
+          leaf_test<TIE>(prims, leaf, ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best,
+                         ts);
+          leaf = 0;
+          if (cur < 0) {
+            leaf = cur;
+            cur = pop();
+          }
+        }
       }
     }
+    if (!TIE || !ts.amb || ts.fixed) break;
+    // the near-tie window shrank past a hit this walk no longer knows: walk
+    // once more with the final window
+    ts.fixed = true;
+    t_cull = ts.t_min * (1.0f + kTieRel);
+    have = false;
+    t_best = FLT_MAX;
+    sp = 0;
+    cur = S.root;
+    leaf = 0;
+    budget = 2u * S.n_nodes + S.n_prims + 64u;
   }
   return have;
 }
@@ -321,20 +393,20 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
 // children at once and descends into the nearest hit internal child, pushing
 // the others farthest first. Because the tie rule makes the winner
 // independent of the visit order and a box is skipped only beyond
-// best * (1 + 1e-6), the hit is the one the binary walk finds (up to chains of
-// near-ties, which neither walk orders the reference's way).
+// the window, the hit is the one the binary walk finds: the near-tie rule
+// depends only on the set of hits (TieState).
 //
 // One node step; returns the next node, or kDone4 once the stack is empty.
 constexpr int kDone4 = 0x7FFFFFFF;
 __device__ __forceinline__ int bvh4_step(const float4* __restrict__ nodes, const float4* __restrict__ prims, int cur,
                                          float ox, float oy, float oz, float dx, float dy, float dz, float ix,
                                          float iy, float iz, bool& have, float& t_best, float& t_cull,
-                                         int& prim_best, uint32_t& s_best, uint32_t& tri_best, int* stack_ref,
-                                         float* stack_t, int& sp, uint32_t* err) {
+                                         int& prim_best, uint32_t& s_best, uint32_t& tri_best, TieState& ts,
+                                         int* stack_ref, float* stack_t, int& sp, uint32_t* err) {
   const float4* nd = nodes + 8 * cur;
   const float4 lx = __ldg(nd + 0), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
   const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5), rf = __ldg(nd + 6);
-  const float tmax = have ? t_cull : FLT_MAX;
+  const float tmax = t_cull;
   const float blx[4] = {lx.x, lx.y, lx.z, lx.w}, bhx[4] = {hx.x, hx.y, hx.z, hx.w};
   const float bly[4] = {ly.x, ly.y, ly.z, ly.w}, bhy[4] = {hy.x, hy.y, hy.z, hy.w};
   const float blz[4] = {lz.x, lz.y, lz.z, lz.w}, bhz[4] = {hz.x, hz.y, hz.z, hz.w};
@@ -358,8 +430,8 @@ __device__ __forceinline__ int bvh4_step(const float4* __restrict__ nodes, const
     for (int j = 0; j < 4; j++)
       if (r[j] < 0 && t[j] <= bt) { bt = t[j]; bk = j; }
     if (bk < 0) break;
-    if (!have || bt <= t_cull)
-      leaf_test<true>(prims, r[bk], ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best);
+    if (bt <= t_cull)
+      leaf_test<true>(prims, r[bk], ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best, ts);
     r[bk] = kDone4;
     t[bk] = FLT_MAX;
   }
@@ -374,14 +446,14 @@ __device__ __forceinline__ int bvh4_step(const float4* __restrict__ nodes, const
   cswap(0, 1); cswap(2, 3); cswap(0, 2); cswap(1, 3); cswap(1, 2);
 #pragma unroll
   for (int k = 3; k >= 1; k--) {
-    if (r[k] == kDone4 || (have && t[k] > t_cull)) continue;
+    if (r[k] == kDone4 || t[k] > t_cull) continue;
     if (sp < STACK_DEPTH) { stack_ref[sp] = r[k]; stack_t[sp] = t[k]; sp++; }
     else atomicOr(err, 1u);
   }
-  int nxt = (r[0] == kDone4 || (have && t[0] > t_cull)) ? kDone4 : r[0];
+  int nxt = (r[0] == kDone4 || t[0] > t_cull) ? kDone4 : r[0];
   while (nxt == kDone4 && sp > 0) {
     sp--;
-    if (have && stack_t[sp] > t_cull) continue;
+    if (stack_t[sp] > t_cull) continue;
     nxt = stack_ref[sp];
   }
   return nxt;
@@ -395,18 +467,30 @@ __device__ __forceinline__ bool mesh_closest4(const DScene& S, float ox, float o
   bool have = false;
   float t_cull = FLT_MAX;
   uint32_t s_best = 0, tri_best = 0;
+  TieState ts = tie_begin();
   int stack_ref[STACK_DEPTH];
   float stack_t[STACK_DEPTH];
   int sp = 0;
   int cur = S.root4;
-  uint32_t budget = S.n_nodes4 + 1u;   // every node is entered at most once
-  while (cur != kDone4) {
-    if (budget-- == 0u) {
-      atomicOr(err, 4u);
-      return have;
+  uint32_t budget = S.n_nodes4 + 1u;   // every node is entered at most once per pass
+  while (true) {
+    while (cur != kDone4) {
+      if (budget-- == 0u) {
+        atomicOr(err, 4u);
+        return have;
+      }
+      cur = bvh4_step(S.nodes4, S.prims, cur, ox, oy, oz, dx, dy, dz, ix, iy, iz, have, t_best, t_cull, prim_best,
+                      s_best, tri_best, ts, stack_ref, stack_t, sp, err);
     }
-    cur = bvh4_step(S.nodes4, S.prims, cur, ox, oy, oz, dx, dy, dz, ix, iy, iz, have, t_best, t_cull, prim_best,
-                    s_best, tri_best, stack_ref, stack_t, sp, err);
+    if (!ts.amb || ts.fixed) break;
+    // a second walk with the final near-tie window (see TieState)
+    ts.fixed = true;
+    t_cull = ts.t_min * (1.0f + kTieRel);
+    have = false;
+    t_best = FLT_MAX;
+    sp = 0;
+    cur = S.root4;
+    budget = S.n_nodes4 + 1u;
   }
   return have;
 }

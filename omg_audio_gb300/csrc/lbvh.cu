@@ -353,10 +353,10 @@ namespace {
 // Child boxes of every binary node grown by 2^-19 m[a] on each side, rounded
 // outward (DScene::nodes_f).
 __global__ void grow_nodes_kernel(const float4* __restrict__ in, float4* __restrict__ out, uint32_t n, float mx,
-                                  float my, float mz) {
+                                  float my, float mz, float pad) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const float g[3] = {ldexpf(mx, -19), ldexpf(my, -19), ldexpf(mz, -19)};
+  const float g[3] = {__fadd_ru(ldexpf(mx, -19), pad), __fadd_ru(ldexpf(my, -19), pad), __fadd_ru(ldexpf(mz, -19), pad)};
   float v[16];
   for (int i = 0; i < 4; i++) {
     const float4 q = in[4 * k + i];
@@ -371,9 +371,10 @@ __global__ void grow_nodes_kernel(const float4* __restrict__ in, float4* __restr
 }
 }  // namespace
 
-cudaError_t grow_nodes(const float4* nodes, float4* out, uint32_t n_nodes, const float m[3], cudaStream_t s) {
+cudaError_t grow_nodes(const float4* nodes, float4* out, uint32_t n_nodes, const float m[3], float pad,
+                       cudaStream_t s) {
   if (n_nodes == 0) return cudaSuccess;
-  grow_nodes_kernel<<<(n_nodes + 255) / 256, 256, 0, s>>>(nodes, out, n_nodes, m[0], m[1], m[2]);
+  grow_nodes_kernel<<<(n_nodes + 255) / 256, 256, 0, s>>>(nodes, out, n_nodes, m[0], m[1], m[2], pad);
   return cudaGetLastError();
 }
 

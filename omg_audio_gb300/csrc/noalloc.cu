@@ -63,13 +63,13 @@ __global__ void noalloc_setup_kernel(float* scratch, DJob job, WallMats walls, u
   }
 }
 
-// sum + comp into the caller's buffers
+// (sum + comp) * 2^-64 into the caller's buffers (the accumulators are scaled, kAccScale)
 __global__ void noalloc_finalize_kernel(const float* scratch, uint32_t n_bins, uint32_t nb, float* bins,
                                         float* dirs) {
   const uint32_t nbb = n_bins * nb, nd = n_bins * 3;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nbb + nd; i += gridDim.x * blockDim.x) {
-    if (i < nbb) bins[i] = scratch[i] + scratch[nbb + i];
-    else dirs[i - nbb] = scratch[2 * nbb + (i - nbb)] + scratch[2 * nbb + nd + (i - nbb)];
+    if (i < nbb) bins[i] = (scratch[i] + scratch[nbb + i]) * kAccUnscale;
+    else dirs[i - nbb] = (scratch[2 * nbb + (i - nbb)] + scratch[2 * nbb + nd + (i - nbb)]) * kAccUnscale;
   }
 }
 

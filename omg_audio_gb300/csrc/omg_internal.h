@@ -61,10 +61,12 @@ struct DScene {
   // children over 4 lanes: 32 B per child, child k of node n at float4 index
   // 8 n + 2 k: (lo.x, lo.y, lo.z, hi.x), (hi.y, hi.z, ref bits, 0).
   const float4* nodes4c;
-  // `nodes` with every child box grown by 2^-19 M_a on each side (M_a: the
-  // scene's largest |coordinate| along axis a, plus 1 m), for the fused
-  // multiply-add slab test of near-tie walks whose origin lies within
-  // |o_a| <= 7 M_a (device_common.cuh:ray_aabb_fma); null: exact test only.
+  // `nodes` with every child box grown by 2^-19 M_a + pad on each side (M_a:
+  // the scene's largest |coordinate| along axis a, plus 1 m; pad: 2^-17 x the
+  // longest primitive edge), for the near-tie walks: the fused multiply-add
+  // slab test of walks whose origin lies within |o_a| <= 7 M_a
+  // (device_common.cuh:ray_aabb_fma), and a margin that holds every hit
+  // Möller–Trumbore accepts just outside a triangle; null: a leaf root.
   const float4* nodes_f;
   float fast_m[3];
 };
@@ -127,6 +129,11 @@ struct alignas(16) DLaunch {
   uint32_t pad[2];
 };
 
+// Histogram accumulators hold values scaled by 2^64 (exact): the float
+// atomics flush subnormals, and scaled values of energies down to 2^-149 stay
+// normal. Finalizing multiplies by 2^-64, exact wherever the result is normal.
+constexpr float kAccScale = 18446744073709551616.0f;        // 2^64
+constexpr float kAccUnscale = 5.42101086242752217e-20f;     // 2^-64
 // Accumulator block of one job (all float, compensated pairs):
 //   bins_s[n_bins*nb], bins_c[n_bins*nb], dirs_s[n_bins*3], dirs_c[n_bins*3]
 inline uint64_t acc_floats(uint32_t n_bins, uint32_t nb) { return 2ull * n_bins * (nb + 3); }
@@ -250,8 +257,10 @@ cudaError_t launch_late_update(const DLateUpdate* up, uint32_t n_up, const float
 cudaError_t lbvh_build(const float4* prims_in, uint32_t n_prims, float4* prims_out, float4* nodes_out,
                        int32_t* root_ref, void* scratch, size_t scratch_bytes, cudaStream_t s);
 size_t lbvh_scratch_bytes(uint32_t n_prims);
-// DScene::nodes_f from `nodes` on the device (m: the bound of |coordinate| per axis)
-cudaError_t grow_nodes(const float4* nodes, float4* out, uint32_t n_nodes, const float m[3], cudaStream_t s);
+// DScene::nodes_f from `nodes` on the device (m: the bound of |coordinate| per
+// axis; pad: near_tie_pad of the primitives)
+cudaError_t grow_nodes(const float4* nodes, float4* out, uint32_t n_nodes, const float m[3], float pad,
+                       cudaStream_t s);
 
 // dome.cu
 struct DDomePanel {

@@ -608,7 +608,7 @@ int32_t flatten_bvh4(const std::vector<float>& ref_boxes, const std::vector<uint
   return 0;
 }
 
-void grow_nodes_for_fma(const std::vector<float>& dev_nodes, std::vector<float>& out, float m[3]) {
+void grow_nodes_for_fma(const std::vector<float>& dev_nodes, std::vector<float>& out, float m[3], float pad) {
   const size_t n = dev_nodes.size() / 16;
   // child box c of node k: lo at 16k + 6c + {0,1,2}, hi at 16k + 6c + {3,4,5}
   float mx[3] = {0.0f, 0.0f, 0.0f};
@@ -623,12 +623,37 @@ void grow_nodes_for_fma(const std::vector<float>& dev_nodes, std::vector<float>&
   for (size_t k = 0; k < n; k++)
     for (int c = 0; c < 2; c++)
       for (int a = 0; a < 3; a++) {
-        const float grow = std::ldexp(m[a], -19);
+        const float grow = std::ldexp(m[a], -19) + pad;
         float& lo = out[16 * k + 6 * c + a];
         float& hi = out[16 * k + 6 * c + 3 + a];
         lo = std::nextafter(lo - grow, -INFINITY);
         hi = std::nextafter(hi + grow, INFINITY);
       }
+}
+
+void grow_ref_boxes(std::vector<float>& boxes, const float m[3], float pad) {
+  for (size_t k = 0; k < boxes.size() / 6; k++)
+    for (int a = 0; a < 3; a++) {
+      const float grow = std::ldexp(m[a], -19) + pad;
+      boxes[6 * k + a] = std::nextafter(boxes[6 * k + a] - grow, -INFINITY);
+      boxes[6 * k + 3 + a] = std::nextafter(boxes[6 * k + 3 + a] + grow, INFINITY);
+    }
+}
+
+float near_tie_pad(const std::vector<float>& prim_geo) {
+  // 2^-17 x the longest primitive edge: Möller–Trumbore accepts barycentrics
+  // down to -1e-6 (mesh.rs:446-451), i.e. hits up to about 2e-6 x the
+  // edge lengths outside the triangle, beyond its exact bounding box
+  double e = 0.0;
+  for (size_t i = 0; i < prim_geo.size() / 9; i++) {
+    const float* g = &prim_geo[9 * i];
+    const double e1 = std::sqrt((double)g[3] * g[3] + (double)g[4] * g[4] + (double)g[5] * g[5]);
+    const double e2 = std::sqrt((double)g[6] * g[6] + (double)g[7] * g[7] + (double)g[8] * g[8]);
+    const double e3 = std::sqrt(((double)g[6] - g[3]) * ((double)g[6] - g[3]) + ((double)g[7] - g[4]) * ((double)g[7] - g[4]) +
+                                ((double)g[8] - g[5]) * ((double)g[8] - g[5]));
+    e = std::max(e, std::max(e1, std::max(e2, e3)));
+  }
+  return (float)std::ldexp(e, -17);
 }
 
 // mesh.rs:458-461 per original triangle; .w carries the material id bits.

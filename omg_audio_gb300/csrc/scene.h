@@ -60,11 +60,18 @@ int32_t flatten_bvh2(const std::vector<float>& ref_boxes, const std::vector<uint
 // walk of it can need.
 int32_t flatten_bvh4(const std::vector<float>& ref_boxes, const std::vector<uint32_t>& ref_ab,
                      std::vector<float>& dev_nodes, uint32_t* max_stack);
-// The binary nodes (flatten_bvh2 layout) with every child box grown for the
-// fused multiply-add slab test: by 2^-19 m[a] on each side, rounded outward,
-// where m[a] bounds |coordinate| along axis a of the scene (filled here: the
-// largest |box coordinate| plus 1 m).
-void grow_nodes_for_fma(const std::vector<float>& dev_nodes, std::vector<float>& out, float m[3]);
+// The binary nodes (flatten_bvh2 layout) with every child box grown by
+// 2^-19 m[a] + pad on each side, rounded outward, where m[a] bounds
+// |coordinate| along axis a of the scene (filled here: the largest |box
+// coordinate| plus 1 m). The first term covers the rounding of the fused
+// multiply-add slab test; pad (near_tie_pad) covers the hits Möller–Trumbore
+// accepts just outside a triangle, so that walks on these boxes find every
+// hit of every primitive.
+void grow_nodes_for_fma(const std::vector<float>& dev_nodes, std::vector<float>& out, float m[3], float pad);
+// The same growth on reference-form boxes (6 floats each).
+void grow_ref_boxes(std::vector<float>& boxes, const float m[3], float pad);
+// 2^-17 x the longest primitive edge (prim_geo: a, e1, e2 per primitive).
+float near_tie_pad(const std::vector<float>& prim_geo);
 void tri_normals(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
                  std::vector<float>& out);
 DMat make_dmat(const omg_material& m, uint32_t nb);

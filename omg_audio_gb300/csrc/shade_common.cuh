@@ -10,7 +10,11 @@ namespace omg {
 // Compensated accumulation: the atomic returns the old value, so the exact
 // rounding error of the add it performed is recovered with TwoSum (Knuth)
 // and accumulated in a second float. sum + comp carries ~2x the f32 precision.
+// Values are accumulated scaled by 2^64 (kAccScale, exact): float atomics
+// flush subnormal operands and results to zero, and a band whose energy has
+// decayed below 2^-126 must still add up as the reference's f32 sums do.
 __device__ __forceinline__ void acc_add(float* s, float* c, float x) {
+  x = x * kAccScale;
   float old = atomicAdd(s, x);
   float sum = old + x;
   float bp = sum - old;

@@ -33,6 +33,7 @@ struct Walk {
   float t_best, t_cull;
   uint32_t s_best, tri_best;
   int prim_best;
+  TieState ts;           // near-tie state (TIE walks)
   float ix, iy, iz;
   bool fast;             // origin within the grown boxes' margin (else every box counts as hit)
   uint32_t budget;
@@ -50,7 +51,7 @@ template <bool TIE>
 __device__ __forceinline__ int walk_pop(Walk& w) {
   while (w.sp > 0) {
     w.sp--;
-    if (w.have && (TIE ? w.stack_t[w.sp] > w.t_cull : w.stack_t[w.sp] >= w.t_best)) continue;
+    if (TIE ? w.stack_t[w.sp] > w.t_cull : (w.have && w.stack_t[w.sp] >= w.t_best)) continue;
     return w.stack_ref[w.sp];
   }
   return kDone;
@@ -70,33 +71,59 @@ __device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float ox, f
   w.s_best = 0;
   w.tri_best = 0;
   w.prim_best = 0;
+  w.ts = tie_begin();
   w.ix = __frcp_rn(dx);
   w.iy = __frcp_rn(dy);
   w.iz = __frcp_rn(dz);
-  // the margin 2^-19 M_a covers the slab test's rounding for |o_a| <= 7 M_a
-  w.fast = fabsf(ox) <= 7.0f * S.fast_m[0] && fabsf(oy) <= 7.0f * S.fast_m[1] && fabsf(oz) <= 7.0f * S.fast_m[2];
+  // the margin 2^-19 M_a covers the fma slab test's rounding for |o_a| <= 7 M_a;
+  // the test also needs finite products (no direction component near 0)
+  const float kTiny = 8.673617379884035e-19f;   // 2^-60
+  w.fast = fabsf(ox) <= 7.0f * S.fast_m[0] && fabsf(oy) <= 7.0f * S.fast_m[1] && fabsf(oz) <= 7.0f * S.fast_m[2] &&
+           fabsf(dx) >= kTiny && fabsf(dy) >= kTiny && fabsf(dz) >= kTiny;
   w.budget = 2u * S.n_nodes + S.n_prims + 64u;
+}
+
+// A near-tie walk that ended with an ambiguous window (TieState::amb) starts
+// over in fixed mode from `root`: the caller keeps walking.
+__device__ __forceinline__ bool walk_restart_fixed(Walk& w, int root, uint32_t budget) {
+  if (!w.ts.amb || w.ts.fixed) return false;
+  w.ts.fixed = true;
+  w.t_cull = w.ts.t_min * (1.0f + kTieRel);
+  w.have = false;
+  w.t_best = FLT_MAX;
+  w.cur = root;
+  w.leaf = 0;
+  w.sp = 0;
+  w.budget = budget;
+  return true;
 }
 
 // Up to `steps` node steps of the 4-wide walk (mesh_closest4 in pieces).
 __device__ __forceinline__ bool walk4_steps(Walk& w, const DScene& S, float ox, float oy, float oz, float dx,
                                             float dy, float dz, int steps, uint32_t* err) {
-  while (steps-- > 0 && w.cur != kDone) {
+  while (steps-- > 0) {
+    if (w.cur == kDone) {
+      if (!walk_restart_fixed(w, S.root4, 2u * S.n_nodes + S.n_prims + 64u)) break;
+      continue;
+    }
     if (w.budget-- == 0u) {
       atomicOr(err, 4u);
       w.cur = kDone;
+      w.ts.amb = false;
       break;
     }
     w.cur = bvh4_step(S.nodes4, S.prims, w.cur, ox, oy, oz, dx, dy, dz, w.ix, w.iy, w.iz, w.have, w.t_best,
-                      w.t_cull, w.prim_best, w.s_best, w.tri_best, w.stack_ref, w.stack_t, w.sp, err);
+                      w.t_cull, w.prim_best, w.s_best, w.tri_best, w.ts, w.stack_ref, w.stack_t, w.sp, err);
   }
+  if (w.cur == kDone) walk_restart_fixed(w, S.root4, 2u * S.n_nodes + S.n_prims + 64u);
   return w.cur == kDone;
 }
 
 // The near-tie walk (TIE = true): speculative while-while over the grown
 // boxes with the fused multiply-add slab test. A ray whose origin lies beyond
 // the boxes' margin (|o_a| > 7 M_a: never in a trace that starts inside the
-// scene) takes every box as hit and walks the whole tree: slow, still exact.
+// scene) or that runs along a coordinate plane (a direction component of 0)
+// uses the plain slab test on the same grown boxes.
 __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, float oy, float oz, float dx,
                                           float dy, float dz, int steps, uint32_t* err) {
   // speculative while-while: descend, postponing one leaf, until every lane of
@@ -115,17 +142,16 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
     const float4 n1 = __ldg(tnodes + 4 * w.cur + 1);
     const float4 n2 = __ldg(tnodes + 4 * w.cur + 2);
     const float4 n3 = __ldg(tnodes + 4 * w.cur + 3);
-    const float tmax = w.have ? w.t_cull : FLT_MAX;
+    const float tmax = w.t_cull;   // FLT_MAX before the first hit; the final window in fixed mode
     float ta, tb;
     bool h0, h1;
-    {
+    if (w.fast) {
       const float oix = ox * w.ix, oiy = oy * w.iy, oiz = oz * w.iz;
       h0 = ray_aabb_fma(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, oix, oiy, oiz, w.ix, w.iy, w.iz, tmax, ta);
       h1 = ray_aabb_fma(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, oix, oiy, oiz, w.ix, w.iy, w.iz, tmax, tb);
-      if (!w.fast) {
-        h0 = h1 = true;
-        ta = tb = 0.0f;
-      }
+    } else {
+      h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ox, oy, oz, w.ix, w.iy, w.iz, tmax, ta);
+      h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ox, oy, oz, w.ix, w.iy, w.iz, tmax, tb);
     }
     const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
     if (h0 && h1) {
@@ -167,14 +193,18 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
       return true;
     }
     leaf_test<true>(prims, w.leaf, ox, oy, oz, dx, dy, dz, w.have, w.t_best, w.t_cull, w.prim_best, w.s_best,
-                   w.tri_best);
+                    w.tri_best, w.ts);
     w.leaf = 0;
     if (w.cur < 0) {
       w.leaf = w.cur;
       w.cur = walk_pop<true>(w);
     }
   }
-  return w.cur == kDone && w.leaf == 0;
+  if (w.cur == kDone && w.leaf == 0) {
+    // an ambiguous near-tie window: the walk starts over in fixed mode
+    return !walk_restart_fixed(w, S.root, 2u * S.n_nodes + S.n_prims + 64u);
+  }
+  return false;
 }
 
 // Up to `steps` node visits / leaf tests; returns true when the walk is done.
@@ -224,7 +254,7 @@ __device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, f
         }
       } else {
         leaf_test<TIE>(prims, w.cur, ox, oy, oz, dx, dy, dz, w.have, w.t_best, w.t_cull, w.prim_best, w.s_best,
-                       w.tri_best);
+                       w.tri_best, w.ts);
         w.cur = walk_pop<TIE>(w);
       }
     }
@@ -607,7 +637,7 @@ __global__ void __launch_bounds__(256, 4) trace_wl_kernel(const DJob* __restrict
   }
 }
 
-// out = sum + comp per float, bins then dirs, per job.
+// out = (sum + comp) * 2^-64 per float, bins then dirs, per job.
 __global__ void finalize_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs, const float* __restrict__ acc,
                                 float* __restrict__ out) {
   const uint32_t j = blockIdx.y;
@@ -620,7 +650,7 @@ __global__ void finalize_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs, 
     float v;
     if (i < nbb) v = A[i] + A[nbb + i];
     else v = A[2 * nbb + (i - nbb)] + A[2 * nbb + nd + (i - nbb)];
-    O[i] = v;
+    O[i] = v * kAccUnscale;
   }
 }
 

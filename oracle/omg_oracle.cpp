@@ -327,6 +327,38 @@ uint32_t orc_trace_mesh_log(int real, void* hv, const TraceParams* P, const floa
   return (uint32_t)lt.size();
 }
 
+// The same log for a trace with panels and the context's near-tie rule
+// (P->tie_mode), f32 only: the segments the tracer itself walks.
+uint32_t orc_trace_mesh_log_panels(void* hv, const BoxPanelC* panels, uint32_t n_panels, const TraceParams* P,
+                                   const float* src, const float* lis, uint32_t n_rays, const float* energy,
+                                   uint32_t seed, uint32_t ray_begin, uint32_t ray_end, float* seg_out,
+                                   uint32_t* tri_out, uint32_t cap) {
+  MeshHandle* h = (MeshHandle*)hv;
+  if (h->real != 0) return 0;
+  std::vector<uint32_t> lt;
+  std::vector<float> ls;
+  size_t nbin = (size_t)P->n_bins * P->n_bands;
+  std::vector<float> bins(nbin), dirs(P->n_bins * 3);
+  auto pn = panels_of<float>(panels, n_panels);
+  const Mesh<float>& m = h->mf;
+  auto fn = [&](const V3<float>& p, const V3<float>& d, GeomHit<float>* g, uint32_t* tri, TraversalStats* st) {
+    TieMesh<float> tm{&m, P->tie_mode != 0};
+    if (pn.empty()) return tm.raycast_hit(p, d, g, st, tri);
+    return with_panels_hit<float>(tm, pn, p, d, g, st);
+  };
+  V3<float> s = from_f<float>(src), l = from_f<float>(lis);
+  for (uint32_t r = ray_begin; r < ray_end; r++) {
+    PcgRay g(seed, r);
+    trace_ray<float, float>(fn, *P, s, l, 1.0f / (float)n_rays, energy, g, bins.data(), dirs.data(), nullptr, &lt,
+                            &ls);
+  }
+  for (size_t i = 0; i < lt.size() && i < cap; i++) {
+    tri_out[i] = lt[i];
+    for (int k = 0; k < 6; k++) seg_out[6 * i + k] = ls[6 * i + k];
+  }
+  return (uint32_t)lt.size();
+}
+
 // ---------------------------------------------------------------- reverb
 // tracer.rs:204-257. level_f32 != 0 sums the late energy in f32 as the
 // reference does; 0 sums it in double (FP64 oracle).

@@ -372,7 +372,21 @@ struct Mesh {
     size_t n = prims.size();
     build_node(prims, 0, n);
     packed.swap(prims);
+    // near-tie walks test boxes grown by 2^-19 M_a + 2^-17 x the longest
+    // primitive edge (M_a: the largest |box coordinate| on axis a plus 1 m), so
+    // that they find every hit Möller–Trumbore accepts, even just outside a
+    // triangle's bounds; the CUDA walks grow theirs the same way
+    double mx[3] = {0, 0, 0}, e = 0;
+    for (const BvhNode<R>& nd : nodes)
+      for (int a = 0; a < 3; a++)
+        mx[a] = std::max(mx[a], std::max(std::fabs((double)nd.bmin.get(a)), std::fabs((double)nd.bmax.get(a))));
+    for (const PackedTri<R>& p : packed) {
+      const V3<R> e3 = p.e2 - p.e1;
+      e = std::max(e, std::max((double)p.e1.length(), std::max((double)p.e2.length(), (double)e3.length())));
+    }
+    for (int a = 0; a < 3; a++) tie_grow[a] = R(std::ldexp(mx[a] + 1.0, -19) + std::ldexp(e, -17));
   }
+  R tie_grow[3] = {0, 0, 0};
 
   // mesh.rs:292-405 — 16-bin SAH on the widest centroid axis, leaf <= 4,
   // median fallback, stable two-pointer partition.
@@ -514,77 +528,111 @@ struct Mesh {
   // (node, t_enter), near child on top, strict `<` (first found wins ties).
   // Returns the ORIGINAL triangle id.
   //
-  // tie = true: a hit within a relative t-gap of 1e-6 of the best replaces it
-  // only with a lower authored surface id (then original triangle id), and
-  // nodes are culled only beyond best * (1 + 1e-6) — the precision-independent
-  // near-tie rule (the one segment_hits applies to crossings, mesh.rs:583-602).
+  // tie = true: the precision-independent near-tie rule. Among all hits, let
+  // t_min be the nearest; the hits within t_min * (1 + 1e-6) are near-ties of
+  // it, and the winner is the lowest (authored surface id, original triangle
+  // id, t) among them — the rule segment_hits applies to crossings
+  // (mesh.rs:583-602), made a function of the set of hits alone. The walk
+  // keeps the exact t_min and the winner so far and culls beyond
+  // t_min * (1 + 1e-6); when a nearer hit shrinks the window past the winner
+  // while an earlier hit may still be inside, it walks once more with the
+  // final window (`fixed`) and takes the lowest key in it. The CUDA walks do
+  // the same, so both find the same hit whatever their trees and orders.
   bool raycast(const V3<R>& o, const V3<R>& d, R* tout, uint32_t* triout, TraversalStats* st = nullptr,
                bool tie = false) const {
     if (nodes.empty()) return false;
     V3<R> inv_d(R(1) / d.x, R(1) / d.y, R(1) / d.z);
     const R rel = R(1e-6f);
-    bool have = false;
-    R bt = 0, bcull = 0;
+    const R RMAX = R(std::numeric_limits<float>::max());
+    bool have = false, fixed = false, amb = false;
+    R bt = 0, bcull = RMAX, tmin = RMAX;
     uint32_t btri = 0, bsurf = 0;
-    uint32_t sn[64];
-    R stt[64];
-    size_t sp = 1;
-    sn[0] = 0; stt[0] = 0;
-    while (sp > 0) {
-      sp--;
-      uint32_t ni = sn[sp];
-      R t_enter = stt[sp];
-      if (have && (tie ? t_enter > bcull : t_enter >= bt)) continue;
-      const BvhNode<R>& node = nodes[ni];
-      if (st) st->node_reads++;
-      if (node.a & LEAF_BIT) {
-        uint32_t start = node.a & ~LEAF_BIT;
-        for (uint32_t i = start; i < start + node.b; i++) {
-          const PackedTri<R>& pt = packed[i];
-          if (st) st->prim_tests++;
-          R t;
-          if (ray_tri_packed(pt.a, pt.e1, pt.e2, o, d, &t)) {
-            bool take;
-            if (!tie) {
-              take = !have || t < bt;
-            } else if (!have || t < bt * (R(1) - rel)) {
-              take = true;
-            } else if (t <= bcull) {
-              uint32_t s = tri_surface[pt.tri];
-              take = s < bsurf || (s == bsurf && pt.tri < btri);
-            } else {
-              take = false;
-            }
-            if (take) {
-              have = true;
-              bt = t;
-              btri = pt.tri;
-              bsurf = tri_surface[pt.tri];
-              bcull = tie ? t * (R(1) + rel) : t;
+    auto key_less = [](uint32_t as, uint32_t atr, R at, uint32_t bs, uint32_t btr, R btt) {
+      return as < bs || (as == bs && (atr < btr || (atr == btr && at < btt)));
+    };
+    for (int pass = 0; pass < 2; pass++) {
+      uint32_t sn[64];
+      R stt[64];
+      size_t sp = 1;
+      sn[0] = 0; stt[0] = 0;
+      while (sp > 0) {
+        sp--;
+        uint32_t ni = sn[sp];
+        R t_enter = stt[sp];
+        if (tie ? t_enter > bcull : (have && t_enter >= bt)) continue;
+        const BvhNode<R>& node = nodes[ni];
+        if (st) st->node_reads++;
+        if (node.a & LEAF_BIT) {
+          uint32_t start = node.a & ~LEAF_BIT;
+          for (uint32_t i = start; i < start + node.b; i++) {
+            const PackedTri<R>& pt = packed[i];
+            if (st) st->prim_tests++;
+            R t;
+            if (ray_tri_packed(pt.a, pt.e1, pt.e2, o, d, &t)) {
+              bool take;
+              const uint32_t s = tri_surface[pt.tri];
+              if (!tie) {
+                take = !have || t < bt;
+              } else if (fixed) {
+                take = t <= bcull && (!have || key_less(s, pt.tri, t, bsurf, btri, bt));
+              } else if (!have) {
+                take = true;
+                tmin = t;
+              } else if (t < tmin) {
+                const R win = t * (R(1) + rel);
+                if (bt <= win) {
+                  take = key_less(s, pt.tri, t, bsurf, btri, bt);
+                } else {
+                  if (tmin <= win) amb = true;
+                  take = true;
+                }
+                tmin = t;
+              } else {
+                take = t <= bcull && key_less(s, pt.tri, t, bsurf, btri, bt);
+              }
+              if (tie && !fixed) bcull = tmin * (R(1) + rel);
+              if (take) {
+                have = true;
+                bt = t;
+                btri = pt.tri;
+                bsurf = s;
+                if (!tie) bcull = t;
+              }
             }
           }
-        }
-      } else {
-        R tmax = have ? bcull : R(std::numeric_limits<float>::max());
-        const BvhNode<R>& l = nodes[node.a];
-        const BvhNode<R>& r = nodes[node.b];
-        if (st) st->node_reads += 2;
-        R ta, tb;
-        bool hl = ray_aabb(l.bmin, l.bmax, o, inv_d, tmax, &ta);
-        bool hr = ray_aabb(r.bmin, r.bmax, o, inv_d, tmax, &tb);
-        if (hl && hr) {
-          uint32_t nearn, farn; R nt, ft;
-          if (ta <= tb) { nearn = node.a; nt = ta; farn = node.b; ft = tb; }
-          else { nearn = node.b; nt = tb; farn = node.a; ft = ta; }
-          sn[sp] = farn; stt[sp] = ft;
-          sn[sp + 1] = nearn; stt[sp + 1] = nt;
-          sp += 2;
-        } else if (hl) {
-          sn[sp] = node.a; stt[sp] = ta; sp++;
-        } else if (hr) {
-          sn[sp] = node.b; stt[sp] = tb; sp++;
+        } else {
+          R tmax = (tie || have) ? bcull : RMAX;
+          const BvhNode<R>& l = nodes[node.a];
+          const BvhNode<R>& r = nodes[node.b];
+          if (st) st->node_reads += 2;
+          R ta, tb;
+          bool hl, hr;
+          if (tie) {
+            const V3<R> g(tie_grow[0], tie_grow[1], tie_grow[2]);
+            hl = ray_aabb(l.bmin - g, l.bmax + g, o, inv_d, tmax, &ta);
+            hr = ray_aabb(r.bmin - g, r.bmax + g, o, inv_d, tmax, &tb);
+          } else {
+            hl = ray_aabb(l.bmin, l.bmax, o, inv_d, tmax, &ta);
+            hr = ray_aabb(r.bmin, r.bmax, o, inv_d, tmax, &tb);
+          }
+          if (hl && hr) {
+            uint32_t nearn, farn; R nt, ft;
+            if (ta <= tb) { nearn = node.a; nt = ta; farn = node.b; ft = tb; }
+            else { nearn = node.b; nt = tb; farn = node.a; ft = ta; }
+            sn[sp] = farn; stt[sp] = ft;
+            sn[sp + 1] = nearn; stt[sp + 1] = nt;
+            sp += 2;
+          } else if (hl) {
+            sn[sp] = node.a; stt[sp] = ta; sp++;
+          } else if (hr) {
+            sn[sp] = node.b; stt[sp] = tb; sp++;
+          }
         }
       }
+      if (!tie || !amb || fixed) break;
+      fixed = true;
+      bcull = tmin * (R(1) + rel);
+      have = false;
     }
     if (have) { *tout = bt; *triout = btri; }
     return have;

@@ -1,0 +1,119 @@
+"""Parity at the benchmark's full sizes, on the benchmark's own inputs and tree.
+
+- The 40-room scene (49k primitives, panes as panels): all 64 pairs x 4096
+  rays x 3 bands, 2000 x 1 ms bins, 200 bounces, floor 1e-6, near-tie rule, in
+  one batch on the three-axis SAH tree, against the f32 oracle on the
+  reference's tree: every job's segment count is identical (the trajectories
+  are the same: under the near-tie rule the hit does not depend on the tree),
+  every job's histogram within 1e-5 per bin (bins holding >= 1e-6 of the band
+  total; the oracle sums the f32 trajectories in FP64), and the batch total
+  is the bench's segment count.
+- The 256-room uneven batch (triangles lognormal 12-20k, rays 512-65536,
+  3 or 8 bands, 0.5-4 s): the same checks for every room.
+- The 1 M-triangle city, 16 sources x 1 M rays x 8 bands: the same checks.
+The oracle runs on all host cores; the three tests take about a minute.
+"""
+import os
+
+import pytest
+
+from omg_audio_gb300 import Context, Job, MeshBuilder, TraceConfig, _lib
+from omg_audio_gb300 import workloads as W
+
+from test_gpu_parity import oparams, rel_bins
+from test_oracle_golden import omat
+
+pytestmark = pytest.mark.gpu
+
+CFG = dict(n_bands=3, n_bins=2000, bin_dt=0.001, max_time=2.0, max_bounces=200, energy_floor=1e-6, tie_mode=1)
+THREADS = os.cpu_count() or 8
+
+
+def _oracle_mesh(O, rec):
+    ob = O.MeshBuilder()
+    rec.replay(ob, lambda m: omat(O, m))
+    return ob.build("f32")
+
+
+def test_full_multiroom_batch_matches_the_oracle(oracle):
+    O = oracle
+    case = W.multiroom(seed=2, n_pairs=64)
+    with Context(TraceConfig(timeout_ms=60000, **CFG)) as ctx:
+        mb = MeshBuilder()
+        case.recorder.replay(mb)
+        scene = ctx.upload_builder(mb, 3, _lib.BVH_SAH3)
+        jobs = [Job(src, lis, 4096, seed=1000 + p, scene=scene, panel_offset=0, n_panels=len(case.panels))
+                for p, (src, lis) in enumerate(case.pairs)]
+        b = ctx.batch(jobs, case.panels)
+        b.autotune(reps=1)
+        b.launch()
+        res = b.read()
+        total = b.segments()
+        b.destroy()
+        scene.release()
+    om = _oracle_mesh(O, case.recorder)
+    P = oparams(O, ctx.cfg)
+    pan = [(mn, mx, omat(O, m)) for (mn, mx, m) in case.panels]
+    seg_sum = 0
+    for p, ((e, rv), (src, lis)) in enumerate(zip(res, case.pairs)):
+        ob, od, st = O.trace_mesh(om, src, lis, 4096, P=P, seed=1000 + p, panels=pan, threads=THREADS, acc64=True)
+        assert rv.segments == st["segments"], (p, rv.segments, st["segments"])
+        assert rel_bins(e.bins, ob) <= 1e-5, p
+        seg_sum += st["segments"]
+    assert total == seg_sum
+
+
+def test_full_uneven_batch_matches_the_oracle(oracle):
+    O = oracle
+    rooms = W.room_batch(seed=3, n_rooms=256)
+    with Context(TraceConfig(timeout_ms=60000, **CFG)) as ctx:
+        scenes, jobs = [], []
+        for k, r in enumerate(rooms):
+            mb = MeshBuilder()
+            r.recorder.replay(mb)
+            sc = ctx.upload_builder(mb, r.n_bands, _lib.BVH_SAH3)
+            scenes.append(sc)
+            jobs.append(Job(r.src, r.lis, r.n_rays, seed=100 + k, scene=sc, n_bands=r.n_bands, n_bins=r.n_bins,
+                            max_time=r.max_time))
+        b = ctx.batch(jobs)
+        b.autotune(reps=1)
+        b.launch()
+        res = b.read()
+        b.destroy()
+        for sc in scenes:
+            sc.release()
+    assert len(res) == 256 and {r.n_bands for r in rooms} == {3, 8}
+    for k, (r, (e, rv)) in enumerate(zip(rooms, res)):
+        P = oparams(O, ctx.cfg)
+        P.n_bands, P.n_bins, P.max_time = r.n_bands, r.n_bins, r.max_time
+        ob, _, st = O.trace_mesh(_oracle_mesh(O, r.recorder), r.src, r.lis, r.n_rays, energy=[1.0] * r.n_bands,
+                                 P=P, seed=100 + k, threads=THREADS, acc64=True)
+        assert rv.segments == st["segments"], k
+        assert e.bins.shape == (r.n_bins, r.n_bands)
+        assert rel_bins(e.bins, ob) <= 1e-5, k
+
+
+def test_full_city_matches_the_oracle(oracle):
+    """The stress scene at its full size: 1 M triangles (1.94 M primitives) on the
+    three-axis SAH tree, 16 sources x 1 M rays x 8 bands, 4 s at 1 ms, in one
+    batch: identical segment counts and per-bin histograms within 1e-5 of the
+    f32 oracle for every source."""
+    O = oracle
+    case = W.city(seed=5, n_dome=16)
+    cfg = dict(CFG, n_bands=8, n_bins=4000, max_time=4.0)
+    with Context(TraceConfig(timeout_ms=300000, **cfg)) as ctx:
+        mb = MeshBuilder()
+        case.recorder.replay(mb)
+        scene = ctx.upload_builder(mb, 8, _lib.BVH_SAH3)
+        jobs = [Job(tuple(s), tuple(l), 1 << 20, seed=500 + k, scene=scene)
+                for k, (s, l) in enumerate(zip(case.sources, case.listeners))]
+        assert len(jobs) == 16
+        res = ctx.trace_batch(jobs)
+        scene.release()
+    om = _oracle_mesh(O, case.recorder)
+    P = oparams(O, ctx.cfg)
+    for k, ((e, rv), j) in enumerate(zip(res, jobs)):
+        ob, _, st = O.trace_mesh(om, j.src, j.lis, 1 << 20, energy=[1.0] * 8, P=P, seed=500 + k, threads=THREADS,
+                                 acc64=True)
+        assert rv.segments == st["segments"], k
+        assert rel_bins(e.bins, ob) <= 1e-5, k
