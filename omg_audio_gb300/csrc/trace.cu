@@ -29,17 +29,30 @@ struct Walk {
   int cur;
   int leaf;          // postponed leaf (TIE), or 0
   int sp;
-  bool have;
-  float t_best, t_cull;
-  uint32_t s_best, tri_best;
-  int prim_best;
-  TieState ts;           // near-tie state (TIE walks)
+  int prim_best;     // the winner so far (-1: no hit yet)
+  float t_best;
+  float t_min;       // TIE: exact nearest hit so far (FLT_MAX: none); the window is t_min (1 + 1e-6)
+  uint32_t flags;    // TIE: kWalkAmb, kWalkFixed (TieState, device_common.cuh)
   float ix, iy, iz;
-  bool fast;             // origin within the grown boxes' margin (else every box counts as hit)
+  bool fast;         // the fused multiply-add slab test applies (origin within the margin, no d_a near 0)
   uint32_t budget;
   int* stack_ref;
   float* stack_t;
 };
+// The near-tie state is kept compact (the winner's surface and triangle ids
+// are read back from its primitive when a comparison needs them, the culling
+// bound is recomputed from t_min): the walk's scalars live in registers next
+// to the ray's, under the persistent kernels' 64-register cap.
+constexpr uint32_t kWalkAmb = 1u, kWalkFixed = 2u;
+
+__device__ __forceinline__ bool walk_have(const Walk& w) { return w.prim_best >= 0; }
+
+// Culling bound. TIE: the near-tie window (infinite before the first hit);
+// otherwise the best t (the reference's strict culling).
+template <bool TIE>
+__device__ __forceinline__ float walk_cull(const Walk& w) {
+  return TIE ? w.t_min * (1.0f + kTieRel) : (w.prim_best >= 0 ? w.t_best : FLT_MAX);
+}
 
 constexpr int kDone = 0x7FFFFFFF;  // never a node index (< 2^28)
 // Loop iterations of one warp of a persistent kernel before it gives up and
@@ -49,9 +62,10 @@ constexpr uint32_t kMaxLoop = 1u << 22;
 
 template <bool TIE>
 __device__ __forceinline__ int walk_pop(Walk& w) {
+  const float cull = walk_cull<TIE>(w);
   while (w.sp > 0) {
     w.sp--;
-    if (TIE ? w.stack_t[w.sp] > w.t_cull : (w.have && w.stack_t[w.sp] >= w.t_best)) continue;
+    if (TIE ? w.stack_t[w.sp] > cull : (walk_have(w) && w.stack_t[w.sp] >= w.t_best)) continue;
     return w.stack_ref[w.sp];
   }
   return kDone;
@@ -65,13 +79,10 @@ __device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float ox, f
   w.cur = S.n_prims ? ((TIE && wide && S.nodes4) ? S.root4 : S.root) : kDone;
   w.leaf = 0;
   w.sp = 0;
-  w.have = false;
+  w.prim_best = -1;
   w.t_best = FLT_MAX;
-  w.t_cull = FLT_MAX;
-  w.s_best = 0;
-  w.tri_best = 0;
-  w.prim_best = 0;
-  w.ts = tie_begin();
+  w.t_min = FLT_MAX;
+  w.flags = 0u;
   w.ix = __frcp_rn(dx);
   w.iy = __frcp_rn(dy);
   w.iz = __frcp_rn(dz);
@@ -83,19 +94,63 @@ __device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float ox, f
   w.budget = 2u * S.n_nodes + S.n_prims + 64u;
 }
 
-// A near-tie walk that ended with an ambiguous window (TieState::amb) starts
-// over in fixed mode from `root`: the caller keeps walking.
+// A near-tie walk that ended with an ambiguous window starts over in fixed
+// mode from `root` (t_min stays: the window is final); the caller keeps walking.
 __device__ __forceinline__ bool walk_restart_fixed(Walk& w, int root, uint32_t budget) {
-  if (!w.ts.amb || w.ts.fixed) return false;
-  w.ts.fixed = true;
-  w.t_cull = w.ts.t_min * (1.0f + kTieRel);
-  w.have = false;
+  if (!(w.flags & kWalkAmb) || (w.flags & kWalkFixed)) return false;
+  w.flags |= kWalkFixed;
+  w.prim_best = -1;
   w.t_best = FLT_MAX;
   w.cur = root;
   w.leaf = 0;
   w.sp = 0;
   w.budget = budget;
   return true;
+}
+
+// One leaf of a near-tie walk (the rule of tie_take, device_common.cuh, on the
+// compact state).
+__device__ __forceinline__ void walk_leaf_tie(Walk& w, const float4* __restrict__ prims, int leaf, float ox,
+                                              float oy, float oz, float dx, float dy, float dz) {
+  const uint32_t code = ~(uint32_t)leaf;
+  const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
+  for (uint32_t i = start; i < end; i++) {
+    const float4 p0 = __ldg(prims + 3 * i + 0);
+    const float4 p1 = __ldg(prims + 3 * i + 1);
+    const float4 p2 = __ldg(prims + 3 * i + 2);
+    float t;
+    if (!ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) continue;
+    const uint32_t s = __float_as_uint(p2.w), tr = __float_as_uint(p1.w);
+    const bool have = w.prim_best >= 0;
+    // the winner's key, read back from its primitive
+    auto less_than_best = [&]() {
+      const uint32_t bs = __float_as_uint(__ldg(prims + 3 * w.prim_best + 2).w);
+      const uint32_t btr = __float_as_uint(__ldg(prims + 3 * w.prim_best + 1).w);
+      return tie_key_less(s, tr, t, bs, btr, w.t_best);
+    };
+    bool take;
+    if (w.flags & kWalkFixed) {
+      take = t <= w.t_min * (1.0f + kTieRel) && (!have || less_than_best());
+    } else if (!have) {
+      take = true;
+      w.t_min = t;
+    } else if (t < w.t_min) {
+      const float win = t * (1.0f + kTieRel);
+      if (w.t_best <= win) {
+        take = less_than_best();
+      } else {
+        if (w.t_min <= win) w.flags |= kWalkAmb;
+        take = true;
+      }
+      w.t_min = t;
+    } else {
+      take = t <= w.t_min * (1.0f + kTieRel) && less_than_best();
+    }
+    if (take) {
+      w.prim_best = (int)i;
+      w.t_best = t;
+    }
+  }
 }
 
 // Up to `steps` node steps of the 4-wide walk (mesh_closest4 in pieces).
@@ -109,11 +164,27 @@ __device__ __forceinline__ bool walk4_steps(Walk& w, const DScene& S, float ox, 
     if (w.budget-- == 0u) {
       atomicOr(err, 4u);
       w.cur = kDone;
-      w.ts.amb = false;
+      w.flags &= ~kWalkAmb;
       break;
     }
-    w.cur = bvh4_step(S.nodes4, S.prims, w.cur, ox, oy, oz, dx, dy, dz, w.ix, w.iy, w.iz, w.have, w.t_best,
-                      w.t_cull, w.prim_best, w.s_best, w.tri_best, w.ts, w.stack_ref, w.stack_t, w.sp, err);
+    // the compact state expanded for the generic 4-wide step
+    bool have = walk_have(w);
+    float t_cull = walk_cull<true>(w);
+    int pb = w.prim_best;
+    uint32_t sb = 0, tb = 0;
+    if (have) {
+      sb = __float_as_uint(__ldg(S.prims + 3 * pb + 2).w);
+      tb = __float_as_uint(__ldg(S.prims + 3 * pb + 1).w);
+    }
+    TieState ts;
+    ts.t_min = w.t_min;
+    ts.amb = (w.flags & kWalkAmb) != 0u;
+    ts.fixed = (w.flags & kWalkFixed) != 0u;
+    w.cur = bvh4_step(S.nodes4, S.prims, w.cur, ox, oy, oz, dx, dy, dz, w.ix, w.iy, w.iz, have, w.t_best, t_cull,
+                      pb, sb, tb, ts, w.stack_ref, w.stack_t, w.sp, err);
+    w.prim_best = have ? pb : -1;
+    w.t_min = ts.t_min;
+    w.flags = (ts.amb ? kWalkAmb : 0u) | (ts.fixed ? kWalkFixed : 0u);
   }
   if (w.cur == kDone) walk_restart_fixed(w, S.root4, 2u * S.n_nodes + S.n_prims + 64u);
   return w.cur == kDone;
@@ -142,7 +213,7 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
     const float4 n1 = __ldg(tnodes + 4 * w.cur + 1);
     const float4 n2 = __ldg(tnodes + 4 * w.cur + 2);
     const float4 n3 = __ldg(tnodes + 4 * w.cur + 3);
-    const float tmax = w.t_cull;   // FLT_MAX before the first hit; the final window in fixed mode
+    const float tmax = walk_cull<true>(w);   // infinite before the first hit; the final window in fixed mode
     float ta, tb;
     bool h0, h1;
     if (w.fast) {
@@ -192,8 +263,7 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
       w.leaf = 0;
       return true;
     }
-    leaf_test<true>(prims, w.leaf, ox, oy, oz, dx, dy, dz, w.have, w.t_best, w.t_cull, w.prim_best, w.s_best,
-                    w.tri_best, w.ts);
+    walk_leaf_tie(w, prims, w.leaf, ox, oy, oz, dx, dy, dz);
     w.leaf = 0;
     if (w.cur < 0) {
       w.leaf = w.cur;
@@ -227,7 +297,7 @@ __device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, f
         const float4 n1 = __ldg(nodes + 4 * w.cur + 1);
         const float4 n2 = __ldg(nodes + 4 * w.cur + 2);
         const float4 n3 = __ldg(nodes + 4 * w.cur + 3);
-        const float tmax = w.have ? w.t_cull : FLT_MAX;
+        const float tmax = walk_cull<false>(w);
         float ta, tb;
         const bool h0 = ray_aabb(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ox, oy, oz, w.ix, w.iy, w.iz, tmax, ta);
         const bool h1 = ray_aabb(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ox, oy, oz, w.ix, w.iy, w.iz, tmax, tb);
@@ -244,17 +314,20 @@ __device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, f
           } else {
             atomicOr(err, 1u);
           }
-          w.cur = (w.have && nt >= w.t_best) ? walk_pop<TIE>(w) : nr;
+          w.cur = (walk_have(w) && nt >= w.t_best) ? walk_pop<TIE>(w) : nr;
         } else if (h0) {
-          w.cur = (w.have && ta >= w.t_best) ? walk_pop<TIE>(w) : c0;
+          w.cur = (walk_have(w) && ta >= w.t_best) ? walk_pop<TIE>(w) : c0;
         } else if (h1) {
-          w.cur = (w.have && tb >= w.t_best) ? walk_pop<TIE>(w) : c1;
+          w.cur = (walk_have(w) && tb >= w.t_best) ? walk_pop<TIE>(w) : c1;
         } else {
           w.cur = walk_pop<TIE>(w);
         }
       } else {
-        leaf_test<TIE>(prims, w.cur, ox, oy, oz, dx, dy, dz, w.have, w.t_best, w.t_cull, w.prim_best, w.s_best,
-                       w.tri_best, w.ts);
+        bool have = walk_have(w);
+        float t_cull = walk_cull<false>(w);
+        uint32_t sb = 0, tb = 0;
+        TieState ts = tie_begin();
+        leaf_test<false>(prims, w.cur, ox, oy, oz, dx, dy, dz, have, w.t_best, t_cull, w.prim_best, sb, tb, ts);
         w.cur = walk_pop<TIE>(w);
       }
     }
@@ -397,7 +470,7 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
       const DJob& J = jobs[ji];
       const DScene& S = scenes[J.scene];
       if (walk_steps<TIE>(w, S, px, py, pz, dx, dy, dz, walk_budget, wide, err)) {
-        have = w.have;
+        have = walk_have(w);
         h.t = FLT_MAX;
         h.m = nullptr;
         if (have) {
@@ -624,7 +697,7 @@ __global__ void __launch_bounds__(256, 4) trace_wl_kernel(const DJob* __restrict
     // ---- walk, at most walk_budget steps this iteration
     bool finished = false;
     if (rid != kNone && walk_steps<TIE>(w, *wsc, ox, oy, oz, dx, dy, dz, walk_budget, wide, err)) {
-      st.hit[rid] = make_float2(w.t_best, __int_as_float(w.have ? w.prim_best : -1));
+      st.hit[rid] = make_float2(w.t_best, __int_as_float(w.prim_best));
       finished = true;
     }
     const unsigned fm = __ballot_sync(FULL, finished);
