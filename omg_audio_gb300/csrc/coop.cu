@@ -241,8 +241,10 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
     walking = __ballot_sync(FULL, leader && rid != kNone);
     if (!walking && !sh_cnt && !wk_cnt && (exhausted || parking)) break;
 
-    // ---- cooperative walk steps, until a walk ends or walk_budget steps
+    // ---- cooperative walk steps, until a walk ends or walk_budget steps (none
+    // when no group of the warp walks: rays may only be waiting to be shaded)
     for (int step = 0; step < walk_budget; step++) {
+      if (__ballot_sync(FULL, rid != kNone) == 0u) break;
       const bool wk = rid != kNone;   // the same in the 4 lanes of a group
       bool out_of_budget = false;
       if (wk) {

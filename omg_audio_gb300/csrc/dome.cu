@@ -44,7 +44,10 @@ __device__ bool trace_escape(const DScene& S, const DDomeLaunch& L, float px, fl
     events++;
     float tm = FLT_MAX;
     int prim = 0;
-    const bool mh = mesh_closest<TIE>(S, px, py, pz, dx, dy, dz, tm, prim, &L.hdr->error);
+    // under the near-tie rule the 4-wide tree gives the same hit in half the
+    // dependent steps (this kernel has one thread per fan ray: latency-bound)
+    const bool mh = (TIE && S.nodes4) ? mesh_closest4(S, px, py, pz, dx, dy, dz, tm, prim, &L.hdr->error)
+                                      : mesh_closest<TIE>(S, px, py, pz, dx, dy, dz, tm, prim, &L.hdr->error);
     const float t_mesh = mh ? tm : FLT_MAX;
     float t_pan = t_mesh;
     int pan = -1;
