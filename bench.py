@@ -391,10 +391,24 @@ def run_workload(args):
     setup_s = time.perf_counter() - t0
     ctx.set_stream(stream.cuda_stream)
     batch = ctx.batch(jobs)
-    tune = batch.autotune(reps=1) if args.autotune else batch.shape()
+    if args.shape:
+        batch.set_shape(**json.loads(args.shape))
+        tune = batch.shape()
+    else:
+        tune = batch.autotune(reps=1) if args.autotune else batch.shape()
     for _ in range(max(args.warmup, 1)):
         batch.launch()
     torch.cuda.synchronize()
+    if args.profile:
+        # small case for a profiler: the launches only, nothing timed or printed
+        for _ in range(args.steps):
+            batch.launch()
+            if dome is not None:
+                dome.submit(case.dome_eyes, n_rays=512, stream=stream.cuda_stream, want=2)
+                torch.cuda.synchronize()
+                dome.collect()
+        torch.cuda.synchronize()
+        return 0
     ms, dms = [], []
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
