@@ -877,6 +877,19 @@ int32_t omg_batch_autotune(omg_ctx* ctx, uint32_t id, uint32_t reps, omg_tune_re
         rc = try_shape(sh);
       }
     }
+  // the same persistent kernel walking the 4-wide tree (near-tie rule, every
+  // scene host-built): fewer dependent steps per walk, which pays where the
+  // walks wait on memory (trees beyond L2)
+  if (B.coop_ok && best_shape.mode != 2) {
+    const LaunchShape base = best_shape;
+    for (uint32_t wk : walks) {
+      if (rc) continue;
+      LaunchShape sh = base;
+      sh.wide = 1;
+      sh.walk_steps = wk;
+      rc = try_shape(sh);
+    }
+  }
   const LaunchShape persistent = best_shape;
   for (uint32_t tm : tail_modes)
     for (uint32_t ne : epoch_counts)

@@ -7,7 +7,8 @@
   are the same: under the near-tie rule the hit does not depend on the tree),
   every job's histogram within 1e-5 per bin (bins holding >= 1e-6 of the band
   total; the oracle sums the f32 trajectories in FP64), and the batch total
-  is the bench's segment count.
+  is the bench's segment count; against the FP64 oracle on the same streams,
+  every pair's RT60 within 1 % and late level within 0.1 dB.
 - The 256-room uneven batch (triangles lognormal 12-20k, rays 512-65536,
   3 or 8 bands, 0.5-4 s): the same checks for every room.
 - The 1 M-triangle city, 16 sources x 1 M rays x 8 bands: the same checks.
@@ -15,6 +16,7 @@ The oracle runs on all host cores; the three tests take about a minute.
 """
 import os
 
+import numpy as np
 import pytest
 
 from omg_audio_gb300 import Context, Job, MeshBuilder, TraceConfig, _lib
@@ -52,6 +54,9 @@ def test_full_multiroom_batch_matches_the_oracle(oracle):
         b.destroy()
         scene.release()
     om = _oracle_mesh(O, case.recorder)
+    ob64 = O.MeshBuilder()
+    case.recorder.replay(ob64, lambda m: omat(O, m))
+    om64 = ob64.build("f64")
     P = oparams(O, ctx.cfg)
     pan = [(mn, mx, omat(O, m)) for (mn, mx, m) in case.panels]
     seg_sum = 0
@@ -60,6 +65,11 @@ def test_full_multiroom_batch_matches_the_oracle(oracle):
         assert rv.segments == st["segments"], (p, rv.segments, st["segments"])
         assert rel_bins(e.bins, ob) <= 1e-5, p
         seg_sum += st["segments"]
+        # the FP64 oracle on the same stream: RT60 within 1 %, late level within 0.1 dB
+        b64, _, _ = O.trace_mesh(om64, src, lis, 4096, P=P, seed=1000 + p, panels=pan, threads=THREADS)
+        rt, lv, _ = O.estimate_reverb(b64, ctx.cfg.bin_dt, level_f32=False)
+        assert np.all(np.abs(rv.rt60 / rt - 1) < 0.01), (p, rv.rt60, rt)
+        assert np.all(np.abs(20 * np.log10(rv.level / lv)) < 0.1), (p, rv.level, lv)
     assert total == seg_sum
 
 
