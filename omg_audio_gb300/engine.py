@@ -203,8 +203,8 @@ class Context:
     def trace_batch(self, jobs: Sequence["Job"], panels: Sequence[Panel] = ()):
         """One-shot batch through the host-buffer entry point."""
         arr, nbf, ndf = jobs_to_c(jobs, self.cfg)
-        bins = np.zeros(nbf, np.float32)
-        dirs = np.zeros(ndf, np.float32)
+        bins = np.empty(nbf, np.float32)       # every float is written by the call
+        dirs = np.empty(ndf, np.float32)
         rv = (_lib.omg_reverb * len(jobs))()
         parr = panels_to_c(panels)
         rc = lib().omg_trace_batch(self.h, arr, len(jobs), parr, len(panels), _p(bins), _p(dirs), rv)
@@ -319,13 +319,12 @@ def jobs_to_c(jobs: Sequence[Job], cfg: TraceConfig):
 
 
 def split_outputs(jobs, cfg, bins, dirs, rv):
+    """Per-job echograms as views of the batch's output arrays (no copies)."""
     out = []
     bo = do = 0
     for i, j in enumerate(jobs):
         nb, n = j.bands(cfg), j.bins_len(cfg)
-        e = Echogram(n, nb, cfg.bin_dt)
-        e.bins[:] = bins[bo:bo + n * nb].reshape(n, nb)
-        e.dirs[:] = dirs[do:do + n * 3].reshape(n, 3)
+        e = Echogram.wrap(bins[bo:bo + n * nb].reshape(n, nb), dirs[do:do + n * 3].reshape(n, 3), cfg.bin_dt)
         bo += n * nb
         do += n * 3
         out.append((e, _reverb_of(rv[i], nb)))
@@ -343,18 +342,19 @@ class Batch:
         ctx._check(lib().omg_batch_create(ctx.h, arr, len(jobs), parr, len(panels), C.byref(bid)),
                    "omg_batch_create")
         self.id = bid.value
-        self._bins = np.zeros(self.n_bin_floats, np.float32)
-        self._dirs = np.zeros(self.n_dir_floats, np.float32)
-        self._rv = (_lib.omg_reverb * len(jobs))()
 
     def launch(self, part: int = 0):
         """part 0: everything; 1: clear + trace kernel; 2: finalize + reverb."""
         self.ctx._check(lib().omg_batch_launch_part(self.ctx.h, self.id, part), "omg_batch_launch_part")
 
     def read(self):
-        rc = lib().omg_batch_read(self.ctx.h, self.id, _p(self._bins), _p(self._dirs), self._rv)
+        """Fresh arrays on every read: the echograms returned are views of them."""
+        bins = np.empty(self.n_bin_floats, np.float32)
+        dirs = np.empty(self.n_dir_floats, np.float32)
+        rv = (_lib.omg_reverb * len(self.jobs))()
+        rc = lib().omg_batch_read(self.ctx.h, self.id, _p(bins), _p(dirs), rv)
         self.ctx._check(rc, "omg_batch_read")
-        return split_outputs(self.jobs, self.ctx.cfg, self._bins, self._dirs, self._rv)
+        return split_outputs(self.jobs, self.ctx.cfg, bins, dirs, rv)
 
     def segments(self) -> int:
         s = C.c_uint64()
@@ -490,21 +490,24 @@ class DomeProbe:
         self._pending = (len(eyes), n_rays, want)
 
     def collect(self):
+        """Wait for the submitted sample; arrays not asked for at submit() come back as None."""
         n_eyes, n_rays, want = self._pending
         nb = self.nb
         out = (_lib.omg_dome_bin * (9 * n_eyes))()
-        raw = np.zeros((n_eyes, 9, nb), np.float32)
-        esc = np.zeros((n_eyes, n_rays), np.uint8)
-        tp = np.zeros((n_eyes, n_rays, nb), np.float32)
-        rc = lib().omg_dome_collect(self.ctx.h, self.id, out, _p(raw), _p(esc), _p(tp))
+        raw = np.empty((n_eyes, 9, nb), np.float32) if want & 1 else None
+        esc = np.empty((n_eyes, n_rays), np.uint8) if want & 2 else None
+        tp = np.empty((n_eyes, n_rays, nb), np.float32) if want & 4 else None
+        rc = lib().omg_dome_collect(self.ctx.h, self.id, out, _p(raw) if raw is not None else None,
+                                    _p(esc) if esc is not None else None, _p(tp) if tp is not None else None)
         self.ctx._check(rc, "omg_dome_collect")
-        return self._result(out, n_eyes, raw if want & 1 else None, esc if want & 2 else None,
-                            tp if want & 4 else None)
+        return self._result(out, n_eyes, raw, esc, tp)
 
     def _result(self, out, n_eyes, raw, esc, tp):
         nb = self.nb
-        energy = np.array([[out[e * 9 + k].energy[:nb] for k in range(9)] for e in range(n_eyes)], np.float32)
-        dirs = np.array([[out[e * 9 + k].dir[:] for k in range(9)] for e in range(n_eyes)], np.float32)
+        # omg_dome_bin is 11 packed floats: dir[3], energy[8]
+        flat = np.ctypeslib.as_array(C.cast(out, C.POINTER(C.c_float)), (9 * n_eyes * 11,)).reshape(n_eyes, 9, 11)
+        energy = flat[:, :, 3:3 + nb].copy()
+        dirs = flat[:, :, :3].copy()
         ev, th = C.c_uint64(), C.c_uint64()
         lib().omg_dome_segments(self.ctx.h, self.id, C.byref(ev), C.byref(th))
         return dict(energy=energy, dir=dirs, raw=raw, escape=esc, ray_tp=tp,

@@ -29,6 +29,13 @@ class Echogram:
         self.bins = np.zeros((n_bins, n_bands), np.float32)
         self.dirs = np.zeros((n_bins, 3), np.float32)
 
+    @classmethod
+    def wrap(cls, bins: np.ndarray, dirs: np.ndarray, bin_dt: float) -> "Echogram":
+        """An echogram over existing (n_bins, n_bands) and (n_bins, 3) f32 arrays, not copied."""
+        e = cls.__new__(cls)
+        e.bin_dt, e.bins, e.dirs = float(bin_dt), bins, dirs
+        return e
+
     @property
     def n_bins(self) -> int:
         return self.bins.shape[0]

@@ -49,6 +49,29 @@ def test_struct_sizes_match_the_header(built_lib):
     assert C.sizeof(_lib.omg_panel) == 24 + 68
     assert C.sizeof(_lib.omg_reverb) == 3 * 32 + 8
     assert C.sizeof(_lib.omg_late_state) == 2 * 32 + 16 + 8
+    assert C.sizeof(_lib.omg_dome_bin) == 11 * 4
+
+
+def test_dome_bins_read_as_arrays(built_lib):
+    """DomeProbe reads omg_dome_bin records as one float view: same values as field by field."""
+    import numpy as np
+    from omg_audio_gb300 import _lib
+    from omg_audio_gb300.engine import DomeProbe
+    n_eyes, nb = 3, 5
+    out = (_lib.omg_dome_bin * (9 * n_eyes))()
+    for i in range(9 * n_eyes):
+        out[i].dir[:] = [i, i + 0.25, i + 0.5]
+        out[i].energy[:] = [100 * i + b for b in range(8)]
+    probe = DomeProbe.__new__(DomeProbe)
+    probe.nb = nb
+    probe.ctx = type("Ctx", (), {"h": None})()     # no context: the segment query is refused, counts stay 0
+    probe.id = 0
+    r = probe._result(out, n_eyes, None, None, None)
+    for e in range(n_eyes):
+        for k in range(9):
+            assert np.array_equal(r["energy"][e, k], np.float32(out[e * 9 + k].energy[:nb]))
+            assert np.array_equal(r["dir"][e, k], np.float32(out[e * 9 + k].dir[:]))
+    assert r["energy"].shape == (n_eyes, 9, nb) and r["energy"].flags.owndata
 
 
 def test_mesh_builder_matches_oracle_on_cpu(built_lib, oracle):
