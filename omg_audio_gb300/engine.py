@@ -69,6 +69,17 @@ def _reverb_of(r: _lib.omg_reverb, nb: int) -> ReverbParams:
                         np.array(r.rt60_fit[:nb], np.float32), int(r.segments))
 
 
+# omg_reverb as a numpy record: rt60[8], level[8], rt60_fit[8] f32, segments u64 (104 bytes)
+_REVERB_DTYPE = np.dtype([("rt60", np.float32, 8), ("level", np.float32, 8), ("rt60_fit", np.float32, 8),
+                          ("segments", np.uint64)])
+
+
+def _reverbs_of(rv, n: int):
+    """All n omg_reverb records of a ctypes array as (rt60, level, rt60_fit, segments) arrays, one copy."""
+    rec = np.frombuffer(rv, _REVERB_DTYPE, count=n).copy()
+    return rec["rt60"], rec["level"], rec["rt60_fit"], rec["segments"].tolist()
+
+
 class Context:
     """omg_create / omg_destroy. Raises when no CUDA device is usable."""
 
@@ -322,12 +333,13 @@ def split_outputs(jobs, cfg, bins, dirs, rv):
     """Per-job echograms as views of the batch's output arrays (no copies)."""
     out = []
     bo = do = 0
+    rt, lv, fit, seg = _reverbs_of(rv, len(jobs))
     for i, j in enumerate(jobs):
         nb, n = j.bands(cfg), j.bins_len(cfg)
         e = Echogram.wrap(bins[bo:bo + n * nb].reshape(n, nb), dirs[do:do + n * 3].reshape(n, 3), cfg.bin_dt)
         bo += n * nb
         do += n * 3
-        out.append((e, _reverb_of(rv[i], nb)))
+        out.append((e, ReverbParams(rt[i, :nb], lv[i, :nb], fit[i, :nb], seg[i])))
     return out
 
 
