@@ -262,7 +262,7 @@ int32_t omg_early_solve(omg_ctx* ctx, uint32_t early_id, const uint16_t* source_
                         uint32_t n_sources, const omg_chain* chains, uint32_t n_chains, const float listener[3],
                         const omg_aabb* extras, uint32_t n_extras, omg_mesh_record* out) {
   if (!ctx || !listener || !finite3(listener) || (n_sources && (!source_ids || !source_pos)) ||
-      (n_chains && !chains) || (n_extras && !extras) || ((uint64_t)n_sources * n_chains && !out))
+      (n_chains && !chains) || (n_extras && !extras) || ((uint64_t)n_sources * n_chains != 0 && !out))
     return OMG_E_INVALID;
   for (uint32_t c = 0; c < n_chains; c++)
     if (chains[c].order > OMG_CHAIN_MAX_ORDER) return OMG_E_INVALID;

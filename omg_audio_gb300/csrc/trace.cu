@@ -227,9 +227,9 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
     const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
     if (h0 && h1) {
       int nr, fr;
-      float nt, ft;
-      if (ta <= tb) { nr = c0; nt = ta; fr = c1; ft = tb; }
-      else { nr = c1; nt = tb; fr = c0; ft = ta; }
+      float ft;
+      if (ta <= tb) { nr = c0; fr = c1; ft = tb; }
+      else { nr = c1; fr = c0; ft = ta; }
       if (w.sp < STACK_DEPTH) {
         w.stack_ref[w.sp] = fr;
         w.stack_t[w.sp] = ft;
@@ -237,7 +237,7 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
       } else {
         atomicOr(err, 1u);
       }
-      w.cur = nr;   // nt <= tmax = t_cull: never culled here
+      w.cur = nr;   // the nearer entry t <= tmax = t_cull: never culled here
     } else if (h0) {
       w.cur = c0;
     } else if (h1) {
