@@ -10,7 +10,9 @@ histograms within 1e-5 per bin on bins holding >= 1e-6 of the band total):
   scene.rs:41-47 returns no hit);
 - a listener at the source;
 - invalid requests (a job without rays, alone or in a batch) rejected with OMG_E_INVALID, the context
-  still usable afterwards.
+  still usable afterwards;
+- a host wait that runs out (OMG_E_TIMEOUT) while the batch keeps running, and a
+  later read of the finished batch.
 """
 import numpy as np
 import pytest
@@ -94,3 +96,47 @@ def test_invalid_requests_are_rejected(ctx):
                          Job((1, 1, 1), (2, 2, 2), 0, box_size=(6, 4, 3), box_walls=walls)])
     e, rv = ctx.trace_box((6, 4, 3), walls, (1, 1, 1), (2, 2, 2), 256, seed=1)   # still usable
     assert rv.segments >= 256 and np.isfinite(e.bins).all()
+
+
+def test_host_wait_times_out_and_the_context_stays_usable(oracle):
+    """The host's bounded wait (timeout_ms = 1) gives up on a batch that runs
+    ~10 ms and returns OMG_E_TIMEOUT; nothing on the device is interrupted.
+    A later read of the same batch, once it has finished, returns the same
+    result as a context with the default wait."""
+    import time
+    from omg_audio_gb300 import workloads as W
+    case = W.multiroom(seed=2, n_pairs=64)
+    cfg = dict(n_bands=3, n_bins=2000, bin_dt=0.001, max_time=2.0, max_bounces=200, energy_floor=1e-6, tie_mode=1)
+    out = []
+    for timeout in (1, 60000):
+        with Context(TraceConfig(timeout_ms=timeout, **cfg)) as ctx:
+            mb = MeshBuilder()
+            case.recorder.replay(mb)
+            scene = ctx.upload_builder(mb, 3, _lib.BVH_SAH3)
+            jobs = [Job(src, lis, 4096, seed=1000 + p, scene=scene, panel_offset=0, n_panels=len(case.panels))
+                    for p, (src, lis) in enumerate(case.pairs)]
+            b = ctx.batch(jobs, case.panels)
+            b.launch()
+            if timeout == 1:
+                with pytest.raises(_lib.OmgError) as ex:
+                    b.read()
+                assert ex.value.status == _lib.E_TIMEOUT
+                time.sleep(1.0)                       # the batch finishes on its own
+            res = seg = None
+            for _ in range(50):                       # a read's own copies may still outlast a 1 ms wait
+                try:
+                    res = res or b.read()
+                    seg = b.segments()
+                    break
+                except _lib.OmgError as e:
+                    assert e.status == _lib.E_TIMEOUT
+                    time.sleep(0.1)
+            assert res is not None and seg is not None
+            out.append((seg, res))
+            b.destroy()
+            scene.release()
+    (s1, r1), (s2, r2) = out
+    assert s1 == s2
+    for (e1, v1), (e2, v2) in zip(r1, r2):
+        assert v1.segments == v2.segments
+        assert rel_bins(e1.bins, e2.bins) <= 1e-5
