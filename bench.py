@@ -125,33 +125,61 @@ def oracle_mesh(case, real="f32"):
     return mb.build(real)
 
 
-def cpu_sample(case, n_pairs, threads, n_rays=N_RAYS, ray_end=None):
-    """The f32 oracle (the reference's algorithm and arithmetic) on pairs
-    [0, n_pairs): segments, seconds and the traversal counters."""
+def cpu_sample(case, n_pairs, threads, n_rays=N_RAYS, ray_end=None, fans=True):
+    """The f32 oracle running the reference's own algorithm: its first-found
+    closest hit (tie_mode 0, mesh.rs:505) over its own SAH tree
+    (mesh.rs:241-405), in its f32 arithmetic, on pairs [0, n_pairs), then (fans)
+    the 512-ray dome fan of each of those pairs' listeners (dome.rs:425-478).
+    Returns segments, seconds and the trace's traversal counters."""
+    from concurrent.futures import ThreadPoolExecutor
+
     from oracle import oracle as O
     mesh = oracle_mesh(case)
-    P = O.params(tie_mode=1, **CFG)
+    P = O.params(tie_mode=0, **CFG)
     pan = [(mn, mx, O.Material.make(m.absorption, m.scattering, m.transmission)) for (mn, mx, m) in case.panels]
-    seg = nodes = prims = hits = 0
+    tot = {k: 0 for k in ("segments", "receiver_hits") + O.TRAV_KEYS}
+    glass = [g.as_dict() for g in case.glass]
+    eyes = [lis for (_, lis) in case.pairs[:n_pairs]] if fans else []
+    probes = [O.DomeProbe(mesh, glass, n_fan=DOME_RAYS, nb=3) for _ in range(min(threads, len(eyes)))]
     t0 = time.perf_counter()
     for p in range(n_pairs):
         src, lis = case.pairs[p]
         _, _, st = O.trace_mesh(mesh, src, lis, n_rays, P=P, seed=1000 + p, panels=pan, threads=threads,
                                 ray_end=ray_end)
-        seg += st["segments"]
-        nodes += st["node_reads"]
-        prims += st["prim_tests"]
-        hits += st["receiver_hits"]
+        for k in tot:
+            tot[k] += st[k]
+    dome_seg = 0
+    if eyes:
+        # one probe per host thread (ctypes releases the GIL during the call)
+        def fan(i):
+            pr = probes[i]
+            n = 0
+            for eye in eyes[i::len(probes)]:
+                r = pr.sample(eye, (), n_rays=DOME_RAYS)
+                n += r["stats"]["escape_events"] + r["stats"]["through_calls"]
+            return n
+        with ThreadPoolExecutor(len(probes)) as ex:
+            dome_seg = sum(ex.map(fan, range(len(probes))))
     dt = time.perf_counter() - t0
-    return dict(segments=seg, seconds=dt, node_reads=nodes, prim_tests=prims, receiver_hits=hits)
+    del probes
+    return dict(tot, seconds=dt, dome_segments=dome_seg)
 
 
 def bytes_per_segment(st, nb=3):
-    """B_seg = 32 N_node + 48 N_prim + 4 (NB + 3) h: bytes the reference's ordered
-    traversal reads per segment (32 B nodes, 48 B primitives) plus histogram writes."""
+    """B_seg = 32 N_node + 48 N_prim + 4 (NB + 3) h, per segment of the reference's
+    ordered traversal over its own tree (mesh.rs:484-541): N_node the DISTINCT
+    32-byte node records a closest-hit query reads (the root, plus both children
+    of every internal node it processes; a child popped later is the record its
+    parent already read), N_prim the 48-byte primitives it tests, h the receiver
+    hits (one histogram row of NB + 3 floats each)."""
     s = max(st["segments"], 1)
-    n_node, n_prim, h = st["node_reads"] / s, st["prim_tests"] / s, st["receiver_hits"] / s
-    return 32.0 * n_node + 48.0 * n_prim + 4.0 * (nb + 3) * h, dict(n_node=n_node, n_prim=n_prim, h=h)
+    n_node, n_prim, h = st["unique_nodes"] / s, st["prim_tests"] / s, st["receiver_hits"] / s
+    parts = dict(n_node=n_node, n_prim=n_prim, h=h,
+                 per_segment={k: st[k] / s for k in ("queries", "internal_visits", "leaf_visits", "child_boxes",
+                                                     "unique_nodes", "node_reads", "prim_tests", "receiver_hits")},
+                 formula="32 * unique_nodes + 48 * prim_tests + 4 * (NB + 3) * receiver_hits, per segment; "
+                         "unique_nodes = queries + child_boxes")
+    return 32.0 * n_node + 48.0 * n_prim + 4.0 * (nb + 3) * h, parts
 
 
 def max_over_ranks(vals, ws, device="cuda"):
@@ -179,6 +207,13 @@ def dist_env():
     return ws, rank, local
 
 
+def config_of(case_prims):
+    """The workload's config, the same dict in both arms."""
+    return {"workload": WORKLOAD, "prims": case_prims, "pairs": N_PAIRS, "rays_per_pair": N_RAYS, "bands": 3,
+            "bins": CFG["n_bins"], "dome_fans": N_PAIRS, "dome_rays": DOME_RAYS,
+            "l2": "GPU arm: flushed (256 MB write) before every timed step; CPU arm: n/a"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -187,19 +222,22 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     pairs = max(1, min(N_PAIRS, args.ref_pairs))
     for _ in range(max(0, args.warmup)):
-        cpu_sample(case, 1, threads, ray_end=256)
+        cpu_sample(case, 1, threads, ray_end=256, fans=False)
     times, segs = [], []
     for _ in range(args.steps):
         st = cpu_sample(case, pairs, threads)
         times.append(st["seconds"])
-        segs.append(st["segments"])
+        segs.append(st["segments"] + st["dome_segments"])
     v = float(np.sum(segs) / np.sum(times))
-    sample = f"{pairs} of {N_PAIRS} pairs x {N_RAYS} rays per step (the full fans skipped)"
+    sample = (f"{pairs} of {N_PAIRS} pairs x {N_RAYS} rays and their {pairs} dome fans per step, "
+              f"{threads} host threads")
+    prims = oracle_mesh(case).info()["prims"]
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": WORKLOAD, "sample": sample, "l2": "n/a (CPU)"},
+            "config": config_of(prims),
             "impl": "reference",
+            "tie_rule": "first found (the reference's, mesh.rs:505) on the reference's SAH tree",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -442,36 +480,37 @@ def run_workload(args):
     # give the reference's bytes per segment on this configuration
     from oracle import oracle as O
     threads = os.cpu_count() or 1
-    seg = nodes = prims_t = hits = 0
+    tot = {k: 0 for k in ("segments", "receiver_hits") + O.TRAV_KEYS}
     sec = sec1 = seg1 = 0.0
     for rec, src, lis, n_rays, seed, nb, n_bins, tmax in oracle_jobs:
         ob = O.MeshBuilder()
         rec.replay(ob, lambda m: O.Material.make(m.absorption, m.scattering, m.transmission))
         mesh = ob.build("f32")
-        P = O.params(tie_mode=1, n_bands=nb, n_bins=n_bins, bin_dt=0.001, max_time=tmax, max_bounces=200,
+        # the reference's algorithm: first-found closest hits on its own tree
+        P = O.params(tie_mode=0, n_bands=nb, n_bins=n_bins, bin_dt=0.001, max_time=tmax, max_bounces=200,
                      energy_floor=1e-6)
         t0 = time.perf_counter()
         _, _, st = O.trace_mesh(mesh, src, lis, n_rays, energy=[1.0] * nb, P=P, seed=seed, threads=threads)
         sec += time.perf_counter() - t0
-        seg += st["segments"]
-        nodes += st["node_reads"]
-        prims_t += st["prim_tests"]
-        hits += st["receiver_hits"]
+        for k in tot:
+            tot[k] += st[k]
         t0 = time.perf_counter()
         _, _, s1 = O.trace_mesh(mesh, src, lis, n_rays, energy=[1.0] * nb, P=P, seed=seed, threads=1,
                                 ray_end=min(n_rays, 256))
         sec1 += time.perf_counter() - t0
         seg1 += s1["segments"]
+    seg = tot["segments"]
     if seg:
         nbm = max(r[5] for r in oracle_jobs)
-        bseg = 32.0 * nodes / seg + 48.0 * prims_t / seg + 4.0 * (nbm + 3) * hits / seg
+        bseg, parts = bytes_per_segment(tot, nbm)
         peak, peak_kind = peaks()
         line["cpu_baseline"] = {"value": seg / sec, "unit": "ray-segments/s", "cores": threads, "kind": "port",
                                 "one_thread": seg1 / sec1,
-                                "sample": f"{len(oracle_jobs)} job(s) of the workload (f32 oracle)"}
+                                "sample": f"{len(oracle_jobs)} job(s) of the workload (f32 oracle, first-found "
+                                          f"rule, reference tree)"}
         line["roofline"] = {"bound": "hbm", "bytes_per_segment": bseg, "achieved": line["value"] * bseg / 1e9,
                             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                            "frac": line["value"] * bseg / 1e9 / peak}
+                            "frac": line["value"] * bseg / 1e9 / peak, **parts}
     if dome is not None:
         dseg = dres["segments"]["escape_events"] + dres["segments"]["through_calls"]
         line["dome"] = {"eyes": len(case.dome_eyes), "ms": float(np.mean(dms)), "segments": dseg,
@@ -596,7 +635,8 @@ def run_ours(args):
 
     line = None
     if rank == 0:
-        # CPU baseline + bytes per segment from the oracle's reference traversal
+        # CPU baseline (the reference's algorithm: first-found hits on its own
+        # tree, plus the fans) and bytes per segment from its traversal counters
         threads = os.cpu_count() or 1
         cpu = cpu_sample(case, args.ref_pairs, threads)
         bseg, parts = bytes_per_segment(cpu)
@@ -607,11 +647,12 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": WORKLOAD, "prims": scene.info()["prims"], "bvh": args.bvh,
-                       "l2": "flushed (256 MB write) before every timed step", "segments_per_step": segments,
-                       "dome_segments_per_step": dome_seg, "trace_ms": float(np.mean(trace_ms)),
-                       "step_ms": float(np.mean(step_ms)), "step_ms_max": float(np.max(step_ms)),
-                       "dome_alone_ms": float(np.mean(dome_ms)),
+            "config": config_of(scene.info()["prims"]),
+            "tie_rule": "near-tie rule (tie_mode 1: lowest surface id among hits within 1e-6 relative t) on the "
+                        f"{args.bvh} tree",
+            "detail": {"bvh": args.bvh, "segments_per_step": segments, "dome_segments_per_step": dome_seg,
+                       "trace_ms": float(np.mean(trace_ms)), "step_ms": float(np.mean(step_ms)),
+                       "step_ms_max": float(np.max(step_ms)), "dome_alone_ms": float(np.mean(dome_ms)),
                        "dome": "the 64 fans after the trace, on its stream", "autotune": tune,
                        "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
@@ -620,13 +661,16 @@ def run_ours(args):
             "gpu_launches": int(args.steps * (batch.kernel_count() + 3)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic(), "peak_kind": peak_kind,
-                         "bytes_per_segment": bseg, **{k: round(v, 4) for k, v in parts.items()},
+                         "bytes_per_segment": bseg, "segments_per_launch": segments,
+                         "trace_ms": float(np.mean(trace_ms)), **parts,
+                         "counters_from": f"the f32 oracle's reference traversal (first-found, reference SAH tree) "
+                                          f"on {args.ref_pairs} of {N_PAIRS} pairs: {cpu['segments']} segments",
                          "kernel": "the trace part of a step (persistent trace kernels, CUDA events on their "
                                    "stream)"},
-            "cpu_baseline": {"value": cpu["segments"] / cpu["seconds"], "unit": UNIT, "cores": threads,
-                             "kind": "port",
-                             "sample": f"{args.ref_pairs} of {N_PAIRS} pairs x {N_RAYS} rays (f32 oracle, "
-                                       f"{threads} threads)"},
+            "cpu_baseline": {"value": (cpu["segments"] + cpu["dome_segments"]) / cpu["seconds"], "unit": UNIT,
+                             "cores": threads, "kind": "port",
+                             "sample": f"{args.ref_pairs} of {N_PAIRS} pairs x {N_RAYS} rays and their dome fans "
+                                       f"(f32 oracle, the reference's first-found rule and tree, {threads} threads)"},
             "clocks": clk.summary(),
         }
         if args.surrogate:

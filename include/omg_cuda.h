@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define OMG_ABI_VERSION 1
+#define OMG_ABI_VERSION 2
 #define OMG_MAX_BANDS 8
 #define OMG_DOME_BINS 9          /* dome.rs:30: 8 azimuth sectors + zenith */
 
@@ -77,6 +77,14 @@ typedef struct omg_params {
                                     0 = the first one found in the reference's traversal
                                     order (mesh.rs:505, strict <); 1 = the lowest authored
                                     surface id, then triangle id (precision-independent) */
+    /* Device-side limits. Each ends the kernel's work early with a flag, so no
+     * kernel can spin; a call whose kernels raised a flag returns OMG_E_OVERFLOW
+     * and omg_last_flags() gives the flags. The context stays usable. */
+    uint32_t walk_budget;        /* node and leaf visits of one closest-hit walk before it stops
+                                    (flag 4); 0 = 2 x nodes + primitives + 64, which no walk of
+                                    a sound tree reaches. Smaller values cap it. */
+    uint32_t loop_guard;         /* loop iterations of one warp of a persistent trace kernel
+                                    before it stops (flag 8); 0 = 2^22 */
 } omg_params;
 
 /* LateBackend::trace job (late.rs:28-40): analytic shoebox [0,size]^3, walls in
@@ -168,6 +176,15 @@ int32_t omg_abi_version(void);
 const char* omg_status_string(int32_t status);
 /* Last CUDA error text of the context (empty when none). */
 const char* omg_last_error(const omg_ctx* ctx);
+/* Kernel flag word of the context's last trace or dome call that read one
+ * back: 0 = none; 1 traversal stack overflow, 2 crossing list overflow,
+ * 4 walk budget (omg_params.walk_budget), 8 persistent-kernel loop guard
+ * (omg_params.loop_guard). Any flag makes that call return OMG_E_OVERFLOW. */
+uint32_t omg_last_flags(const omg_ctx* ctx);
+/* Change the context's device-side limits (omg_params.walk_budget and
+ * loop_guard; 0 = default) for every later call, batches already created
+ * included. Waits for the context's stream first. */
+int32_t omg_set_limits(omg_ctx* ctx, uint32_t walk_budget, uint32_t loop_guard);
 /* Launch work of this context on a caller stream (a cudaStream_t; NULL = the
  * context's own stream). */
 int32_t omg_set_stream(omg_ctx* ctx, void* cuda_stream);
@@ -566,18 +583,28 @@ int32_t omg_tc_gemm(omg_ctx* ctx, const uint16_t* a, const uint16_t* b, float* c
  * allocator. The caller passes the job, the constants and its own DEVICE
  * output buffers bins_dev[n_bins*n_bands] and dirs_dev[n_bins*3]; the work is
  * queued on cuda_stream (NULL = the legacy default stream) and the call
- * returns without waiting. The scratch memory lives in one fixed device array
- * per GPU (kept until the process exits), so:
+ * returns without waiting. flags_dev (nullable) is a caller device word that
+ * receives the kernels' flag word, as omg_last_flags describes it: 0 when the
+ * trace ran to its end, else the trace was cut short (traversal stack, walk
+ * budget, params->loop_guard) and the echogram is incomplete; read it after
+ * the stream has reached the call. The job is checked as omg_trace_box checks
+ * it (finite positions and size, finite materials): OMG_E_INVALID otherwise.
+ * The scratch memory lives in one fixed device array per GPU (kept until the
+ * process exits), so:
  *  - n_bins * (n_bands + 3) must not exceed OMG_NOALLOC_MAX_CELLS, else
  *    OMG_E_INVALID (about 352 KB of device memory per GPU);
  *  - calls that overlap on the GPU race on that array: order them on one
  *    stream;
- *  - the first call on a device looks up the array's address (once per
- *    device); make it before any stream capture.
+ *  - the first call on a device looks up the array's address and loads every
+ *    kernel a call may launch (3 or 8 bands, either tie_mode), once per
+ *    device, so that no later call waits on the driver's lazy kernel loading;
+ *    make it before any stream capture;
+ *  - the address is kept for the life of the process: cudaDeviceReset while
+ *    this entry point is in use is not supported.
  * It allocates nothing: no cudaMalloc, no cudaFree, no allocating library call. */
 #define OMG_NOALLOC_MAX_CELLS 45056   /* 4096 bins x (8 bands + 3) */
 int32_t omg_trace_box_noalloc(const omg_box_job* job, const omg_params* params, float* bins_dev, float* dirs_dev,
-                              void* cuda_stream);
+                              uint32_t* flags_dev, void* cuda_stream);
 
 #ifdef __cplusplus
 }

@@ -31,7 +31,8 @@ class omg_params(C.Structure):
     _fields_ = [("n_bands", C.c_uint32), ("n_bins", C.c_uint32), ("bin_dt", C.c_float), ("max_time", C.c_float),
                 ("max_bounces", C.c_uint32), ("energy_floor", C.c_float), ("receiver_radius", C.c_float),
                 ("wall_eps", C.c_float), ("speed_of_sound", C.c_float), ("dir_band", C.c_uint32),
-                ("device", C.c_int32), ("timeout_ms", C.c_uint32), ("tie_mode", C.c_uint32)]
+                ("device", C.c_int32), ("timeout_ms", C.c_uint32), ("tie_mode", C.c_uint32),
+                ("walk_budget", C.c_uint32), ("loop_guard", C.c_uint32)]
 
 
 class omg_box_job(C.Structure):
@@ -123,6 +124,8 @@ SIGNATURES = {
     "omg_abi_version": (I32, []),
     "omg_status_string": (C.c_char_p, [I32]),
     "omg_last_error": (C.c_char_p, [P]),
+    "omg_last_flags": (U32, [P]),
+    "omg_set_limits": (I32, [P, U32, U32]),
     "omg_set_stream": (I32, [P, P]),
     "omg_mb_create": (P, []),
     "omg_mb_destroy": (None, [P]),
@@ -181,7 +184,7 @@ SIGNATURES = {
     "omg_mlp_params": (I32, [P, U32, U32, P, PU64]),
     "omg_mlp_set_params": (I32, [P, U32, U32, P, U64]),
     "omg_tc_gemm": (I32, [P, P, P, P, U32, U32, U32]),
-    "omg_trace_box_noalloc": (I32, [C.POINTER(omg_box_job), C.POINTER(omg_params), P, P, P]),
+    "omg_trace_box_noalloc": (I32, [C.POINTER(omg_box_job), C.POINTER(omg_params), P, P, P, P]),
     "omg_early_create": (I32, [P, U32, P, U32, PU32]),
     "omg_early_destroy": (I32, [P, U32]),
     "omg_early_info": (I32, [P, U32, PU32, PU32]),

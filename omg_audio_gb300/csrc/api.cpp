@@ -41,7 +41,8 @@ bool valid_material(const omg_material& m, uint32_t nb) {
 
 bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
 
-DScene scene_view(const SceneRec& s) {
+// walk_cap: omg_params.walk_budget (0: no cap below the structural bound)
+DScene scene_view(const SceneRec& s, uint32_t walk_cap) {
   DScene d;
   std::memset(&d, 0, sizeof(d));
   d.nodes = s.nodes.p;
@@ -59,6 +60,10 @@ DScene scene_view(const SceneRec& s) {
   for (int a = 0; a < 3; a++) d.fast_m[a] = s.fast_m[a];
   d.root4 = s.root4;
   d.n_nodes4 = s.n_nodes4;
+  const uint64_t b2 = 2ull * s.n_nodes + s.n_prims + 64ull, b4 = (uint64_t)s.n_nodes4 + 1ull;
+  const uint64_t cap = walk_cap ? walk_cap : 0xFFFFFFFFull;
+  d.walk_budget = (uint32_t)std::min(std::min(b2, cap), (uint64_t)0xFFFFFFFFull);
+  d.walk_budget4 = (uint32_t)std::min(b4, cap);
   return d;
 }
 
@@ -72,7 +77,7 @@ int32_t sync_scene_table(omg_ctx* ctx) {
   }
   std::vector<DScene> table(ctx->scene_cap);
   std::memset(table.data(), 0, table.size() * sizeof(DScene));
-  for (auto& kv : ctx->scenes) table[kv.first] = scene_view(*kv.second);
+  for (auto& kv : ctx->scenes) table[kv.first] = scene_view(*kv.second, ctx->prm.walk_budget);
   CK(cudaMemcpy(ctx->d_scenes.p, table.data(), table.size() * sizeof(DScene), cudaMemcpyHostToDevice));
   return OMG_OK;
 }
@@ -323,6 +328,7 @@ int32_t record_launch(omg_ctx* ctx, BatchRec& B, cudaStream_t s, int parts = 3) 
     CK(cudaMemsetAsync(B.d_ep_ctl.p, 0, (kMaxEpochs + 1) * sizeof(EpochCtl), s));
     // cooperative walks need the near-tie rule and a 4-wide tree in every scene
     LaunchShape eff = B.shape;
+    eff.loop_guard = ctx->prm.loop_guard;
     if (eff.mode == 2 && !B.coop_ok) eff.mode = 0;
     if (eff.tail_mode == 2 && !B.coop_ok) eff.tail_mode = 0;
     CK(launch_wavefront(B.d_jobs.p, B.n_jobs, B.total_rays, B.max_nb, ctx->d_scenes.p, B.d_job_mats.p,
@@ -393,6 +399,7 @@ int32_t prepare_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n
 }
 
 int32_t check_kernel_flags(omg_ctx* ctx, const BatchRec& B) {
+  ctx->last_flags = B.h_hdr.p->error;
   if (B.h_hdr.p->error) {
     ctx->last_error = "trace kernel: traversal stack, walk budget or loop guard exceeded (flags " +
                       std::to_string(B.h_hdr.p->error) + ")";
@@ -556,6 +563,24 @@ const char* omg_status_string(int32_t s) {
 }
 
 const char* omg_last_error(const omg_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+uint32_t omg_last_flags(const omg_ctx* ctx) { return ctx ? ctx->last_flags : 0u; }
+
+int32_t omg_set_limits(omg_ctx* ctx, uint32_t walk_budget, uint32_t loop_guard) {
+  if (!ctx) return OMG_E_INVALID;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, cudaGetLastError(), "cudaSetDevice");
+  // nothing of this context may be in flight while its tables and graphs change
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->prm.walk_budget = walk_budget;
+  ctx->prm.loop_guard = loop_guard;
+  int32_t rc = sync_scene_table(ctx);   // the walk budgets live in the scene records
+  if (rc) return rc;
+  // the loop guard is a kernel argument recorded in each batch's graphs
+  ctx->cached.reset();
+  for (auto& kv : ctx->batches)
+    if ((rc = build_graphs(ctx, *kv.second))) return rc;
+  return OMG_OK;
+}
 
 omg_ctx* omg_create(const omg_params* p) {
   omg_params prm;

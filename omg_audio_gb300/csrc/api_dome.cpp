@@ -236,6 +236,7 @@ int32_t dome_collect(omg_ctx* ctx, DomeRec& D, omg_dome_bin* out, float* raw_ene
   D.pending = false;
   const uint32_t nb = D.nb, n_eyes = D.p_eyes;
   const uint64_t nr = (uint64_t)n_eyes * D.p_rays;
+  ctx->last_flags = D.h_hdr.p->error;
   if (D.h_hdr.p->error) {
     ctx->last_error = (D.h_hdr.p->error & 2u) ? "dome: too many crossings on one straight-through segment"
                                               : "dome: traversal stack overflow";

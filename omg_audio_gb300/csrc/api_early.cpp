@@ -60,7 +60,7 @@ int32_t early_view(omg_ctx* ctx, const EarlyRec& R, DEarly& E) {
   auto it = ctx->scenes.find(R.scene_id);
   if (it == ctx->scenes.end()) return OMG_E_NOT_FOUND;
   std::memset(&E, 0, sizeof(E));
-  E.S = scene_view(*it->second);
+  E.S = scene_view(*it->second, ctx->prm.walk_budget);
   E.surf = R.surf.p;
   E.n_surf = R.n_surf;
   E.base_overlay = R.base_overlay;

@@ -27,7 +27,6 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr uint32_t kQ = 64;                 // warp queues (at most 8 + 31 + 32 rays owned, see below)
 constexpr int kDoneC = 0x7FFFFFFF;
-constexpr uint32_t kMaxLoopC = 1u << 22;    // warp loop guard (error 8)
 constexpr int kGroupsPerBlock = 64;         // 256 threads / 4
 
 // Two lanes' near-tie states merged (TieState, device_common.cuh): the union
@@ -126,7 +125,7 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
     const bool walkable = J.geom == OMG_GEOM_MESH && S.n_prims != 0u && nodes != nullptr;
     cur = walkable ? S.root4 : kDoneC;
     root = cur;
-    budget0 = walkable ? S.n_nodes4 + 1u : 1u;   // every node is entered at most once per pass
+    budget0 = walkable ? S.walk_budget4 : 1u;   // every node is entered at most once per pass
     budget = budget0;
     sp = 0;
     have = false;
@@ -157,7 +156,7 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
 
   uint32_t iters = 0;
   while (true) {
-    if (++iters > kMaxLoopC) {
+    if (++iters > ea.max_loop) {
       atomicOr(err, 8u);
       break;
     }

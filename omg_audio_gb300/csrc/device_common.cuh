@@ -288,7 +288,7 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
   int leaf = 0;                      // postponed leaf (< 0), or 0
   // every node and leaf is visited at most once per ray and pass: a walk
   // longer than this bound means a corrupt tree; stop and flag it rather than spin
-  uint32_t budget = 2u * S.n_nodes + S.n_prims + 64u;
+  uint32_t budget = S.walk_budget;
   auto culled = [&](float t) { return TIE ? t > t_cull : (have && t >= t_best); };
   // next stacked entry that is not culled, or kDone
   auto pop = [&]() -> int {
@@ -383,7 +383,7 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
     sp = 0;
     cur = S.root;
     leaf = 0;
-    budget = 2u * S.n_nodes + S.n_prims + 64u;
+    budget = S.walk_budget;
   }
   return have;
 }
@@ -472,7 +472,7 @@ __device__ __forceinline__ bool mesh_closest4(const DScene& S, float ox, float o
   float stack_t[STACK_DEPTH];
   int sp = 0;
   int cur = S.root4;
-  uint32_t budget = S.n_nodes4 + 1u;   // every node is entered at most once per pass
+  uint32_t budget = S.walk_budget4;   // every node is entered at most once per pass
   while (true) {
     while (cur != kDone4) {
       if (budget-- == 0u) {
@@ -490,7 +490,7 @@ __device__ __forceinline__ bool mesh_closest4(const DScene& S, float ox, float o
     t_best = FLT_MAX;
     sp = 0;
     cur = S.root4;
-    budget = S.n_nodes4 + 1u;
+    budget = S.walk_budget4;
   }
   return have;
 }

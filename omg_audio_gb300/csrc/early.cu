@@ -258,7 +258,7 @@ __device__ void segment_hits(const DEarly& E, float ax, float ay, float az, floa
   int stack[STACK_DEPTH];
   int sp = 0;
   stack[sp++] = S.root;
-  uint32_t budget = 2u * S.n_nodes + S.n_prims + 64u;
+  uint32_t budget = S.walk_budget;
   bool full = false;
   while (sp > 0) {
     if (budget-- == 0u) {

@@ -9,6 +9,9 @@
 // segment counter, the job and wall-material records) lives in one
 // file-scope device array of fixed size. The caller passes the job and its
 // own device output buffers; the call allocates nothing and does not wait.
+// The kernels' flag word (traversal stack, walk budget, loop guard) goes to
+// the caller's optional device word flags_dev, written by the last kernel of
+// the call: 0 when the trace ran to its end.
 //
 // Limits and sharing:
 //  - n_bins * (n_bands + 3) <= OMG_NOALLOC_MAX_CELLS (larger jobs are rejected
@@ -18,8 +21,12 @@
 //    overlap on the GPU (different streams, or different host threads without
 //    ordering) race on it;
 //  - the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (once per device); make that first call before any
-//    stream capture.
+//    cudaGetSymbolAddress and loads every kernel the call may launch (the
+//    trace kernel for 3 and 8 bands, with and without the near-tie rule), so
+//    that no later call waits for the driver to load one (CUDA loads kernels
+//    lazily by default); make that first call before any stream capture;
+//  - the address is looked up once per device for the life of the process:
+//    a cudaDeviceReset while this entry point is in use is not supported.
 #include <cstring>
 #include <mutex>
 
@@ -27,6 +34,9 @@
 #include "scene.h"
 
 namespace omg {
+
+bool valid_material(const omg_material& m, uint32_t nb);   // api.cpp
+bool finite3(const float* v);                               // api.cpp
 
 namespace {
 
@@ -63,10 +73,13 @@ __global__ void noalloc_setup_kernel(float* scratch, DJob job, WallMats walls, u
   }
 }
 
-// (sum + comp) * 2^-64 into the caller's buffers (the accumulators are scaled, kAccScale)
+// (sum + comp) * 2^-64 into the caller's buffers (the accumulators are scaled,
+// kAccScale), and the kernels' flag word into *flags (when given)
 __global__ void noalloc_finalize_kernel(const float* scratch, uint32_t n_bins, uint32_t nb, float* bins,
-                                        float* dirs) {
+                                        float* dirs, uint32_t* flags) {
   const uint32_t nbb = n_bins * nb, nd = n_bins * 3;
+  if (flags && blockIdx.x == 0 && threadIdx.x == 0)
+    *flags = reinterpret_cast<const DLaunch*>(scratch + kHdrOff)->error;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nbb + nd; i += gridDim.x * blockDim.x) {
     if (i < nbb) bins[i] = (scratch[i] + scratch[nbb + i]) * kAccUnscale;
     else dirs[i - nbb] = (scratch[2 * nbb + (i - nbb)] + scratch[2 * nbb + nd + (i - nbb)]) * kAccUnscale;
@@ -89,6 +102,12 @@ cudaError_t scratch_for(int dev, float** out, int* n_sms) {
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
+    // load now every kernel a call may launch (lazy loading would otherwise
+    // load each on its first launch, inside a caller's time-critical call)
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, noalloc_setup_kernel)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&fa, noalloc_finalize_kernel)) != cudaSuccess) return e;
+    if ((e = preload_trace_kernels()) != cudaSuccess) return e;
     g_addr[dev] = static_cast<float*>(p);
     g_sms[dev] = sms;
   }
@@ -104,12 +123,16 @@ cudaError_t scratch_for(int dev, float** out, int* n_sms) {
 using namespace omg;
 
 extern "C" int32_t omg_trace_box_noalloc(const omg_box_job* job, const omg_params* prm, float* bins_dev,
-                                         float* dirs_dev, void* cuda_stream) {
+                                         float* dirs_dev, uint32_t* flags_dev, void* cuda_stream) {
   if (!job || !prm || !bins_dev || !dirs_dev) return OMG_E_INVALID;
   const uint32_t nb = prm->n_bands, n_bins = prm->n_bins;
   if (nb == 0 || nb > (uint32_t)MAXB || n_bins == 0 || job->n_rays == 0 || prm->dir_band >= nb ||
       !(prm->bin_dt > 0.0f) || !(prm->speed_of_sound > 0.0f))
     return OMG_E_INVALID;
+  // the checks omg_trace_box makes on a box job: finite geometry and materials
+  if (!finite3(job->src) || !finite3(job->lis) || !finite3(job->size)) return OMG_E_INVALID;
+  for (int w = 0; w < 6; w++)
+    if (!valid_material(job->walls[w], nb)) return OMG_E_INVALID;
   if ((uint64_t)n_bins * (nb + 3) > kCells) return OMG_E_INVALID;  // beyond the fixed scratch
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
@@ -156,6 +179,7 @@ extern "C" int32_t omg_trace_box_noalloc(const omg_box_job* job, const omg_param
   const uint32_t acc = (uint32_t)(2ull * n_bins * (nb + 3));
   noalloc_setup_kernel<<<64, 256, 0, s>>>(scratch, d, walls, acc);
   LaunchShape shape;
+  shape.loop_guard = prm->loop_guard;
   cudaError_t e = launch_trace(reinterpret_cast<const DJob*>(scratch + kJobOff), 1, job->n_rays, nb, nullptr,
                                reinterpret_cast<const DMat*>(scratch + kMatOff), nullptr, nullptr, scratch,
                                reinterpret_cast<DLaunch*>(scratch + kHdrOff),
@@ -164,7 +188,7 @@ extern "C" int32_t omg_trace_box_noalloc(const omg_box_job* job, const omg_param
     cudaGetLastError();
     return OMG_E_DEVICE;
   }
-  noalloc_finalize_kernel<<<16, 256, 0, s>>>(scratch, n_bins, nb, bins_dev, dirs_dev);
+  noalloc_finalize_kernel<<<16, 256, 0, s>>>(scratch, n_bins, nb, bins_dev, dirs_dev, flags_dev);
   if (cudaGetLastError() != cudaSuccess) return OMG_E_DEVICE;
   return OMG_OK;
 }

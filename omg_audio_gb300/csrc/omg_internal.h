@@ -69,6 +69,13 @@ struct DScene {
   // Möller–Trumbore accepts just outside a triangle; null: a leaf root.
   const float4* nodes_f;
   float fast_m[3];
+  // Node and leaf visits one closest-hit walk may take before it stops and
+  // flags error 4: every node is entered at most once per pass, so a longer walk
+  // means a corrupt tree. walk_budget = min(2 n_nodes + n_prims + 64, the
+  // context's omg_params.walk_budget); walk_budget4 the same for the 4-wide tree
+  // (n_nodes4 + 1).
+  uint32_t walk_budget;
+  uint32_t walk_budget4;
 };
 constexpr int32_t kEmpty4 = 0x7FFFFFFE;
 
@@ -159,7 +166,10 @@ struct LaunchShape {
   uint32_t park_pct = 50;       // an epoch parks its rays once at most this % of them remain
   uint32_t park_min = 4096;     // epochs of at most this many rays run to the end
   uint32_t wl_shade_min = 32;   // modes 1 and 2: rays a warp shades together once that many wait
+  uint32_t loop_guard = 0;      // loop iterations of one warp of a persistent kernel before it stops
+                                // and flags error 8 (0: kDefaultLoopGuard); from omg_params.loop_guard
 };
+constexpr uint32_t kDefaultLoopGuard = 1u << 22;
 
 // Wavefront state (wavefront.cu). One record per ray of the batch, indexed by
 // the ray's global id, holds everything the bounce loop carries from one
@@ -203,6 +213,7 @@ struct EpochArgs {
   uint32_t park_pct;
   uint32_t park_min;
   WfState st;            // per-ray records (saved and restored state)
+  uint32_t max_loop;     // the persistent kernels' per-warp loop guard (error 8)
 };
 
 // ----------------------------------------------------------- kernel launchers
@@ -212,6 +223,10 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
                          const DPanelGroup* groups, float* acc,
                          DLaunch* hdr, uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie,
                          cudaStream_t s, const EpochArgs* ep = nullptr);
+// trace.cu: load the per-lane trace kernel variants launch_trace may pick for a
+// single launch (3 and 8 bands, with and without the near-tie rule) now, so
+// that a later launch does not wait for the driver's lazy module loading.
+cudaError_t preload_trace_kernels();
 // coop.cu: the mode-2 persistent kernel (same arguments as launch_trace).
 cudaError_t launch_trace_coop(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
                               const DScene* scenes, const DMat* job_mats, const DPanel* panels,

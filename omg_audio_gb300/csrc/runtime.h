@@ -155,6 +155,7 @@ struct omg_ctx {
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   std::string last_error;
+  uint32_t last_flags = 0;   // kernel flag word of the last trace or dome call (omg_last_flags)
   std::map<uint32_t, std::unique_ptr<omg::SceneRec>> scenes;
   uint32_t next_scene = 1;
   omg::DevBuf<omg::DScene> d_scenes;           // scene table indexed by scene id
@@ -191,7 +192,7 @@ uint32_t timeout_of(const omg_ctx* ctx);
 int32_t wait_event(omg_ctx* ctx, cudaEvent_t ev, uint32_t timeout_ms);
 int32_t sync_scene_table(omg_ctx* ctx);
 // The device view of an uploaded scene (one entry of the scene table).
-DScene scene_view(const SceneRec& s);
+DScene scene_view(const SceneRec& s, uint32_t walk_cap);
 // api.cpp: a batch record for `jobs` (allocations, uploads, launch graphs);
 // the same record refilled with new per-job values when the job layout
 // (batch_layout) is unchanged; the kernels' error flags of its last read-back.

@@ -55,10 +55,6 @@ __device__ __forceinline__ float walk_cull(const Walk& w) {
 }
 
 constexpr int kDone = 0x7FFFFFFF;  // never a node index (< 2^28)
-// Loop iterations of one warp of a persistent kernel before it gives up and
-// flags error 8: far above any legitimate count (each iteration advances a
-// walk, a shading pass or the ray queue).
-constexpr uint32_t kMaxLoop = 1u << 22;
 
 template <bool TIE>
 __device__ __forceinline__ int walk_pop(Walk& w) {
@@ -91,7 +87,7 @@ __device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float ox, f
   const float kTiny = 8.673617379884035e-19f;   // 2^-60
   w.fast = fabsf(ox) <= 7.0f * S.fast_m[0] && fabsf(oy) <= 7.0f * S.fast_m[1] && fabsf(oz) <= 7.0f * S.fast_m[2] &&
            fabsf(dx) >= kTiny && fabsf(dy) >= kTiny && fabsf(dz) >= kTiny;
-  w.budget = 2u * S.n_nodes + S.n_prims + 64u;
+  w.budget = S.walk_budget;
 }
 
 // A near-tie walk that ended with an ambiguous window starts over in fixed
@@ -158,7 +154,7 @@ __device__ __forceinline__ bool walk4_steps(Walk& w, const DScene& S, float ox, 
                                             float dy, float dz, int steps, uint32_t* err) {
   while (steps-- > 0) {
     if (w.cur == kDone) {
-      if (!walk_restart_fixed(w, S.root4, 2u * S.n_nodes + S.n_prims + 64u)) break;
+      if (!walk_restart_fixed(w, S.root4, S.walk_budget)) break;
       continue;
     }
     if (w.budget-- == 0u) {
@@ -186,7 +182,7 @@ __device__ __forceinline__ bool walk4_steps(Walk& w, const DScene& S, float ox, 
     w.t_min = ts.t_min;
     w.flags = (ts.amb ? kWalkAmb : 0u) | (ts.fixed ? kWalkFixed : 0u);
   }
-  if (w.cur == kDone) walk_restart_fixed(w, S.root4, 2u * S.n_nodes + S.n_prims + 64u);
+  if (w.cur == kDone) walk_restart_fixed(w, S.root4, S.walk_budget);
   return w.cur == kDone;
 }
 
@@ -272,7 +268,7 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
   }
   if (w.cur == kDone && w.leaf == 0) {
     // an ambiguous near-tie window: the walk starts over in fixed mode
-    return !walk_restart_fixed(w, S.root, 2u * S.n_nodes + S.n_prims + 64u);
+    return !walk_restart_fixed(w, S.root, S.walk_budget);
   }
   return false;
 }
@@ -406,7 +402,7 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
   };
 
   while (true) {
-    if (++iters > kMaxLoop) {
+    if (++iters > ea.max_loop) {
       atomicOr(err, 8u);
       break;
     }
@@ -619,7 +615,7 @@ __global__ void __launch_bounds__(256, 4) trace_wl_kernel(const DJob* __restrict
 
   uint32_t iters = 0;   // loop guard (warp-uniform)
   while (true) {
-    if (++iters > kMaxLoop) {
+    if (++iters > ea.max_loop) {
       atomicOr(err, 8u);
       break;
     }
@@ -759,6 +755,10 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
   if (n_jobs == 0 || total_rays == 0) return cudaSuccess;
   EpochArgs ea{};
   if (ep) ea = *ep;
+  // loop iterations of one warp of a persistent kernel before it gives up and
+  // flags error 8: by default far above any legitimate count (each iteration
+  // advances a walk, a shading pass or the ray queue)
+  ea.max_loop = shape.loop_guard ? shape.loop_guard : kDefaultLoopGuard;
   if (shape.mode == 2 && tie && ea.st.pos)
     return launch_trace_coop(jobs, n_jobs, total_rays, max_nb, scenes, job_mats, panels, groups, acc, hdr,
                              job_segments, shape, n_sms, ea, s);
@@ -790,6 +790,15 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
   }
 #undef OMG_TRACE_LAUNCH
   return cudaGetLastError();
+}
+
+cudaError_t preload_trace_kernels() {
+  cudaFuncAttributes fa;
+  cudaError_t e;
+  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<3, false>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<3, true>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<8, false>)) != cudaSuccess) return e;
+  return cudaFuncGetAttributes(&fa, trace_kernel<8, true>);
 }
 
 cudaError_t launch_finalize(const DJob* jobs, uint32_t n_jobs, const float* acc, float* out, uint64_t total_out,

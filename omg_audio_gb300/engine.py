@@ -42,11 +42,14 @@ class TraceConfig:
     device: int = 0
     timeout_ms: int = 20000
     tie_mode: int = 0          # 0: reference first-found; 1: lowest surface id among near-ties
+    walk_budget: int = 0       # visits of one closest-hit walk before it stops (flag 4); 0: structural bound
+    loop_guard: int = 0        # per-warp loop iterations of a persistent trace kernel (flag 8); 0: 2^22
 
     def to_c(self) -> _lib.omg_params:
         p = _lib.omg_params()
         for k in ("n_bands", "n_bins", "bin_dt", "max_time", "max_bounces", "energy_floor", "receiver_radius",
-                  "wall_eps", "speed_of_sound", "dir_band", "device", "timeout_ms", "tie_mode"):
+                  "wall_eps", "speed_of_sound", "dir_band", "device", "timeout_ms", "tie_mode", "walk_budget",
+                  "loop_guard"):
             setattr(p, k, getattr(self, k))
         return p
 
@@ -106,6 +109,16 @@ class Context:
 
     def last_error(self) -> str:
         return lib().omg_last_error(self.h).decode()
+
+    def set_limits(self, walk_budget: int = 0, loop_guard: int = 0) -> None:
+        """Device-side limits for later calls (omg_set_limits; 0 = default)."""
+        self._check(lib().omg_set_limits(self.h, walk_budget, loop_guard), "omg_set_limits")
+        self.cfg.walk_budget, self.cfg.loop_guard = walk_budget, loop_guard
+
+    def last_flags(self) -> int:
+        """Kernel flag word of the last trace or dome call (omg_last_flags):
+        1 stack overflow, 2 crossing list overflow, 4 walk budget, 8 loop guard."""
+        return int(lib().omg_last_flags(self.h))
 
     def _check(self, rc: int, what: str):
         if rc < 0:

@@ -25,6 +25,23 @@ struct BoxPanelC {
   Material m;
 };
 
+void add_trav(TraversalStats& a, const TraversalStats& b) {
+  a.node_reads += b.node_reads;
+  a.prim_tests += b.prim_tests;
+  a.queries += b.queries;
+  a.internal_visits += b.internal_visits;
+  a.leaf_visits += b.leaf_visits;
+  a.child_boxes += b.child_boxes;
+  a.unique_nodes += b.unique_nodes;
+}
+
+// The traversal counters as 7 words: node_reads, prim_tests, queries,
+// internal_visits, leaf_visits, child_boxes, unique_nodes.
+void trav_out(const TraversalStats& t, uint64_t* o) {
+  o[0] = t.node_reads; o[1] = t.prim_tests; o[2] = t.queries; o[3] = t.internal_visits;
+  o[4] = t.leaf_visits; o[5] = t.child_boxes; o[6] = t.unique_nodes;
+}
+
 template <class R>
 std::vector<BoxPanel<R>> panels_of(const BoxPanelC* p, uint32_t n) {
   std::vector<BoxPanel<R>> v(n);
@@ -88,9 +105,16 @@ void run_trace(HitFn hitfn, const TraceParams& P, const float* src, const float*
     dirs_out[i] = acc;
   }
   if (stats_out) {
-    uint64_t seg = 0, hits = 0, nodes = 0, prims = 0;
-    for (auto& t : ts) { seg += t.segments; hits += t.receiver_hits; nodes += t.trav.node_reads; prims += t.trav.prim_tests; }
-    stats_out[0] = seg; stats_out[1] = hits; stats_out[2] = nodes; stats_out[3] = prims;
+    // segments, receiver hits, then the traversal counters (trav_out)
+    uint64_t seg = 0, hits = 0;
+    TraversalStats tr;
+    for (auto& t : ts) {
+      seg += t.segments;
+      hits += t.receiver_hits;
+      add_trav(tr, t.trav);
+    }
+    stats_out[0] = seg; stats_out[1] = hits;
+    trav_out(tr, stats_out + 2);
   }
 }
 
@@ -209,7 +233,7 @@ int orc_mesh_raycast(void* hv, const float* o, const float* d, uint32_t n, int b
     t_out[i] = t;
     tri_out[i] = tri;
   }
-  if (stats) { stats[0] = st.node_reads; stats[1] = st.prim_tests; }
+  if (stats) trav_out(st, stats);
   return 0;
 }
 
@@ -425,7 +449,7 @@ int orc_dome_sample(void* dv, const float* eye, const DomePanel* leaves, uint32_
   }
   if (stats) {
     stats[0] = st.escape_events; stats[1] = st.through_calls;
-    stats[2] = st.trav.node_reads; stats[3] = st.trav.prim_tests;
+    trav_out(st.trav, stats + 2);
   }
   return 0;
 }

@@ -164,9 +164,20 @@ inline V3<R> unit_sphere(G& g) {
 }
 
 // ----------------------------------------------------------------- geometry
+// Traversal counters. The reference's ordered walk (mesh.rs:484-541) reads a
+// popped node's record, and for an internal node both children's records (their
+// boxes); a child popped later is the record its parent already read. So the
+// DISTINCT 32-byte records a closest-hit query touches are the root plus the
+// children of every internal node it processes: unique_nodes = queries +
+// child_boxes. node_reads counts every read, repeats included.
 struct TraversalStats {
-  uint64_t node_reads = 0;   // BvhNode records read (32 B each in the flattened layout)
-  uint64_t prim_tests = 0;   // PackedTri records tested (48 B each)
+  uint64_t node_reads = 0;       // BvhNode records read, repeats included (32 B each in the flattened layout)
+  uint64_t prim_tests = 0;       // PackedTri records tested (48 B each)
+  uint64_t queries = 0;          // closest-hit or crossing queries
+  uint64_t internal_visits = 0;  // internal nodes popped and processed
+  uint64_t leaf_visits = 0;      // leaves popped and processed
+  uint64_t child_boxes = 0;      // child boxes read by internal visits (2 each)
+  uint64_t unique_nodes = 0;     // distinct node records touched per query, summed over queries
 };
 
 template <class R>
@@ -550,6 +561,7 @@ struct Mesh {
     auto key_less = [](uint32_t as, uint32_t atr, R at, uint32_t bs, uint32_t btr, R btt) {
       return as < bs || (as == bs && (atr < btr || (atr == btr && at < btt)));
     };
+    if (st) { st->queries++; st->unique_nodes++; }
     for (int pass = 0; pass < 2; pass++) {
       uint32_t sn[64];
       R stt[64];
@@ -563,6 +575,7 @@ struct Mesh {
         const BvhNode<R>& node = nodes[ni];
         if (st) st->node_reads++;
         if (node.a & LEAF_BIT) {
+          if (st) st->leaf_visits++;
           uint32_t start = node.a & ~LEAF_BIT;
           for (uint32_t i = start; i < start + node.b; i++) {
             const PackedTri<R>& pt = packed[i];
@@ -604,7 +617,15 @@ struct Mesh {
           R tmax = (tie || have) ? bcull : RMAX;
           const BvhNode<R>& l = nodes[node.a];
           const BvhNode<R>& r = nodes[node.b];
-          if (st) st->node_reads += 2;
+          if (st) {
+            st->node_reads += 2;
+            st->internal_visits++;
+            st->child_boxes += 2;
+            // counted on the first pass only: exact for the reference's
+            // one-pass walk; a near-tie walk's fixed-window second pass
+            // re-reads (mostly) records the first pass touched
+            if (pass == 0) st->unique_nodes += 2;
+          }
           R ta, tb;
           bool hl, hr;
           if (tie) {
@@ -669,12 +690,15 @@ struct Mesh {
     stack[0] = 0;
     struct H { R t; uint32_t tri; uint16_t mat; };
     std::vector<H> hs;
+    if (st) st->queries++;
     while (sp > 0) {
       sp--;
       const BvhNode<R>& node = nodes[stack[sp]];
-      if (st) st->node_reads++;
+      // this walk tests each node's own box when it pops it: every record once
+      if (st) { st->node_reads++; st->unique_nodes++; }
       R tdummy;
       if (!ray_aabb(node.bmin, node.bmax, a, inv_d, len, &tdummy)) continue;
+      if (st) (node.a & LEAF_BIT) ? st->leaf_visits++ : st->internal_visits++;
       if (node.a & LEAF_BIT) {
         uint32_t start = node.a & ~LEAF_BIT;
         for (uint32_t i = start; i < start + node.b; i++) {

@@ -141,6 +141,15 @@ def _p(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
 
 
+TRAV_KEYS = ("node_reads", "prim_tests", "queries", "internal_visits", "leaf_visits", "child_boxes",
+             "unique_nodes")
+
+
+def _trav(st) -> dict:
+    """The traversal counters (omg_oracle.hpp TraversalStats) by name."""
+    return {k: int(v) for k, v in zip(TRAV_KEYS, st)}
+
+
 def _f3(v):
     return np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(3))
 
@@ -236,9 +245,9 @@ class Mesh:
         n = len(o)
         t = np.zeros(n, np.float64)
         tri = np.zeros(n, np.uint32)
-        st = np.zeros(2, np.uint64)
+        st = np.zeros(7, np.uint64)
         lib().orc_mesh_raycast(self.h, _p(o), _p(d), n, int(brute) | (2 if tie else 0), _p(t), _p(tri), _p(st))
-        return t, tri, dict(node_reads=int(st[0]), prim_tests=int(st[1]))
+        return t, tri, _trav(st)
 
     def segment_hits(self, a, b, cap: int = 256):
         fa, fb = _f3(a), _f3(b)
@@ -268,7 +277,7 @@ def _trace_common(fn, first, real, panels, P, src, lis, n_rays, energy, rng, see
     nb = P.n_bands
     bins = np.zeros((P.n_bins, nb), np.float64)
     dirs = np.zeros((P.n_bins, 3), np.float64)
-    st = np.zeros(4, np.uint64)
+    st = np.zeros(2 + 7, np.uint64)
     e = np.zeros(MAXB, np.float32)
     e[:nb] = np.asarray(energy, np.float32)[:nb]
     parr, np_ = _panels_arr(panels)
@@ -277,8 +286,7 @@ def _trace_common(fn, first, real, panels, P, src, lis, n_rays, energy, rng, see
             C.byref(P), _p(_f3(src)), _p(_f3(lis)), n_rays, _p(e), (0 if rng == "xorshift" else 1) | (0x10 if acc64 else 0), seed,
             ray_begin, ray_end, threads, _p(bins), _p(dirs), _p(st))
     assert rc == 0, rc
-    return bins, dirs, dict(segments=int(st[0]), receiver_hits=int(st[1]), node_reads=int(st[2]),
-                            prim_tests=int(st[3]))
+    return bins, dirs, dict(segments=int(st[0]), receiver_hits=int(st[1]), **_trav(st[2:]))
 
 
 def trace_box(size, walls, src, lis, n_rays, energy=(1, 1, 1), P=None, *, real="f32", rng="pcg", seed=1,
@@ -380,14 +388,13 @@ class DomeProbe:
         raw = np.zeros((9, nb), np.float64)
         esc = np.zeros(n_rays, np.uint8)
         tp = np.zeros((n_rays, nb), np.float32)
-        st = np.zeros(4, np.uint64)
+        st = np.zeros(2 + 7, np.uint64)
         rc = lib().orc_dome_sample(self.h, _p(_f3(eye)), C.cast(arr, C.c_void_p) if arr is not None else None,
                                    n, n_rays, max_events, nb, ema, _p(out_dir), _p(out_e), _p(raw), _p(esc),
                                    _p(tp), _p(st))
         assert rc == 0, rc
         return dict(dir=out_dir, energy=out_e, raw=raw, escape=esc, ray_tp=tp,
-                    stats=dict(escape_events=int(st[0]), through_calls=int(st[1]), node_reads=int(st[2]),
-                               prim_tests=int(st[3])))
+                    stats=dict(escape_events=int(st[0]), through_calls=int(st[1]), **_trav(st[2:])))
 
 
 def dome_fan(n: int, real: str = "f32") -> np.ndarray:

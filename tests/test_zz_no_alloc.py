@@ -6,8 +6,11 @@ allocator): its scratch lives in a fixed device array. Here it is called
 through the C ABI twice in a row, on device buffers this test owns, and each
 result must match the allocating entry point's on the same job within the
 tolerance the parity tests use (per-bin relative error <= 1e-5 on bins holding
->= 1e-6 of the band total). The second call checks that the shared scratch is
-cleared between calls. This file is collected last on purpose.
+>= 1e-6 of the band total), and its flag word must read 0 (the trace ran to its
+end). The second call checks that the shared scratch is cleared between calls.
+Jobs beyond the fixed scratch, and jobs with non-finite geometry or materials,
+are rejected before anything is launched. This file is collected last on
+purpose.
 """
 import ctypes as C
 
@@ -39,6 +42,7 @@ def test_noalloc_matches_the_allocating_entry_point_twice(built_lib):
     assert n_bins * (nb + 3) <= _lib.NOALLOC_MAX_CELLS
     bins_dev = torch.empty(n_bins * nb, dtype=torch.float32, device="cuda")
     dirs_dev = torch.empty(n_bins * 3, dtype=torch.float32, device="cuda")
+    flags_dev = torch.empty(1, dtype=torch.int32, device="cuda")
     stream = torch.cuda.current_stream()
     with Context(cfg) as ctx:
         for seed in (11, 12):
@@ -54,10 +58,13 @@ def test_noalloc_matches_the_allocating_entry_point_twice(built_lib):
             job.seed = seed
             bins_dev.fill_(float("nan"))
             dirs_dev.fill_(float("nan"))
+            flags_dev.fill_(-1)
             rc = built_lib.omg_trace_box_noalloc(C.byref(job), C.byref(prm), C.c_void_p(bins_dev.data_ptr()),
-                                                 C.c_void_p(dirs_dev.data_ptr()), C.c_void_p(stream.cuda_stream))
+                                                 C.c_void_p(dirs_dev.data_ptr()), C.c_void_p(flags_dev.data_ptr()),
+                                                 C.c_void_p(stream.cuda_stream))
             assert rc == 0, rc
             torch.cuda.synchronize()
+            assert int(flags_dev.item()) == 0
             got_b = bins_dev.cpu().numpy().reshape(n_bins, nb)
             got_d = dirs_dev.cpu().numpy().reshape(n_bins, 3)
             assert np.isfinite(got_b).all() and np.isfinite(got_d).all()
@@ -65,16 +72,40 @@ def test_noalloc_matches_the_allocating_entry_point_twice(built_lib):
             assert np.allclose(got_d, ref.dirs, rtol=1e-4, atol=1e-9), seed
 
 
-def test_noalloc_rejects_sizes_beyond_its_scratch(built_lib):
-    from omg_audio_gb300 import TraceConfig, _lib
-    from omg_audio_gb300 import materials as M
-    cfg = TraceConfig(n_bins=6000, bin_dt=0.001, n_bands=8)
-    prm = cfg.to_c()
+def _job(M, _lib):
     job = _lib.omg_box_job()
     for k in range(3):
         job.size[k], job.src[k], job.lis[k] = 5.0, 1.0, 2.0
     for w in range(6):
         job.walls[w] = M.CONCRETE.to_c()
     job.n_rays = 64
-    rc = built_lib.omg_trace_box_noalloc(C.byref(job), C.byref(prm), C.c_void_p(1), C.c_void_p(1), None)
+    return job
+
+
+def test_noalloc_rejects_sizes_beyond_its_scratch(built_lib):
+    from omg_audio_gb300 import TraceConfig, _lib
+    from omg_audio_gb300 import materials as M
+    prm = TraceConfig(n_bins=6000, bin_dt=0.001, n_bands=8).to_c()
+    rc = built_lib.omg_trace_box_noalloc(C.byref(_job(M, _lib)), C.byref(prm), C.c_void_p(1), C.c_void_p(1), None,
+                                         None)
+    assert rc == _lib.E_INVALID
+
+
+@pytest.mark.parametrize("bad", ["src", "size", "absorption", "scattering"])
+def test_noalloc_rejects_non_finite_jobs(built_lib, bad):
+    """The checks omg_trace_box makes: NaN positions, sizes or material values
+    never reach the kernel (the buffer pointers are never used)."""
+    from omg_audio_gb300 import TraceConfig, _lib
+    from omg_audio_gb300 import materials as M
+    prm = TraceConfig().to_c()
+    job = _job(M, _lib)
+    if bad == "src":
+        job.src[1] = float("nan")
+    elif bad == "size":
+        job.size[2] = float("inf")
+    elif bad == "absorption":
+        job.walls[3].absorption[0] = float("nan")
+    else:
+        job.walls[0].scattering = float("nan")
+    rc = built_lib.omg_trace_box_noalloc(C.byref(job), C.byref(prm), C.c_void_p(1), C.c_void_p(1), None, None)
     assert rc == _lib.E_INVALID
