@@ -244,29 +244,69 @@ def run_reference(args):
     return 0
 
 
+FWD_FLOP = 2 * (38 * 256 + 3 * 256 * 256 + 256 * 192)   # one sample through the 38-256x4-192 MLP
+
+
+def gemm_leg(ctx):
+    """CUDA-event time of the tensor-core GEMM at the training shapes (rows x
+    out x in), operands resident: TFLOP/s and the fraction of the measured bf16
+    peak."""
+    import ctypes as C
+
+    from omg_audio_gb300 import _lib
+    peak = None
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            peak = float(json.load(fh)["bf16_tflops"])
+    out = {}
+    for name, (m, n, k, split) in {"forward hidden layer 4096x256x256": (4096, 256, 256, 1),
+                                   "forward output layer 4096x192x256": (4096, 192, 256, 1),
+                                   "weight gradient 256x256 over 4096 rows (K split 8)": (256, 256, 4096, 8),
+                                   "input gradient 4096x256x192": (4096, 256, 192, 1)}.items():
+        ms = C.c_float()
+        ctx._check(_lib.lib().omg_tc_gemm_bench(ctx.h, m, n, k, split, 200, C.byref(ms)), "omg_tc_gemm_bench")
+        tf = 2.0 * m * n * k / (ms.value * 1e-3) / 1e12
+        out[name] = {"us": 1e3 * ms.value, "tflops": tf, "frac_of_bf16_peak": tf / peak if peak else None}
+    return out
+
+
 def surrogate_leg(args, device):
     """The learned surrogate against the GPU tracer on the config-1 room family
     (shoebox, 6 x 3 absorptions, up to 4 apertures, poses): training data from
-    the tracer (1024 rays per room), the tensor-core MLP ensemble trained on the
-    GPU, then held-out rooms answered by both. Reported: RT60 error of the
-    surrogate's EDC against the tracer's (4096 rays), the Sabine formula's error
-    (the method without the network), and ms per room of each, end to end
-    through the C ABI with host buffers."""
+    the tracer (args.surrogate_train_rays per room), the tensor-core MLP
+    ensemble trained on the GPU, then held-out rooms answered by both.
+    Reported:
+    - the training speed (TFLOP/s of the training steps, 3 x the forward
+      FLOPs per sample) and the GEMMs alone at the training shapes;
+    - the RT60 error of the surrogate's EDC against the tracer's (4096 rays),
+      the Sabine formula's (the method without the network), and the noise
+      floor of that judge: the tracer at 4096 rays against itself at another
+      seed, and against 65,536 rays, on a subset of the test rooms;
+    - the ensemble-spread gate swept: RT60 error of the ANSWERED rooms against
+      the fraction answered, and the per-room time with the tracer's time for
+      the rooms it falls back on;
+    - ms per room of each, end to end through the C ABI with host buffers."""
     from omg_audio_gb300 import Context, TraceConfig
     from omg_audio_gb300 import surrogate as S
     ctx = Context(TraceConfig(device=device, n_bands=3, n_bins=2000, bin_dt=0.001, max_time=2.0, max_bounces=200,
                               energy_floor=1e-6, timeout_ms=120000))
+    train_rays = args.surrogate_train_rays
     t0 = time.perf_counter()
     train = S.sample_rooms(args.surrogate_rooms, seed=1)
-    bins, _ = S.trace_rooms(ctx, train, 1024, seed=100)
+    bins, _ = S.trace_rooms(ctx, train, train_rays, seed=100)
     edc = S.edc_db(bins, 0.001)
     del bins
     t_data = time.perf_counter() - t0
-    sur = S.RoomSurrogate(ctx, members=4)
+    members = 4
+    sur = S.RoomSurrogate(ctx, members=members)
+    batch = 4096
     t0 = time.perf_counter()
-    losses = sur.fit(train, edc, epochs=args.surrogate_epochs, batch=4096, lr=2e-3, lr_final=2e-5,
+    losses = sur.fit(train, edc, epochs=args.surrogate_epochs, batch=batch, lr=2e-3, lr_final=2e-5,
                      weight_decay=1e-4)
     t_train = time.perf_counter() - t0
+    steps = (len(train) // batch) * args.surrogate_epochs
+    train_tflops = 3.0 * FWD_FLOP * batch * steps * members / t_train / 1e12
     test = S.sample_rooms(args.surrogate_test, seed=99)
     S.trace_rooms(ctx, test.take(np.arange(64)), 4096, seed=7)      # warm-up
     sur.predict(test.take(np.arange(64)))
@@ -274,34 +314,74 @@ def surrogate_leg(args, device):
     bins_t, _ = S.trace_rooms(ctx, test, 4096, seed=7)
     t_trace = time.perf_counter() - t0
     t0 = time.perf_counter()
-    pred, std, ok = sur.predict(test)
+    pred, spread, ok = sur.predict(test)
     t_pred = time.perf_counter() - t0
     t0 = time.perf_counter()
     S.features(test)
     t_feat = time.perf_counter() - t0
     edc_t = S.edc_db(bins_t, 0.001)
     rt_t = S.rt60_from_edc(edc_t)
-    err = np.abs(S.rt60_from_edc(pred) / rt_t - 1.0)
+    rt_p = S.rt60_from_edc(pred)
+    err = np.abs(rt_p / rt_t - 1.0)
     sab = np.abs(S.features(test)[:, S.SABINE_COLS] / rt_t - 1.0)
     n = len(test)
+    # the judge's noise floor, on the first n_floor test rooms
+    n_floor = min(n, args.surrogate_floor_rooms)
+    sub = test.take(np.arange(n_floor))
+    rt_b = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, sub, 4096, seed=8)[0], 0.001))
+    rt_c = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, sub, 65536, seed=9)[0], 0.001))
+    nz_seed = np.abs(rt_b / rt_t[:n_floor] - 1.0)
+    nz_65k = np.abs(rt_t[:n_floor] / rt_c - 1.0)
+    sur_65k = np.abs(rt_p[:n_floor] / rt_c - 1.0)
+
+    def q(a, p):
+        return float(np.nanpercentile(a, p))
+
+    # the spread gate swept: answered = in the family and spread <= threshold
+    inr = S.in_range(S.features(test))
+    tr_ms = 1e3 * t_trace / n
+    su_ms = 1e3 * t_pred / n
+    sweep = []
+    for thr in [0.5, 0.75, 1.0, 1.25, 1.5, 2.0, 2.5, 3.0, 4.0, 6.0, 1e9]:
+        ans = inr & (spread <= thr)
+        fa = float(np.mean(ans))
+        e_ans = err[ans] if ans.any() else np.full((1, 3), np.nan)
+        per_room = su_ms + (1.0 - fa) * tr_ms
+        sweep.append({"spread_db_max": thr if thr < 1e8 else None, "answered_frac": fa,
+                      "rt60_err_median": q(e_ans, 50), "rt60_err_p90": q(e_ans, 90),
+                      "ms_per_room_with_fallback": per_room, "speedup_with_fallback": tr_ms / per_room})
+    ok5 = [r for r in sweep if r["rt60_err_p90"] <= 0.05]
+    chosen = max(ok5, key=lambda r: r["answered_frac"]) if ok5 else None
+    gemm = gemm_leg(ctx)
     ctx.close()
     return {
         "family": "shoebox 4-16 x 4-12 x 2.5-6 m, absorption U[0.02,0.4] x 6 surfaces x 3 bands, scattering 0.1, "
                   "0-4 apertures 1.5 x 2 m with openness U[0,1], poses >= 1 m from walls",
         "network": "38 -> 256 x4 (GELU) -> 192 (64 log-time EDC points x 3 bands), 4-member ensemble, BF16 "
                    "tcgen05 GEMMs, FP32 accumulate and master weights, AdamW",
-        "train_rooms": len(train), "train_rays": 1024, "epochs": args.surrogate_epochs,
+        "train_rooms": len(train), "train_rays": train_rays, "epochs": args.surrogate_epochs,
         "data_s": t_data, "train_s": t_train, "final_loss": float(np.mean(losses[:, -1])),
+        "train_tflops": train_tflops,
+        "train_flops_note": "3 x 510,976 FLOP per sample per member (forward, input and weight gradients)",
+        "gemm": gemm,
         "test_rooms": n, "judge_rays": 4096,
-        "rt60_err_median": float(np.nanmedian(err)), "rt60_err_p90": float(np.nanpercentile(err, 90)),
+        "rt60_err_median": float(np.nanmedian(err)), "rt60_err_p90": q(err, 90),
         "frac_rooms_all_bands_within_5pct": float(np.mean(np.nan_to_num(err, nan=1.0).max(1) <= 0.05)),
         "sabine_rt60_err_median": float(np.nanmedian(sab)),
         "edc_rmse_db": float(np.sqrt(np.mean((pred - edc_t) ** 2))),
-        "usable_frac": float(np.mean(ok)),
-        "tracer_ms_per_room": 1e3 * t_trace / n, "surrogate_ms_per_room": 1e3 * t_pred / n,
+        "judge_noise_floor": {
+            "rooms": n_floor,
+            "tracer_4096_vs_4096_other_seed": {"median": q(nz_seed, 50), "p90": q(nz_seed, 90)},
+            "tracer_4096_vs_65536": {"median": q(nz_65k, 50), "p90": q(nz_65k, 90)},
+            "surrogate_vs_65536": {"median": q(sur_65k, 50), "p90": q(sur_65k, 90)}},
+        "spread_gate_sweep": sweep,
+        "chosen_gate": chosen,
+        "p90_target_met": chosen is not None,
+        "tracer_ms_per_room": tr_ms, "surrogate_ms_per_room": su_ms,
         "speedup": t_trace / t_pred, "surrogate_features_ms_per_room": 1e3 * t_feat / n,
         "timing": "wall clock of the calls with host buffers: trace_rooms (batched jobs, echograms down) vs "
-                  "RoomSurrogate.predict (input features, omg_surrogate_query, decay curves down)",
+                  "RoomSurrogate.predict (input features, omg_surrogate_query, decay curves down); with "
+                  "fallback: the surrogate's time per room plus the tracer's for the share it falls back on",
     }
 
 
@@ -702,6 +782,9 @@ def main():
     ap.add_argument("--surrogate-rooms", type=int, default=131072, help="training rooms (1 M: the full config)")
     ap.add_argument("--surrogate-epochs", type=int, default=60)
     ap.add_argument("--surrogate-test", type=int, default=16384, help="held-out rooms")
+    ap.add_argument("--surrogate-train-rays", type=int, default=1024, help="tracer rays per training room")
+    ap.add_argument("--surrogate-floor-rooms", type=int, default=2048,
+                    help="test rooms traced again (another seed; 65,536 rays) for the judge's noise floor")
     ap.add_argument("--max-bounces", type=int, default=0,
                     help="profiling variant: cap the bounces (0: the workload's 200)")
     ap.add_argument("--shape", default="",

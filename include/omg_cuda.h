@@ -574,6 +574,11 @@ int32_t omg_mlp_set_params(omg_ctx* ctx, uint32_t mlp_id, uint32_t what, const f
  * bf16 bit patterns, row-major with k contiguous; C f32. */
 int32_t omg_tc_gemm(omg_ctx* ctx, const uint16_t* a, const uint16_t* b, float* c, uint32_t m, uint32_t n,
                     uint32_t k);
+/* Device time of that GEMM at one shape (operands resident, K-major, k a
+ * multiple of 8; k_split > 1 splits K over the grid with atomic adds): the
+ * mean ms per launch over `reps` launches timed with CUDA events. */
+int32_t omg_tc_gemm_bench(omg_ctx* ctx, uint32_t m, uint32_t n, uint32_t k, uint32_t k_split, uint32_t reps,
+                          float* ms);
 
 /* ---------------------------------------------------------------- no-alloc */
 /* No counterpart in the reference: an addition of this library.

@@ -184,6 +184,7 @@ SIGNATURES = {
     "omg_mlp_params": (I32, [P, U32, U32, P, PU64]),
     "omg_mlp_set_params": (I32, [P, U32, U32, P, U64]),
     "omg_tc_gemm": (I32, [P, P, P, P, U32, U32, U32]),
+    "omg_tc_gemm_bench": (I32, [P, U32, U32, U32, U32, U32, C.POINTER(C.c_float)]),
     "omg_trace_box_noalloc": (I32, [C.POINTER(omg_box_job), C.POINTER(omg_params), P, P, P, P]),
     "omg_early_create": (I32, [P, U32, P, U32, PU32]),
     "omg_early_destroy": (I32, [P, U32]),

@@ -18,7 +18,37 @@ namespace omg {
 struct MlpLayer {
   uint32_t in = 0, out = 0;
   DevBuf<float> W, b, mW, vW, mb, vb, gW, gb;
-  DevBuf<uint16_t> Wh;   // bf16 copy of W
+  DevBuf<uint16_t> Wh;    // bf16 copy of W [out x in]
+  DevBuf<uint16_t> Wht;   // its transpose [in x out]: the K-major operand of dX = dZ . W
+};
+
+// The work buffers of one batch of `cap` rows. Besides the row-major
+// activations and gradients, the backward pass keeps their bf16 transposes
+// (xht, At, dZht: [features x rows]), so that every GEMM of training reads
+// both operands K-major (the pipelined path of mlp.cu).
+struct MlpBufs {
+  uint32_t cap = 0;
+  DevBuf<uint16_t> xh, xht;               // batch input (bf16) and its transpose
+  DevBuf<float> t;                        // batch targets
+  std::vector<DevBuf<float>> Z;           // pre-activations per layer
+  std::vector<DevBuf<uint16_t>> A, At;    // bf16 activations per hidden layer, and transposes
+  DevBuf<float> out, dX, dZ, loss;
+  DevBuf<uint16_t> dZh, dZht;
+};
+
+// One ensemble member's training lane: its buffers, stream, step graph,
+// epoch permutation and device step counter.
+struct MlpTrainer {
+  MlpBufs bufs;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  DevBuf<uint32_t> perm, step;
+  PinBuf<uint32_t> h_perm;
+  PinBuf<float> h_loss;
+  ~MlpTrainer() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (stream) cudaStreamDestroy(stream);
+  }
 };
 
 struct MlpRec {
@@ -34,16 +64,10 @@ struct MlpRec {
   // dataset (standardized, device)
   uint32_t n_data = 0;
   DevBuf<float> X, Y;
-  DevBuf<uint32_t> perm;
   uint64_t step = 0;
-  // work buffers for a batch of `cap` rows
-  uint32_t cap = 0;
-  DevBuf<uint16_t> xh;                    // batch input (bf16)
-  DevBuf<float> t;                        // batch targets
-  std::vector<DevBuf<float>> Z;           // pre-activations per layer
-  std::vector<DevBuf<uint16_t>> A;        // bf16 activations per hidden layer
-  DevBuf<float> out, dY, dX, dZ, loss_parts;
-  DevBuf<uint16_t> dZh;
+  MlpBufs io;                                   // inference and omg_mlp_grad, on the context's stream
+  std::vector<std::unique_ptr<MlpTrainer>> trainers;   // training, one per member
+  DevBuf<float> sched;                          // per step: learning rate, bias corrections 1 and 2
   DevBuf<uint32_t> err;
   PinBuf<float> h_loss;
 };
@@ -52,37 +76,46 @@ struct MlpRec {
 
 namespace {
 
-constexpr uint32_t kLossParts = 64;
-
 uint32_t n_layers(const MlpRec& M) { return M.cfg.n_hidden + 1; }
 
-int32_t ensure_batch(omg_ctx* ctx, MlpRec& M, uint32_t rows) {
-  if (rows <= M.cap) return OMG_OK;
+int32_t ensure_batch(omg_ctx* ctx, const MlpRec& M, MlpBufs& W, uint32_t rows, bool backward) {
+  if (rows <= W.cap) return OMG_OK;
   const uint32_t L = n_layers(M), H = M.cfg.hidden;
-  CK(M.xh.alloc((size_t)rows * M.cfg.n_in));
-  CK(M.t.alloc((size_t)rows * M.cfg.n_out));
-  M.Z.resize(L);
-  M.A.resize(L);
+  CK(W.xh.alloc((size_t)rows * M.cfg.n_in));
+  CK(W.t.alloc((size_t)rows * M.cfg.n_out));
+  W.Z.resize(L);
+  W.A.resize(L);
+  W.At.resize(L);
   for (uint32_t l = 0; l < L; l++) {
     const uint32_t o = l + 1 == L ? M.cfg.n_out : H;
-    CK(M.Z[l].alloc((size_t)rows * o));
-    CK(M.A[l].alloc((size_t)rows * o));
+    CK(W.Z[l].alloc((size_t)rows * o));
+    CK(W.A[l].alloc((size_t)rows * o));
+    if (backward) CK(W.At[l].alloc((size_t)rows * o));
   }
   const uint32_t wide = std::max(std::max(H, M.cfg.n_out), M.cfg.n_in);
-  CK(M.out.alloc((size_t)rows * M.cfg.n_out));
-  CK(M.dY.alloc((size_t)rows * wide));
-  CK(M.dX.alloc((size_t)rows * wide));
-  CK(M.dZ.alloc((size_t)rows * wide));
-  CK(M.dZh.alloc((size_t)rows * wide));
-  M.cap = rows;
+  CK(W.out.alloc((size_t)rows * M.cfg.n_out));
+  CK(W.dX.alloc((size_t)rows * wide));
+  CK(W.dZ.alloc((size_t)rows * wide));
+  CK(W.dZh.alloc((size_t)rows * wide));
+  if (backward) {
+    CK(W.xht.alloc((size_t)rows * M.cfg.n_in));
+    CK(W.dZht.alloc((size_t)rows * wide));
+  }
+  CK(W.loss.alloc(1));
+  W.cap = rows;
   return OMG_OK;
 }
 
-// X0 (bf16, rows x n_in) -> out (f32, rows x n_out); keeps Z and A for backward
-int32_t forward(omg_ctx* ctx, MlpRec& M, uint32_t e, uint32_t rows, cudaStream_t s) {
+// columns per CTA of a GEMM with n output columns: 128 when that still leaves
+// whole 16-column MMAs, else all of them (<= 256)
+uint32_t n_tile_of(uint32_t n) { return n > 128 ? 128u : ((n + 15) & ~15u); }
+
+// X0 (bf16, rows x n_in) -> out (f32, rows x n_out); keeps Z and A (and, for
+// training, the transposed activations At) for backward
+int32_t forward(omg_ctx* ctx, MlpRec& M, MlpBufs& W, uint32_t e, uint32_t rows, bool keep_t, cudaStream_t s) {
   const uint32_t L = n_layers(M);
   auto& net = M.members[e];
-  const uint16_t* x = M.xh.p;
+  const uint16_t* x = W.xh.p;
   uint32_t in = M.cfg.n_in;
   for (uint32_t l = 0; l < L; l++) {
     MlpLayer& Ly = net[l];
@@ -97,72 +130,82 @@ int32_t forward(omg_ctx* ctx, MlpRec& M, uint32_t e, uint32_t rows, cudaStream_t
     g.M = rows;
     g.N = Ly.out;
     g.K = in;
-    g.n_tile = Ly.out <= 256 ? ((Ly.out + 15) & ~15u) : 256;
+    g.n_tile = n_tile_of(Ly.out);
     g.bias = Ly.b.p;
     g.err = M.err.p;
     if (last) {
-      g.D = M.out.p;
+      g.D = W.out.p;
       g.ldd = Ly.out;
     } else {
-      g.Z = M.Z[l].p;
+      g.Z = W.Z[l].p;
       g.ldz = Ly.out;
-      g.Y = M.A[l].p;
+      g.Y = W.A[l].p;
       g.ldy = Ly.out;
+      if (keep_t) {
+        g.Yt = W.At[l].p;
+        g.ldyt = rows;
+      }
       g.act = 1;
     }
     CK(launch_gemm(g, 1, s));
-    x = M.A[l].p;
+    x = W.A[l].p;
     in = Ly.out;
   }
   return OMG_OK;
 }
 
-// gradients of the MSE (targets in M.t) into the layers' gW, gb; loss parts
-int32_t backward(omg_ctx* ctx, MlpRec& M, uint32_t e, uint32_t rows, cudaStream_t s) {
+// gradients of the MSE (targets in W.t) into the layers' gW, gb; the loss into
+// W.loss (both zeroed here first). Every GEMM reads K-major operands: dW =
+// dZ^T X from the transposes dZht and xht / At, dX = dZ W from dZh and Wht.
+int32_t backward(omg_ctx* ctx, MlpRec& M, MlpBufs& W, uint32_t e, uint32_t rows, cudaStream_t s) {
   const uint32_t L = n_layers(M);
   auto& net = M.members[e];
-  CK(launch_mse(M.out.p, M.t.p, nullptr, rows, M.cfg.n_out, M.dZ.p, M.dZh.p, M.loss_parts.p, kLossParts, s));
+  CK(cudaMemsetAsync(W.loss.p, 0, 4, s));
+  for (auto& Ly : net) CK(cudaMemsetAsync(Ly.gb.p, 0, (size_t)Ly.out * 4, s));
+  MlpLayer& top = net[L - 1];
+  CK(launch_grad_tile(0, W.out.p, W.t.p, nullptr, rows, M.cfg.n_out, W.dZ.p, W.dZh.p, W.dZht.p, top.gb.p,
+                      W.loss.p, s));
   for (int l = (int)L - 1; l >= 0; l--) {
     MlpLayer& Ly = net[l];
-    const uint16_t* xin = l == 0 ? M.xh.p : M.A[l - 1].p;
+    const uint16_t* xt = l == 0 ? W.xht.p : W.At[l - 1].p;
     // dW = dZ^T . X  (reduction over the batch, split over grid z)
     CK(cudaMemsetAsync(Ly.gW.p, 0, (size_t)Ly.out * Ly.in * 4, s));
     GemmArgs g{};
-    g.A = M.dZh.p;
-    g.a_rs = 1;
-    g.a_ks = Ly.out;
-    g.B = xin;
-    g.b_rs = 1;
-    g.b_ks = Ly.in;
+    g.A = W.dZht.p;
+    g.a_rs = rows;
+    g.a_ks = 1;
+    g.B = xt;
+    g.b_rs = rows;
+    g.b_ks = 1;
     g.M = Ly.out;
     g.N = Ly.in;
     g.K = rows;
-    g.n_tile = Ly.in <= 256 ? ((Ly.in + 15) & ~15u) : 256;
+    g.n_tile = n_tile_of(Ly.in);
     g.D = Ly.gW.p;
     g.ldd = Ly.in;
     g.accumulate = 1;
     g.err = M.err.p;
-    const uint32_t split = std::max(1u, std::min(32u, rows / 256u));
+    const uint32_t split = std::max(1u, std::min(8u, rows / 512u));
     CK(launch_gemm(g, split, s));
-    CK(launch_colsum(M.dZ.p, rows, Ly.out, Ly.gb.p, s));
     if (l == 0) break;
-    // dX = dZ . W, then dZ of the layer below through GELU'
+    // dX = dZ . W, then dZ of the layer below through GELU' (and its bias gradient)
     GemmArgs h{};
-    h.A = M.dZh.p;
+    h.A = W.dZh.p;
     h.a_rs = Ly.out;
     h.a_ks = 1;
-    h.B = Ly.Wh.p;
-    h.b_rs = 1;
-    h.b_ks = Ly.in;
+    h.B = Ly.Wht.p;
+    h.b_rs = Ly.out;
+    h.b_ks = 1;
     h.M = rows;
     h.N = Ly.in;
     h.K = Ly.out;
-    h.n_tile = Ly.in <= 256 ? ((Ly.in + 15) & ~15u) : 256;
-    h.D = M.dX.p;
+    h.n_tile = n_tile_of(Ly.in);
+    h.D = W.dX.p;
     h.ldd = Ly.in;
     h.err = M.err.p;
     CK(launch_gemm(h, 1, s));
-    CK(launch_gelu_back(M.dX.p, M.Z[l - 1].p, M.dZ.p, M.dZh.p, (uint64_t)rows * Ly.in, s));
+    CK(launch_grad_tile(1, W.dX.p, W.Z[l - 1].p, nullptr, rows, Ly.in, W.dZ.p, W.dZh.p, W.dZht.p,
+                        net[l - 1].gb.p, nullptr, s));
   }
   return OMG_OK;
 }
@@ -205,6 +248,8 @@ extern "C" {
 
 int32_t omg_mlp_create(omg_ctx* ctx, const omg_mlp_config* cfg, uint32_t* id) {
   if (!ctx || !cfg || !id || !valid_cfg(*cfg)) return OMG_E_INVALID;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, cudaGetLastError(), "cudaSetDevice");
+  CK(gemm_init());
   std::shared_ptr<MlpRec> M(new MlpRec());
   M->cfg = *cfg;
   const uint32_t L = cfg->n_hidden + 1;
@@ -226,6 +271,7 @@ int32_t omg_mlp_create(omg_ctx* ctx, const omg_mlp_config* cfg, uint32_t* id) {
         for (auto& v : w) v *= 0.5f;
       CK(Ly.W.alloc(nw));
       CK(Ly.Wh.alloc(nw));
+      CK(Ly.Wht.alloc(nw));
       CK(Ly.mW.alloc(nw));
       CK(Ly.vW.alloc(nw));
       CK(Ly.gW.alloc(nw));
@@ -239,7 +285,7 @@ int32_t omg_mlp_create(omg_ctx* ctx, const omg_mlp_config* cfg, uint32_t* id) {
       CK(cudaMemset(Ly.b.p, 0, Ly.out * 4));
       CK(cudaMemset(Ly.mb.p, 0, Ly.out * 4));
       CK(cudaMemset(Ly.vb.p, 0, Ly.out * 4));
-      CK(launch_to_bf16(Ly.W.p, Ly.Wh.p, nw, ctx->stream));
+      CK(launch_to_bf16_t(Ly.W.p, Ly.out, Ly.in, Ly.Wh.p, Ly.Wht.p, ctx->stream));
       in = Ly.out;
     }
   }
@@ -247,8 +293,7 @@ int32_t omg_mlp_create(omg_ctx* ctx, const omg_mlp_config* cfg, uint32_t* id) {
   M->x_std.assign(cfg->n_in, 1.0f);
   M->y_mean.assign(cfg->n_out, 0.0f);
   M->y_std.assign(cfg->n_out, 1.0f);
-  CK(M->loss_parts.alloc(kLossParts));
-  CK(M->h_loss.alloc(kLossParts));
+  CK(M->h_loss.alloc(1));
   CK(M->err.alloc(1));
   CK(cudaMemsetAsync(M->err.p, 0, 4, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -303,59 +348,109 @@ int32_t omg_mlp_set_data(omg_ctx* ctx, uint32_t id, const float* x, const float*
   if (rc) return rc;
   CK(M.X.alloc(xs.size()));
   CK(M.Y.alloc(ys.size()));
-  CK(M.perm.alloc(n));
   CK(cudaMemcpy(M.X.p, xs.data(), xs.size() * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(M.Y.p, ys.data(), ys.size() * 4, cudaMemcpyHostToDevice));
   M.n_data = n;
   return OMG_OK;
 }
 
+// Training. Every member trains on its own stream, concurrently: one step
+// (gather the batch, forward, backward, AdamW of every layer, step counter) is
+// recorded once into a CUDA graph per member and launched steps-per-epoch
+// times per epoch; the step's batch rows (this epoch's permutation, uploaded
+// before the epoch) and its learning rate and bias corrections (a schedule
+// uploaded once) are read on the device at the step counter. The host waits
+// once per epoch, for the losses.
 int32_t omg_mlp_train(omg_ctx* ctx, uint32_t id, const omg_mlp_train_config* tc, float* epoch_loss) {
   if (!ctx || !tc || tc->epochs == 0 || tc->batch == 0 || tc->batch % 128 != 0) return OMG_E_INVALID;
   auto it = ctx->mlps.find(id);
   if (it == ctx->mlps.end()) return OMG_E_NOT_FOUND;
   MlpRec& M = *it->second;
   if (M.n_data < tc->batch) return OMG_E_INVALID;
-  int32_t rc = ensure_batch(ctx, M, tc->batch);
-  if (rc) return rc;
-  cudaStream_t s = ctx->stream;
-  const uint32_t L = n_layers(M), B = tc->batch;
-  const uint32_t steps_per_epoch = M.n_data / B;
-  const uint64_t total = (uint64_t)steps_per_epoch * tc->epochs;
-  std::mt19937_64 rng(tc->seed ? tc->seed : 7u);
-  std::vector<uint32_t> perm(M.n_data);
-  for (uint32_t e = 0; e < M.cfg.members; e++) {
-    uint64_t t = 0;
-    for (uint32_t ep = 0; ep < tc->epochs; ep++) {
-      std::iota(perm.begin(), perm.end(), 0u);
-      std::shuffle(perm.begin(), perm.end(), rng);
-      CK(cudaMemcpyAsync(M.perm.p, perm.data(), (size_t)M.n_data * 4, cudaMemcpyHostToDevice, s));
-      double ep_loss = 0.0;
-      for (uint32_t st = 0; st < steps_per_epoch; st++, t++) {
-        CK(launch_gather_rows(M.X.p, M.cfg.n_in, M.perm.p + (size_t)st * B, B, nullptr, M.xh.p, s));
-        CK(launch_gather_rows(M.Y.p, M.cfg.n_out, M.perm.p + (size_t)st * B, B, M.t.p, nullptr, s));
-        if ((rc = forward(ctx, M, e, B, s))) return rc;
-        if ((rc = backward(ctx, M, e, B, s))) return rc;
-        // cosine decay from lr to lr_final
-        const double prog = total > 1 ? (double)t / (double)(total - 1) : 1.0;
-        const float lr = (float)(tc->lr_final + 0.5 * (tc->lr - tc->lr_final) * (1.0 + std::cos(3.14159265358979323846 * prog)));
-        const double step = (double)(t + 1);
-        const float bc1 = (float)(1.0 - std::pow((double)tc->beta1, step));
-        const float bc2 = (float)(1.0 - std::pow((double)tc->beta2, step));
-        for (uint32_t l = 0; l < L; l++) {
-          MlpLayer& Ly = M.members[e][l];
-          CK(launch_adamw(Ly.W.p, Ly.mW.p, Ly.vW.p, Ly.gW.p, Ly.Wh.p, (uint64_t)Ly.out * Ly.in, lr, tc->beta1,
-                          tc->beta2, tc->eps, tc->weight_decay, bc1, bc2, s));
-          CK(launch_adamw(Ly.b.p, Ly.mb.p, Ly.vb.p, Ly.gb.p, nullptr, Ly.out, lr, tc->beta1, tc->beta2, tc->eps,
-                          0.0f, bc1, bc2, s));
-        }
-        if (epoch_loss && (st + 1 == steps_per_epoch)) {
-          CK(cudaMemcpyAsync(M.h_loss.p, M.loss_parts.p, kLossParts * 4, cudaMemcpyDeviceToHost, s));
-          CK(cudaStreamSynchronize(s));
-          for (uint32_t k = 0; k < kLossParts; k++) ep_loss += M.h_loss.p[k];
-        }
+  const uint32_t L = n_layers(M), B = tc->batch, E = M.cfg.members;
+  const uint32_t spe = M.n_data / B;
+  const uint64_t total = (uint64_t)spe * tc->epochs;
+  if (total >= (1ull << 31)) return OMG_E_INVALID;
+  // the schedule: cosine decay from lr to lr_final, AdamW bias corrections
+  std::vector<float> sched(3 * total);
+  for (uint64_t t = 0; t < total; t++) {
+    const double prog = total > 1 ? (double)t / (double)(total - 1) : 1.0;
+    sched[3 * t] = (float)(tc->lr_final + 0.5 * (tc->lr - tc->lr_final) * (1.0 + std::cos(3.14159265358979323846 * prog)));
+    sched[3 * t + 1] = (float)(1.0 - std::pow((double)tc->beta1, (double)(t + 1)));
+    sched[3 * t + 2] = (float)(1.0 - std::pow((double)tc->beta2, (double)(t + 1)));
+  }
+  CK(gemm_init());   // outside the captures below
+  CK(M.sched.alloc(sched.size()));
+  CK(cudaMemcpy(M.sched.p, sched.data(), sched.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaStreamSynchronize(ctx->stream));
+  M.trainers.resize(E);
+  int32_t rc = OMG_OK;
+  for (uint32_t e = 0; e < E; e++) {
+    if (!M.trainers[e]) M.trainers[e].reset(new MlpTrainer());
+    MlpTrainer& T = *M.trainers[e];
+    if (!T.stream) CK(cudaStreamCreateWithFlags(&T.stream, cudaStreamNonBlocking));
+    if ((rc = ensure_batch(ctx, M, T.bufs, B, true))) return rc;
+    CK(T.perm.alloc(M.n_data));
+    CK(T.h_perm.alloc(M.n_data));
+    CK(T.step.alloc(1));
+    CK(T.h_loss.alloc(1));
+    CK(cudaMemsetAsync(T.step.p, 0, 4, T.stream));
+    // record one training step
+    if (T.graph) {
+      cudaGraphExecDestroy(T.graph);
+      T.graph = nullptr;
+    }
+    cudaStream_t s = T.stream;
+    MlpBufs& W = T.bufs;
+    CK(cudaStreamSynchronize(s));
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    auto record = [&]() -> int32_t {
+      CK(launch_gather_step(M.X.p, M.cfg.n_in, T.perm.p, T.step.p, spe, B, nullptr, W.xh.p, W.xht.p, s));
+      CK(launch_gather_step(M.Y.p, M.cfg.n_out, T.perm.p, T.step.p, spe, B, W.t.p, nullptr, nullptr, s));
+      int32_t r;
+      if ((r = forward(ctx, M, W, e, B, true, s))) return r;
+      if ((r = backward(ctx, M, W, e, B, s))) return r;
+      for (uint32_t l = 0; l < L; l++) {
+        MlpLayer& Ly = M.members[e][l];
+        CK(launch_adamw_layer(Ly.W.p, Ly.mW.p, Ly.vW.p, Ly.gW.p, Ly.Wh.p, Ly.Wht.p, Ly.in, Ly.out, Ly.b.p, Ly.mb.p,
+                              Ly.vb.p, Ly.gb.p, M.sched.p, T.step.p, tc->beta1, tc->beta2, tc->eps,
+                              tc->weight_decay, s));
       }
-      if (epoch_loss) epoch_loss[(size_t)e * tc->epochs + ep] = (float)ep_loss;
+      CK(launch_step(T.step.p, s));
+      return OMG_OK;
+    };
+    rc = record();
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess) return fail(ctx, ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&T.graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return fail(ctx, ce, "cudaGraphInstantiate");
+  }
+  std::vector<std::mt19937_64> rngs;
+  for (uint32_t e = 0; e < E; e++) rngs.emplace_back((tc->seed ? tc->seed : 7u) + 0x9E3779B97F4A7C15ull * e);
+  for (uint32_t ep = 0; ep < tc->epochs; ep++) {
+    for (uint32_t e = 0; e < E; e++) {
+      MlpTrainer& T = *M.trainers[e];
+      std::iota(T.h_perm.p, T.h_perm.p + M.n_data, 0u);
+      std::shuffle(T.h_perm.p, T.h_perm.p + M.n_data, rngs[e]);
+      CK(cudaMemcpyAsync(T.perm.p, T.h_perm.p, (size_t)M.n_data * 4, cudaMemcpyHostToDevice, T.stream));
+    }
+    for (uint32_t st = 0; st < spe; st++)
+      for (uint32_t e = 0; e < E; e++) CK(cudaGraphLaunch(M.trainers[e]->graph, M.trainers[e]->stream));
+    for (uint32_t e = 0; e < E; e++) {
+      MlpTrainer& T = *M.trainers[e];
+      CK(cudaMemcpyAsync(T.h_loss.p, T.bufs.loss.p, 4, cudaMemcpyDeviceToHost, T.stream));
+    }
+    // the permutation buffers are refilled next epoch: wait for this one
+    for (uint32_t e = 0; e < E; e++) {
+      MlpTrainer& T = *M.trainers[e];
+      CK(cudaStreamSynchronize(T.stream));
+      if (epoch_loss) epoch_loss[(size_t)e * tc->epochs + ep] = T.h_loss.p[0];
     }
   }
   M.step += total;
@@ -378,7 +473,7 @@ int32_t surrogate_run(omg_ctx* ctx, uint32_t id, const float* x, uint32_t n, flo
   const uint32_t ni = M.cfg.n_in, no = M.cfg.n_out, E = M.cfg.members;
   const uint32_t chunk = 32768;
   const uint32_t rows_max = std::min(n, chunk);
-  int32_t rc = ensure_batch(ctx, M, rows_max);
+  int32_t rc = ensure_batch(ctx, M, M.io, rows_max, false);
   if (rc) return rc;
   if (M.icap < rows_max) {
     CK(M.xin.alloc((size_t)rows_max * ni));
@@ -397,10 +492,10 @@ int32_t surrogate_run(omg_ctx* ctx, uint32_t id, const float* x, uint32_t n, flo
     const uint64_t nx = (uint64_t)rows * ni, ny = (uint64_t)rows * no;
     std::memcpy(M.h_x.p, x + (uint64_t)r0 * ni, nx * 4);
     CK(cudaMemcpyAsync(M.xin.p, M.h_x.p, nx * 4, cudaMemcpyHostToDevice, s));
-    CK(launch_standardize(M.xin.p, M.d_x_mean.p, M.d_x_std.p, ni, nx, M.xh.p, s));
+    CK(launch_standardize(M.xin.p, M.d_x_mean.p, M.d_x_std.p, ni, nx, M.io.xh.p, s));
     for (uint32_t e = 0; e < E; e++) {
-      if ((rc = forward(ctx, M, e, rows, s))) return rc;
-      CK(launch_ensemble(M.out.p, M.d_y_mean.p, M.d_y_std.p, no, ny, M.acc.p, M.acc2.p, e == 0, e + 1 == E,
+      if ((rc = forward(ctx, M, M.io, e, rows, false, s))) return rc;
+      CK(launch_ensemble(M.io.out.p, M.d_y_mean.p, M.d_y_std.p, no, ny, M.acc.p, M.acc2.p, e == 0, e + 1 == E,
                          1.0f / (float)E, s));
     }
     CK(cudaMemcpyAsync(M.h_mean.p, M.acc.p, ny * 4, cudaMemcpyDeviceToHost, s));
@@ -440,17 +535,20 @@ int32_t omg_mlp_grad(omg_ctx* ctx, uint32_t id, uint32_t member, const float* x,
   if (it == ctx->mlps.end()) return OMG_E_NOT_FOUND;
   MlpRec& M = *it->second;
   if (member >= M.cfg.members) return OMG_E_INVALID;
-  int32_t rc = ensure_batch(ctx, M, n);
+  // the inference buffers may have been sized without the transposes
+  if (M.io.cap && !M.io.xht.p) M.io.cap = 0;
+  int32_t rc = ensure_batch(ctx, M, M.io, n, true);
   if (rc) return rc;
   cudaStream_t s = ctx->stream;
+  MlpBufs& W = M.io;
   DevBuf<float> xd;
   CK(xd.alloc((size_t)n * M.cfg.n_in));
   CK(cudaMemcpyAsync(xd.p, x, (size_t)n * M.cfg.n_in * 4, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(M.t.p, y, (size_t)n * M.cfg.n_out * 4, cudaMemcpyHostToDevice, s));
-  CK(launch_to_bf16(xd.p, M.xh.p, (uint64_t)n * M.cfg.n_in, s));
-  if ((rc = forward(ctx, M, member, n, s))) return rc;
-  if ((rc = backward(ctx, M, member, n, s))) return rc;
-  CK(cudaMemcpyAsync(M.h_loss.p, M.loss_parts.p, kLossParts * 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(W.t.p, y, (size_t)n * M.cfg.n_out * 4, cudaMemcpyHostToDevice, s));
+  CK(launch_to_bf16_t(xd.p, n, M.cfg.n_in, W.xh.p, W.xht.p, s));
+  if ((rc = forward(ctx, M, W, member, n, true, s))) return rc;
+  if ((rc = backward(ctx, M, W, member, n, s))) return rc;
+  CK(cudaMemcpyAsync(M.h_loss.p, W.loss.p, 4, cudaMemcpyDeviceToHost, s));
   size_t off = 0;
   for (auto& Ly : M.members[member]) {
     if (grads) {
@@ -462,9 +560,7 @@ int32_t omg_mlp_grad(omg_ctx* ctx, uint32_t id, uint32_t member, const float* x,
   }
   CK(cudaStreamSynchronize(s));
   if (loss) {
-    double l = 0.0;
-    for (uint32_t k = 0; k < kLossParts; k++) l += M.h_loss.p[k];
-    *loss = (float)l;
+    *loss = M.h_loss.p[0];
   }
   return check_err(ctx, M);
 }
@@ -544,7 +640,7 @@ int32_t omg_mlp_set_params(omg_ctx* ctx, uint32_t id, uint32_t what, const float
       for (auto& Ly : net) {
         CK(get_dev(Ly.W.p, (size_t)Ly.out * Ly.in));
         CK(get_dev(Ly.b.p, Ly.out));
-        CK(launch_to_bf16(Ly.W.p, Ly.Wh.p, (uint64_t)Ly.out * Ly.in, ctx->stream));
+        CK(launch_to_bf16_t(Ly.W.p, Ly.out, Ly.in, Ly.Wh.p, Ly.Wht.p, ctx->stream));
       }
     int32_t rc2 = sync_norm(ctx, M);
     if (rc2) return rc2;
@@ -559,6 +655,64 @@ int32_t omg_mlp_set_params(omg_ctx* ctx, uint32_t id, uint32_t what, const float
     M.step = (uint64_t)in[n];
   }
   CK(cudaStreamSynchronize(ctx->stream));
+  return OMG_OK;
+}
+
+// Device time of the tensor-core GEMM at one shape, for the record: A [m x k]
+// and B [n x k] bf16 (K-major), C f32 (atomically accumulated when k_split >
+// 1), operands resident on the device; `reps` launches between two events on
+// the context's stream after 3 untimed ones. *ms = mean per launch.
+int32_t omg_tc_gemm_bench(omg_ctx* ctx, uint32_t m, uint32_t n, uint32_t k, uint32_t k_split, uint32_t reps,
+                          float* ms) {
+  if (!ctx || !ms || m == 0 || n == 0 || k == 0 || k % 8 != 0 || reps == 0 || k_split == 0 || k_split > 64)
+    return OMG_E_INVALID;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t s = ctx->stream;
+  DevBuf<uint16_t> da, db;
+  DevBuf<float> dc;
+  DevBuf<uint32_t> err;
+  CK(da.alloc((size_t)m * k));
+  CK(db.alloc((size_t)n * k));
+  CK(dc.alloc((size_t)m * n));
+  CK(err.alloc(1));
+  CK(cudaMemsetAsync(err.p, 0, 4, s));
+  CK(cudaMemsetAsync(da.p, 0x3C, (size_t)m * k * 2, s));   // bf16 0x3C3C (about 0.0115) everywhere
+  CK(cudaMemsetAsync(db.p, 0x3C, (size_t)n * k * 2, s));
+  CK(cudaMemsetAsync(dc.p, 0, (size_t)m * n * 4, s));
+  GemmArgs g{};
+  g.A = da.p;
+  g.a_rs = k;
+  g.a_ks = 1;
+  g.B = db.p;
+  g.b_rs = k;
+  g.b_ks = 1;
+  g.M = m;
+  g.N = n;
+  g.K = k;
+  g.n_tile = n > 128 ? 128u : ((n + 15) & ~15u);
+  g.D = dc.p;
+  g.ldd = n;
+  g.accumulate = k_split > 1 ? 1u : 0u;
+  g.err = err.p;
+  for (int i = 0; i < 3; i++) CK(launch_gemm(g, k_split, s));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, s));
+  for (uint32_t i = 0; i < reps; i++) CK(launch_gemm(g, k_split, s));
+  CK(cudaEventRecord(e1, s));
+  CK(cudaEventSynchronize(e1));
+  float t = 0.0f;
+  CK(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  uint32_t e = 0;
+  CK(cudaMemcpy(&e, err.p, 4, cudaMemcpyDeviceToHost));
+  if (e) {
+    ctx->last_error = "tensor-core GEMM: an mbarrier wait ran out";
+    return OMG_E_TIMEOUT;
+  }
+  *ms = t / (float)reps;
   return OMG_OK;
 }
 

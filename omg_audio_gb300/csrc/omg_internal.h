@@ -326,10 +326,13 @@ struct GemmArgs {
   int64_t ldz;
   void* Y;                  // __nv_bfloat16 activation out or null
   int64_t ldy;
+  void* Yt;                 // the same activation transposed (element (m, n) at Yt[n ldyt + m]) or null
+  int64_t ldyt;
   uint32_t act;             // 0 none, 1 GELU (tanh form)
   uint32_t* err;            // error word: 16 = an mbarrier wait ran out
 };
 size_t gemm_smem_bytes();
+cudaError_t gemm_init();
 cudaError_t launch_gemm(const GemmArgs& g, uint32_t k_split, cudaStream_t s);
 cudaError_t launch_gelu_back(const float* dA, const float* Z, float* dZ, void* dZh, uint64_t n, cudaStream_t s);
 cudaError_t launch_colsum(const float* X, uint32_t rows, uint32_t cols, float* out, cudaStream_t s);
@@ -338,6 +341,21 @@ cudaError_t launch_mse(const float* Y, const float* T, const float* w, uint32_t 
 cudaError_t launch_adamw(float* W, float* m, float* v, const float* g, void* Wh, uint64_t n, float lr, float b1,
                          float b2, float eps, float wd, float bc1, float bc2, cudaStream_t s);
 cudaError_t launch_to_bf16(const float* x, void* y, uint64_t n, cudaStream_t s);
+// backward elementwise on 32 x 32 tiles: mode 0 the MSE loss gradient of
+// P = outputs against Q = targets (weights w per column, nullable; loss +=),
+// mode 1 dZ = P (dA) * GELU'(Q (Z)); writes dZ, its bf16 copy and transpose,
+// and adds the column sums into gb (zeroed by the caller)
+cudaError_t launch_grad_tile(uint32_t mode, const float* P, const float* Q, const float* w, uint32_t rows,
+                             uint32_t cols, float* dZ, void* dZh, void* dZht, float* gb, float* loss, cudaStream_t s);
+// AdamW of one layer (W [out x in] with bf16 copy and transpose, b [out]); the
+// step's learning rate and bias corrections at sched[3 *step]
+cudaError_t launch_adamw_layer(float* W, float* mW, float* vW, const float* gW, void* Wh, void* Wht, uint32_t in,
+                               uint32_t out, float* b, float* mb, float* vb, const float* gb, const float* sched,
+                               const uint32_t* step, float b1, float b2, float eps, float wd, cudaStream_t s);
+cudaError_t launch_step(uint32_t* step, cudaStream_t s);
+cudaError_t launch_gather_step(const float* X, uint32_t cols, const uint32_t* perm, const uint32_t* step,
+                               uint32_t spe, uint32_t rows, float* out, void* out_h, void* out_ht, cudaStream_t s);
+cudaError_t launch_to_bf16_t(const float* x, uint32_t rows, uint32_t cols, void* xh, void* xht, cudaStream_t s);
 cudaError_t launch_gather_rows(const float* X, uint32_t cols, const uint32_t* idx, uint32_t rows, float* out,
                                void* out_bf16, cudaStream_t s);
 cudaError_t launch_standardize(const float* x, const float* mean, const float* sd, uint32_t cols, uint64_t n,

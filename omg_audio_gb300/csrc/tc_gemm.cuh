@@ -110,6 +110,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
   return false;
 }
 
+// Asynchronous 16-byte global -> shared copies (cp.async, L2 only): `bytes`
+// (0 or 16) are read, the rest of the 16 bytes is filled with zeros.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, uint32_t bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem_dst)), "l"(gsrc), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // 16 consecutive f32 columns of this thread's TMEM lane (warp w of the CTA
 // reads lanes 32 w .. 32 w + 31).
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {

@@ -46,12 +46,15 @@ def _rel(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-30))
 
 
-def test_training_gradients_match_the_oracle(ctx):
+@pytest.mark.parametrize("rows,hidden", [(256, 64), (2048, 256)])
+def test_training_gradients_match_the_oracle(ctx, rows, hidden):
+    """256 rows: one K chunk per dW GEMM; 2048 rows: dW split over the grid
+    (atomic accumulation) and the pipelined GEMM at the training widths."""
     from oracle import mlp_oracle as MO
-    net = Mlp(ctx, n_in=38, hidden=64, n_hidden=3, n_out=48, members=1, seed=5)
+    net = Mlp(ctx, n_in=38, hidden=hidden, n_hidden=3, n_out=48, members=1, seed=5)
     rng = np.random.default_rng(11)
-    x = rng.standard_normal((256, 38)).astype(np.float32)
-    y = rng.standard_normal((256, 48)).astype(np.float32)
+    x = rng.standard_normal((rows, 38)).astype(np.float32)
+    y = rng.standard_normal((rows, 48)).astype(np.float32)
     loss, grads = net.grad(x, y)
     layers = net.layers(0)
     ol, og = MO.loss_and_grads(layers, x, y, bf=True)
@@ -138,3 +141,13 @@ def test_room_surrogate_gains_over_sabine_falls_back_and_checkpoints(tmp_path):
         assert np.array_equal(m1, m2) and np.array_equal(s1, s2)
         net2.close()
         sur.net.close()
+
+
+@pytest.mark.parametrize("m,n,k,split", [(4096, 256, 256, 1), (256, 256, 4096, 8)])
+def test_tc_gemm_bench_times_the_training_shapes(ctx, m, n, k, split):
+    """omg_tc_gemm_bench runs the GEMM at a training shape and reports a
+    positive device time per launch."""
+    ms = C.c_float()
+    rc = _lib.lib().omg_tc_gemm_bench(ctx.h, m, n, k, split, 20, C.byref(ms))
+    ctx._check(rc, "omg_tc_gemm_bench")
+    assert 0.0 < ms.value < 50.0
