@@ -93,37 +93,64 @@ __device__ __forceinline__ void stage_async(uint8_t* tile, const __nv_bfloat16* 
 
 constexpr uint32_t kStages = 3;   // cp.async pipeline depth
 
-// The epilogue: TMEM -> bias, optional GELU, the requested outputs.
-__device__ __forceinline__ void gemm_epilogue(const GemmArgs& g, uint32_t taddr, uint32_t m0, uint32_t n0, uint32_t nt,
-                                              uint32_t nt16) {
+// The epilogue: TMEM -> bias, optional GELU, the requested outputs. The
+// accumulator comes out of TMEM one row per thread (tcgen05.ld 32x32b); the
+// transposed activation Yt is written from that layout (consecutive lanes,
+// consecutive rows: coalesced). For the row-major outputs D, Z and Y each warp
+// stages 32 x 32 blocks in shared memory (the operand stages, free once the
+// last MMA has completed) and writes them row by row with consecutive lanes on
+// consecutive columns: whole 128-byte lines instead of one sector per element.
+__device__ __forceinline__ void gemm_epilogue(const GemmArgs& g, uint8_t* smem, uint32_t taddr, uint32_t m0,
+                                              uint32_t n0, uint32_t nt, uint32_t nt16) {
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   __nv_bfloat16* gY = static_cast<__nv_bfloat16*>(g.Y);
   __nv_bfloat16* gYt = static_cast<__nv_bfloat16*>(g.Yt);
-  const uint32_t row = m0 + warp * 32u + lane;
+  const bool rowwise = g.D || g.Z || gY;
+  float* st = reinterpret_cast<float*>(smem) + warp * (32u * 33u);
+  const uint32_t trow = m0 + warp * 32u + lane;          // this thread's TMEM row
   const uint32_t lane_addr = taddr + ((warp * 32u) << 16);
-  for (uint32_t c = 0; c < nt16; c += 16u) {
-    float v[16];
-    tc::tmem_ld16(lane_addr + c, v);
-    if (row >= g.M) continue;
+  for (uint32_t c = 0; c < nt16; c += 32u) {
+    const uint32_t w = min(32u, nt16 - c);               // 16 or 32 columns
+    float v[32];
+    {
+      float a[16], b[16];
+      tc::tmem_ld16(lane_addr + c, a);
+      if (w == 32u) tc::tmem_ld16(lane_addr + c + 16u, b);
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
-      const uint32_t col = n0 + c + (uint32_t)j;
-      if (c + (uint32_t)j >= nt) break;
-      float z = v[j];
-      if (g.bias) z += g.bias[col];
-      if (g.D) {
-        float* d = g.D + (int64_t)row * g.ldd + col;
-        if (g.accumulate) atomicAdd(d, z);
-        else *d = z;
-      }
-      if (g.Z) g.Z[(int64_t)row * g.ldz + col] = z;
-      if (gY || gYt) {
-        const __nv_bfloat16 y = __float2bfloat16_rn(g.act ? gelu_f(z) : z);
-        if (gY) gY[(int64_t)row * g.ldy + col] = y;
-        // consecutive lanes hold consecutive rows: the transposed store coalesces
-        if (gYt) gYt[(int64_t)col * g.ldyt + row] = y;
+      for (int j = 0; j < 16; j++) {
+        v[j] = a[j];
+        v[16 + j] = w == 32u ? b[j] : 0.0f;
       }
     }
+#pragma unroll
+    for (uint32_t j = 0; j < 32u; j++) {
+      if (j >= w) break;
+      const uint32_t col = n0 + c + j;
+      const bool ok = c + j < nt;
+      float z = v[j];
+      if (g.bias && ok) z += g.bias[col];
+      if (gYt && ok && trow < g.M) gYt[(int64_t)col * g.ldyt + trow] = __float2bfloat16_rn(g.act ? gelu_f(z) : z);
+      st[lane * 33u + j] = z;
+    }
+    __syncwarp();
+    if (rowwise) {
+      const uint32_t col = n0 + c + lane;
+      const bool ok = lane < w && c + lane < nt;
+      for (uint32_t r = 0; r < 32u; r++) {
+        const uint32_t row = m0 + warp * 32u + r;
+        if (row >= g.M) break;
+        if (!ok) continue;
+        const float z = st[r * 33u + lane];
+        if (g.D) {
+          float* d = g.D + (int64_t)row * g.ldd + col;
+          if (g.accumulate) atomicAdd(d, z);
+          else *d = z;
+        }
+        if (g.Z) g.Z[(int64_t)row * g.ldz + col] = z;
+        if (gY) gY[(int64_t)row * g.ldy + col] = __float2bfloat16_rn(g.act ? gelu_f(z) : z);
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -226,7 +253,7 @@ __global__ void __launch_bounds__(128, 1) gemm_kernel(GemmArgs g) {
   __syncthreads();
   tc::fence_after_sync();
   if (!failed && nk > 0) {
-    gemm_epilogue(g, taddr, m0, n0, nt, nt16);
+    gemm_epilogue(g, smem, taddr, m0, n0, nt, nt16);
   } else if (failed) {
     // give the last MMAs issued one more bounded wait before the TMEM is freed
     // (the slow path's only buffer was waited on already)

@@ -87,7 +87,9 @@ def parse_furniture(src: str):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_walkthrough_fixture.py <path of the reference checkout>")
+    ref = sys.argv[1]
     src = open(os.path.join(ref, "crates/omg-scene/src/walkthrough.rs")).read()
     rooms, doors = parse(src)
     furniture, min_vol = parse_furniture(src)
