@@ -271,7 +271,7 @@ def gemm_leg(ctx):
     return out
 
 
-def surrogate_leg(args, device):
+def surrogate_leg(args, device, city=None):
     """The learned surrogate against the GPU tracer on the config-1 room family
     (shoebox, 6 x 3 absorptions, up to 4 apertures, poses): training data from
     the tracer (args.surrogate_train_rays per room), the tensor-core MLP
@@ -356,6 +356,34 @@ def surrogate_leg(args, device):
     ok5 = [r for r in sweep if r["rt60_err_p90"] <= 0.05]
     chosen = max(ok5, key=lambda r: r["answered_frac"]) if ok5 else None
     gemm = gemm_leg(ctx)
+    city_leg = None
+    if city is not None:
+        # config 5's room/source pairs: every building x every source
+        gate = chosen["spread_db_max"] if chosen else sur.threshold_db
+        rooms = S.city_rooms(city.buildings, city.sources, city.absorption, city.window_frac)
+        sur.predict(rooms.take(np.arange(64)))
+        t0 = time.perf_counter()
+        cedc, cspread, cok = sur.predict(rooms)
+        t_cp = time.perf_counter() - t0
+        ans = S.in_range(S.features(rooms)) & (cspread <= (gate if gate is not None else np.inf))
+        fb = np.nonzero(~ans)[0]
+        t0 = time.perf_counter()
+        if len(fb):
+            S.trace_rooms(ctx, rooms.take(fb), 4096, seed=31)
+        t_fb = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        cb, _ = S.trace_rooms(ctx, rooms, 4096, seed=31)
+        t_all = time.perf_counter() - t0
+        crt = S.rt60_from_edc(S.edc_db(cb, 0.001))
+        cerr = np.abs(S.rt60_from_edc(cedc) / crt - 1.0)[ans]
+        city_leg = {"pairs": len(rooms), "rooms": "per building x source: the ground-floor room (<= 15 x 11 x 3.5 m) "
+                    "nearest the source, facade / ground / slab absorption at 250 Hz, 1 kHz, 4 kHz, perimeter walls "
+                    "with their windows as apertures", "spread_gate_db": gate,
+                    "answered_frac": float(np.mean(ans)), "fallback_pairs": int(len(fb)),
+                    "surrogate_ms": 1e3 * t_cp, "fallback_tracer_ms": 1e3 * t_fb,
+                    "ms_with_fallback": 1e3 * (t_cp + t_fb), "tracer_all_pairs_ms": 1e3 * t_all,
+                    "speedup_with_fallback": t_all / (t_cp + t_fb),
+                    "answered_rt60_err_vs_tracer_4096": {"median": q(cerr, 50), "p90": q(cerr, 90)}}
     ctx.close()
     return {
         "family": "shoebox 4-16 x 4-12 x 2.5-6 m, absorption U[0.02,0.4] x 6 surfaces x 3 bands, scattering 0.1, "
@@ -381,6 +409,7 @@ def surrogate_leg(args, device):
         "spread_gate_judge": f"the tracer at 65,536 rays on the first {n_floor} test rooms",
         "chosen_gate": chosen,
         "p90_target_met": chosen is not None,
+        "city_pairs": city_leg,
         "tracer_ms_per_room": tr_ms, "surrogate_ms_per_room": su_ms,
         "speedup": t_trace / t_pred, "surrogate_features_ms_per_room": 1e3 * t_feat / n,
         "timing": "wall clock of the calls with host buffers: trace_rooms (batched jobs, echograms down) vs "
@@ -457,6 +486,19 @@ def run_workload(args):
     torch.cuda.set_device(0)
     from omg_audio_gb300 import build as B
     B.build()
+    line = workload_summary(args, args.workload, args.steps, args.warmup, shape=args.shape or None,
+                            autotune=args.autotune)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_summary(args, workload, steps, warmup, case=None, shape=None, autotune=True):
+    """One secondary configuration measured (see run_workload): segments/s of
+    the trace part (CUDA events, L2 flushed before each step), the roofline by
+    the reference traversal's bytes per segment (the f32 oracle on a sample,
+    first-found rule, reference tree), the oracle's own rate, clocks."""
+    import torch
     from omg_audio_gb300 import Context, DomeProbe, Job, MeshBuilder, TraceConfig, _lib
     from omg_audio_gb300 import workloads as W
     bvh = {"sah": _lib.BVH_SAH, "lbvh": _lib.BVH_LBVH, "sah3": _lib.BVH_SAH3}[args.bvh]
@@ -465,7 +507,7 @@ def run_workload(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     t0 = time.perf_counter()
     oracle_jobs = []   # (mesh recorder or box, src, lis, n_rays, seed, n_bands, n_bins, max_time) for the CPU leg
-    if args.workload == "shoebox12":
+    if workload == "shoebox12":
         case = W.shoebox12(seed=1)
         ctx = Context(TraceConfig(timeout_ms=60000, tie_mode=1, **CFG))
         mb = MeshBuilder()
@@ -476,7 +518,7 @@ def run_workload(args):
         desc = "shoebox12: 10 x 7 x 4 m room as 12 triangles, 4096 rays x 3 bands, 2000 x 1 ms bins, 200 bounces"
         dome = None
         prims = sc.info()["prims"]
-    elif args.workload == "rooms256":
+    elif workload == "rooms256":
         rooms = W.room_batch(seed=3, n_rooms=256)
         ctx = Context(TraceConfig(timeout_ms=120000, tie_mode=1, n_bins=4000, max_time=4.0, max_bounces=200,
                                   energy_floor=1e-6))
@@ -495,7 +537,7 @@ def run_workload(args):
         dome = None
         prims = sum(sc.info()["prims"] for sc in scenes)
     else:
-        case = W.city(seed=5)
+        case = case or W.city(seed=5)
         ctx = Context(TraceConfig(timeout_ms=300000, tie_mode=1, n_bands=case.n_bands, n_bins=4000, bin_dt=0.001,
                                   max_time=4.0, max_bounces=200, energy_floor=1e-6))
         mb = MeshBuilder()
@@ -513,27 +555,27 @@ def run_workload(args):
     setup_s = time.perf_counter() - t0
     ctx.set_stream(stream.cuda_stream)
     batch = ctx.batch(jobs)
-    if args.shape:
-        batch.set_shape(**json.loads(args.shape))
+    if shape:
+        batch.set_shape(**json.loads(shape))
         tune = batch.shape()
     else:
-        tune = batch.autotune(reps=1) if args.autotune else batch.shape()
-    for _ in range(max(args.warmup, 1)):
+        tune = batch.autotune(reps=1) if autotune else batch.shape()
+    for _ in range(max(warmup, 1)):
         batch.launch()
     torch.cuda.synchronize()
     if args.profile:
         # small case for a profiler: the launches only, nothing timed or printed
-        for _ in range(args.steps):
+        for _ in range(steps):
             batch.launch()
             if dome is not None:
                 dome.submit(case.dome_eyes, n_rays=512, stream=stream.cuda_stream, want=2)
                 torch.cuda.synchronize()
                 dome.collect()
         torch.cuda.synchronize()
-        return 0
+        return None
     ms, dms = [], []
     with ClockSampler(0) as clk:
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -553,8 +595,8 @@ def run_workload(args):
     batch.launch()
     res = batch.read()
     segs = batch.segments()
-    line = {"metric": "ray-segments/s", "workload": args.workload, "desc": desc, "prims": prims,
-            "bvh": args.bvh, "setup_s": setup_s, "steps": args.steps, "trace_ms": float(np.mean(ms)),
+    line = {"metric": "ray-segments/s", "workload": workload, "desc": desc, "prims": prims,
+            "bvh": args.bvh, "setup_s": setup_s, "steps": steps, "trace_ms": float(np.mean(ms)),
             "segments": segs, "value": segs / (float(np.mean(ms)) * 1e-3), "unit": "ray-segments/s",
             "autotune": tune, "clocks": clk.summary(),
             "rt60_range": [float(np.nanmin([np.min(rv.rt60) for _, rv in res])),
@@ -600,7 +642,35 @@ def run_workload(args):
         line["dome"] = {"eyes": len(case.dome_eyes), "ms": float(np.mean(dms)), "segments": dseg,
                         "segments_per_s": dseg / (float(np.mean(dms)) * 1e-3),
                         "sky_escape_frac": float(np.mean(dres["escape"]))}
-    print(json.dumps(line), flush=True)
+    ctx.close()
+    torch.cuda.set_stream(torch.cuda.default_stream())
+    return line
+
+
+def compact_summary(line):
+    keep = {k: line[k] for k in ("desc", "prims", "bvh", "setup_s", "steps", "trace_ms", "segments", "value",
+                                 "unit", "autotune", "clocks", "cpu_baseline", "dome") if k in line}
+    rf = line.get("roofline", {})
+    keep["roofline"] = {k: rf[k] for k in ("bytes_per_segment", "achieved", "peak", "unit", "frac", "n_node",
+                                           "n_prim", "h", "formula") if k in rf}
+    return keep
+
+
+def run_gemm_profile(args):
+    """A small case for a profiler: the surrogate's GEMM at its training shapes
+    (omg_tc_gemm_bench, a few launches each), nothing printed."""
+    import ctypes as C
+
+    import torch
+    torch.cuda.set_device(0)
+    from omg_audio_gb300 import build as B
+    B.build()
+    from omg_audio_gb300 import Context, TraceConfig, _lib
+    with Context(TraceConfig(device=0)) as ctx:
+        ms = C.c_float()
+        for (m, n, k, split) in ((4096, 256, 256, 1), (256, 256, 4096, 8)):
+            ctx._check(_lib.lib().omg_tc_gemm_bench(ctx.h, m, n, k, split, max(1, args.steps), C.byref(ms)),
+                       "omg_tc_gemm_bench")
     return 0
 
 
@@ -757,10 +827,20 @@ def run_ours(args):
                                        f"(f32 oracle, the reference's first-found rule and tree, {threads} threads)"},
             "clocks": clk.summary(),
         }
+        city = None
+        if args.extra_workloads:
+            from omg_audio_gb300 import workloads as W
+            city = W.city(seed=5)
         if args.surrogate:
-            line["surrogate"] = surrogate_leg(args, local)
+            line["surrogate"] = surrogate_leg(args, local, city)
         if args.early_listeners > 0:
             line["early"] = early_leg(args, local, case)
+        if args.extra_workloads:
+            # the other two tracer configurations, measured here too (a few
+            # steps each; the full lines come from --workload rooms256 / city)
+            for name in ("rooms256", "city"):
+                line[name] = compact_summary(workload_summary(args, name, args.extra_steps, 1,
+                                                              case=city if name == "city" else None))
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()
@@ -779,6 +859,8 @@ def main():
     ap.add_argument("--ref-pairs", type=int, default=64)
     ap.add_argument("--pairs", type=int, default=N_PAIRS, help="pairs traced per step (default: the workload's 64)")
     ap.add_argument("--profile", action="store_true", help="launches only (a small case under a profiler)")
+    ap.add_argument("--profile-gemm", action="store_true",
+                    help="the surrogate's GEMM at two training shapes, --steps launches each (for a profiler)")
     ap.add_argument("--no-surrogate", dest="surrogate", action="store_false",
                     help="skip the surrogate leg (train on tracer data, compare with the tracer)")
     ap.add_argument("--early-listeners", type=int, default=8,
@@ -798,11 +880,16 @@ def main():
     ap.add_argument("--workload", choices=["multiroom", "shoebox12", "rooms256", "city"], default="multiroom",
                     help="multiroom: the headline (default); rooms256 and city print their own line")
     ap.add_argument("--city-rays", type=int, default=1 << 20, help="rays per source of the city workload")
+    ap.add_argument("--no-extra-workloads", dest="extra_workloads", action="store_false",
+                    help="skip the rooms256 and city summaries of the headline line")
+    ap.add_argument("--extra-steps", type=int, default=3, help="timed steps of each extra workload")
     args = ap.parse_args()
     if args.bvh is None:
         args.bvh = "sah3"
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_gemm:
+        return run_gemm_profile(args)
     if args.workload != "multiroom":
         return run_workload(args)
     return run_ours(args)

@@ -1,7 +1,7 @@
 // estimate_reverb on the GPU (crates/omg-core/src/tracer.rs:204-257): one warp
 // per (echogram, band). FP64 is used only here, for the Schroeder backward
-// integral and the line fit; the late level reads the same FP64 integral at
-// the 80 ms bin (the energy after 80 ms is exactly EDC[late_start]).
+// integral and the line fit. The late level is the reference's own f32 sum of
+// the bins from 80 ms on, in its order (tracer.rs:246-254), by one lane.
 #include <cfloat>
 
 #include "omg_internal.h"
@@ -96,8 +96,9 @@ __global__ void reverb_kernel(const DReverbJob* __restrict__ rj, uint32_t n_jobs
     // tracer.rs:246: late_start = (0.080 / BIN_DT) as usize in f32
     const float q = 0.080f / R.bin_dt;
     const uint64_t ls = (q >= 0.0f) ? (uint64_t)q : 0;
-    const double late = ls < n ? edc[ls] : 0.0;
-    out[j].level[b] = fminf((float)sqrt(late), 0.7f);
+    float late = 0.0f;
+    for (uint64_t i = ls; i < n; i++) late += B[i * nb + b];
+    out[j].level[b] = fminf(sqrtf(late), 0.7f);
     if (b == 0) out[j].segments = job_segments ? job_segments[j] : 0;
   }
 }

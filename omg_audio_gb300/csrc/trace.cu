@@ -55,6 +55,8 @@ __device__ __forceinline__ float walk_cull(const Walk& w) {
 }
 
 constexpr int kDone = 0x7FFFFFFF;  // never a node index (< 2^28)
+constexpr int kMaxWarps = 8;       // warps of a trace_kernel block (at most 256 threads)
+constexpr int kCoopRounds = 8;     // cooperative leaf rounds per loop iteration
 
 template <bool TIE>
 __device__ __forceinline__ int walk_pop(Walk& w) {
@@ -104,19 +106,12 @@ __device__ __forceinline__ bool walk_restart_fixed(Walk& w, int root, uint32_t b
   return true;
 }
 
-// One leaf of a near-tie walk (the rule of tie_take, device_common.cuh, on the
+// One hit of a near-tie walk, primitive i at t with authored surface s and
+// original triangle tr (the rule of tie_take, device_common.cuh, on the
 // compact state).
-__device__ __forceinline__ void walk_leaf_tie(Walk& w, const float4* __restrict__ prims, int leaf, float ox,
-                                              float oy, float oz, float dx, float dy, float dz) {
-  const uint32_t code = ~(uint32_t)leaf;
-  const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
-  for (uint32_t i = start; i < end; i++) {
-    const float4 p0 = __ldg(prims + 3 * i + 0);
-    const float4 p1 = __ldg(prims + 3 * i + 1);
-    const float4 p2 = __ldg(prims + 3 * i + 2);
-    float t;
-    if (!ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) continue;
-    const uint32_t s = __float_as_uint(p2.w), tr = __float_as_uint(p1.w);
+__device__ __forceinline__ void walk_take_tie(Walk& w, const float4* __restrict__ prims, uint32_t i, float t,
+                                              uint32_t s, uint32_t tr) {
+  {
     const bool have = w.prim_best >= 0;
     // the winner's key, read back from its primitive
     auto less_than_best = [&]() {
@@ -146,6 +141,21 @@ __device__ __forceinline__ void walk_leaf_tie(Walk& w, const float4* __restrict_
       w.prim_best = (int)i;
       w.t_best = t;
     }
+  }
+}
+
+// One leaf of a near-tie walk, its primitives in order.
+__device__ __forceinline__ void walk_leaf_tie(Walk& w, const float4* __restrict__ prims, int leaf, float ox,
+                                              float oy, float oz, float dx, float dy, float dz) {
+  const uint32_t code = ~(uint32_t)leaf;
+  const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
+  for (uint32_t i = start; i < end; i++) {
+    const float4 p0 = __ldg(prims + 3 * i + 0);
+    const float4 p1 = __ldg(prims + 3 * i + 1);
+    const float4 p2 = __ldg(prims + 3 * i + 2);
+    float t;
+    if (!ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) continue;
+    walk_take_tie(w, prims, i, t, __float_as_uint(p2.w), __float_as_uint(p1.w));
   }
 }
 
@@ -186,17 +196,17 @@ __device__ __forceinline__ bool walk4_steps(Walk& w, const DScene& S, float ox, 
   return w.cur == kDone;
 }
 
-// The near-tie walk (TIE = true): speculative while-while over the grown
-// boxes with the fused multiply-add slab test. A ray whose origin lies beyond
-// the boxes' margin (|o_a| > 7 M_a: never in a trace that starts inside the
-// scene) or that runs along a coordinate plane (a direction component of 0)
-// uses the plain slab test on the same grown boxes.
-__device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, float oy, float oz, float dx,
-                                          float dy, float dz, int steps, uint32_t* err) {
-  // speculative while-while: descend, postponing one leaf, until every lane of
-  // the warp holds a leaf; then test leaves
+// The node phase of the near-tie walk (TIE = true): speculative while-while
+// descent over the grown boxes with the fused multiply-add slab test,
+// postponing one leaf, until every lane of the warp holds a leaf (or has none
+// left to reach). A ray whose origin lies beyond the boxes' margin (|o_a| >
+// 7 M_a: never in a trace that starts inside the scene) or that runs along a
+// coordinate plane (a direction component of 0) uses the plain slab test on
+// the same grown boxes. Returns true when the walk ran out of its budget (it
+// is then over, flag 4 raised).
+__device__ __forceinline__ bool walk_spec_nodes(Walk& w, const DScene& S, float ox, float oy, float oz, float dx,
+                                                float dy, float dz, int& steps, uint32_t* err) {
   const float4* __restrict__ tnodes = S.nodes_f;
-  const float4* __restrict__ prims = S.prims;
   while (steps > 0 && w.cur >= 0 && w.cur != kDone) {
     steps--;
     if (w.budget-- == 0u) {
@@ -251,6 +261,16 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
     w.leaf = w.cur;
     w.cur = walk_pop<true>(w);
   }
+  return false;
+}
+
+// The near-tie walk (TIE = true): speculative while-while over the grown
+// boxes with the fused multiply-add slab test (walk_spec_nodes), then the
+// postponed leaves one after another.
+__device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, float oy, float oz, float dx,
+                                          float dy, float dz, int steps, uint32_t* err) {
+  const float4* __restrict__ prims = S.prims;
+  if (walk_spec_nodes(w, S, ox, oy, oz, dx, dy, dz, steps, err)) return true;
   while (w.leaf < 0 && steps > 0) {
     steps--;
     if (w.budget-- == 0u) {
@@ -271,6 +291,93 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
     return !walk_restart_fixed(w, S.root, S.walk_budget);
   }
   return false;
+}
+
+// Leaves of near-tie walks tested by the whole warp (every lane calls this,
+// warp-uniformly; `own`: this lane is walking). A leaf holds 1 to 8
+// primitives, and one lane testing its own leaf's primitives one after
+// another leaves most of the warp idle; here the primitives of every lane's
+// pending leaf are laid out in a per-warp slot list (shared memory, `slots`:
+// 256 bytes), each lane tests one slot's primitive against the slot owner's
+// ray (fetched by shuffles), and each owner then takes its hits in leaf order,
+// so the near-tie state sees the sequence walk_leaf_tie would give it. After a
+// round, a walk whose next node is a leaf postpones it, and rounds repeat
+// while any lane holds a leaf (at most `rounds`).
+__device__ __forceinline__ void coop_leaf_rounds(Walk& w, bool own_walk, const float4* lane_prims, float ox,
+                                                 float oy, float oz, float dx, float dy, float dz,
+                                                 uint8_t* __restrict__ slots, int rounds, uint32_t* err) {
+  const unsigned FULL = 0xffffffffu;
+  const uint32_t lane = threadIdx.x & 31u;
+  const unsigned long long my_prims = reinterpret_cast<unsigned long long>(lane_prims);
+  while (rounds-- > 0) {
+    bool own = own_walk && w.leaf < 0;
+    if (__ballot_sync(FULL, own) == 0u) break;
+    uint32_t start = 0, cnt = 0;
+    if (own) {
+      if (w.budget-- == 0u) {
+        // out of budget: the walk is over (and is not walked again)
+        atomicOr(err, 4u);
+        w.cur = kDone;
+        w.leaf = 0;
+        w.flags &= ~kWalkAmb;
+        own = false;
+      } else {
+        const uint32_t code = ~(uint32_t)w.leaf;
+        start = code >> 3;
+        cnt = (code & 7u) + 1u;
+        w.leaf = 0;
+      }
+    }
+    // slot ranges: an inclusive scan of the leaf sizes over the warp
+    uint32_t inc = cnt;
+#pragma unroll
+    for (uint32_t d = 1; d < 32u; d <<= 1) {
+      const uint32_t v = __shfl_up_sync(FULL, inc, d);
+      if (lane >= d) inc += v;
+    }
+    const uint32_t total = __shfl_sync(FULL, inc, 31);
+    const uint32_t excl = inc - cnt;
+    const uint32_t kmax = __reduce_max_sync(FULL, cnt);
+    for (uint32_t k = 0; k < cnt; k++) slots[excl + k] = (uint8_t)lane;
+    __syncwarp();
+    for (uint32_t base = 0; base < total; base += 32u) {
+      const uint32_t p = base + lane;
+      const bool act = p < total;
+      const uint32_t o = act ? slots[p] : 0u;
+      const uint32_t o_start = __shfl_sync(FULL, start, o), o_excl = __shfl_sync(FULL, excl, o);
+      const float rx = __shfl_sync(FULL, ox, o), ry = __shfl_sync(FULL, oy, o), rz = __shfl_sync(FULL, oz, o);
+      const float sx = __shfl_sync(FULL, dx, o), sy = __shfl_sync(FULL, dy, o), sz = __shfl_sync(FULL, dz, o);
+      const float4* P = reinterpret_cast<const float4*>(__shfl_sync(FULL, my_prims, o));
+      const uint32_t i = o_start + (p - o_excl);
+      float t = 0.0f;
+      bool hit = false;
+      uint32_t sid = 0, tri = 0;
+      if (act) {
+        const float4 p0 = __ldg(P + 3 * i + 0);
+        const float4 p1 = __ldg(P + 3 * i + 1);
+        const float4 p2 = __ldg(P + 3 * i + 2);
+        hit = ray_tri(p0, p1, p2, rx, ry, rz, sx, sy, sz, t);
+        sid = __float_as_uint(p2.w);
+        tri = __float_as_uint(p1.w);
+      }
+      // each owner takes its slots of this chunk in leaf order
+      for (uint32_t k = 0; k < kmax; k++) {
+        const uint32_t q = excl + k;
+        const bool mine = own && k < cnt && q >= base && q < base + 32u;
+        const uint32_t src = mine ? q - base : lane;
+        const float tk = __shfl_sync(FULL, t, src);
+        const bool hk = __shfl_sync(FULL, (uint32_t)hit, src) != 0u;
+        const uint32_t sk = __shfl_sync(FULL, sid, src), trk = __shfl_sync(FULL, tri, src);
+        const uint32_t ik = __shfl_sync(FULL, i, src);
+        if (mine && hk) walk_take_tie(w, lane_prims, ik, tk, sk, trk);
+      }
+    }
+    __syncwarp();
+    if (own && w.cur < 0) {
+      w.leaf = w.cur;
+      w.cur = walk_pop<true>(w);
+    }
+  }
 }
 
 // Up to `steps` node visits / leaf tests; returns true when the walk is done.
@@ -387,6 +494,7 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
   const uint32_t keep = (uint32_t)(((uint64_t)n_rays * ea.park_pct) / 100u);
   bool parking = false;
   uint32_t iters = 0;   // loop guard (warp-uniform: every lane runs every iteration)
+  __shared__ uint8_t s_slots[kMaxWarps][256];   // coop_leaf_rounds' slot lists, one per warp
 
   // begin one segment from (p, d): the box hit directly, or a mesh walk
   auto begin_segment = [&](const DJob& J) {
@@ -462,25 +570,48 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
     const bool shade_now = ready != 0u && (walking == 0u || __popc(ready) >= (int)shade_min);
 
     // ---- closest-hit walk, at most walk_budget steps this iteration
-    if (!shade_now && phase == WALK) {
+    // the walk is over: its hit (normal of the original triangle, against d)
+    auto finish_walk = [&](const DScene& S) {
+      have = walk_have(w);
+      h.t = FLT_MAX;
+      h.m = nullptr;
+      if (have) {
+        const float4 p0 = __ldg(S.prims + 3 * w.prim_best + 0);
+        const float4 p1 = __ldg(S.prims + 3 * w.prim_best + 1);
+        const float4 nn = __ldg(S.normals + __float_as_uint(p1.w));
+        float nx = nn.x, ny = nn.y, nz = nn.z;
+        if (nx * dx + ny * dy + nz * dz > 0.0f) { nx = nx * -1.0f; ny = ny * -1.0f; nz = nz * -1.0f; }
+        h.t = w.t_best;
+        h.nx = nx; h.ny = ny; h.nz = nz;
+        h.m = S.mats + __float_as_uint(p0.w);
+      }
+      phase = SHADE;
+    };
+    if (TIE && !wide) {
+      // near-tie walks on the binary tree: the node phase lane by lane, then
+      // the pending leaves tested by the whole warp together
+      if (!shade_now) {
+        const bool wk = phase == WALK;
+        const float4* lp = nullptr;
+        bool over = false;
+        if (wk) {
+          const DScene& S = scenes[jobs[ji].scene];
+          lp = S.prims;
+          int st = walk_budget;
+          over = walk_spec_nodes(w, S, px, py, pz, dx, dy, dz, st, err);
+        }
+        coop_leaf_rounds(w, wk && !over, lp, px, py, pz, dx, dy, dz, s_slots[threadIdx.x >> 5], kCoopRounds, err);
+        if (wk) {
+          const DScene& S = scenes[jobs[ji].scene];
+          // an ambiguous near-tie window: the walk starts over in fixed mode
+          if (!over && w.cur == kDone && w.leaf == 0) over = !walk_restart_fixed(w, S.root, S.walk_budget);
+          if (over) finish_walk(S);
+        }
+      }
+    } else if (!shade_now && phase == WALK) {
       const DJob& J = jobs[ji];
       const DScene& S = scenes[J.scene];
-      if (walk_steps<TIE>(w, S, px, py, pz, dx, dy, dz, walk_budget, wide, err)) {
-        have = walk_have(w);
-        h.t = FLT_MAX;
-        h.m = nullptr;
-        if (have) {
-          const float4 p0 = __ldg(S.prims + 3 * w.prim_best + 0);
-          const float4 p1 = __ldg(S.prims + 3 * w.prim_best + 1);
-          const float4 nn = __ldg(S.normals + __float_as_uint(p1.w));
-          float nx = nn.x, ny = nn.y, nz = nn.z;
-          if (nx * dx + ny * dy + nz * dz > 0.0f) { nx = nx * -1.0f; ny = ny * -1.0f; nz = nz * -1.0f; }
-          h.t = w.t_best;
-          h.nx = nx; h.ny = ny; h.nz = nz;
-          h.m = S.mats + __float_as_uint(p0.w);
-        }
-        phase = SHADE;
-      }
+      if (walk_steps<TIE>(w, S, px, py, pz, dx, dy, dz, walk_budget, wide, err)) finish_walk(S);
     }
 
     // ---- one segment of the bounce loop (tracer.rs:103-200)

@@ -200,6 +200,49 @@ def sample_rooms(n: int, seed: int) -> Rooms:
     return Rooms(size, alpha, openness, src, lis)
 
 
+# the city's octave bands (63 Hz ... 8 kHz) that are the surrogate's 250 Hz, 1 kHz and 4 kHz
+CITY_BANDS = (2, 4, 6)
+CITY_CELL = (15.0, 11.0)     # largest ground-floor room of a building (x, y), inside the family's sizes
+
+
+def city_rooms(buildings, sources, absorption, window_frac=0.4, listener_z=1.5) -> Rooms:
+    """The city's room/source pairs as shoebox rooms (every building x every
+    source): the ground floor of each building is cut into a grid of rooms no
+    larger than CITY_CELL, and the pair's room is the cell nearest the source.
+    Walls take the facade's absorption, the floor the ground's, the ceiling
+    the slabs' (CITY_BANDS of the city's octave bands); a wall on the
+    building's perimeter has its windows (window_frac of it open) as the
+    aperture's openness, an inner wall none. The source stands in the cell at
+    the point nearest the street source, 1 m from the walls; the listener at
+    the cell's centre. buildings (n, 6): footprint min x, y, size x, y,
+    height, storey height; sources (m, 3)."""
+    b = np.asarray(buildings, np.float64)
+    src = np.asarray(sources, np.float64)
+    nb, ns = len(b), len(src)
+    bi = np.repeat(np.arange(nb), ns)
+    si = np.tile(np.arange(ns), nb)
+    x0, y0, w, d, fh = b[bi, 0], b[bi, 1], b[bi, 2], b[bi, 3], b[bi, 5]
+    nx, ny = np.ceil(w / CITY_CELL[0]), np.ceil(d / CITY_CELL[1])
+    cw, cd = w / nx, d / ny
+    px = np.clip(src[si, 0], x0, x0 + w)
+    py = np.clip(src[si, 1], y0, y0 + d)
+    ix = np.minimum(np.floor((px - x0) / cw), nx - 1)
+    iy = np.minimum(np.floor((py - y0) / cd), ny - 1)
+    size = np.stack([cw, cd, fh], 1)
+    lo = np.stack([x0 + ix * cw, y0 + iy * cd], 1)
+    pick = lambda k: np.asarray(absorption[k], np.float64)[list(CITY_BANDS)]
+    alpha = np.empty((len(bi), 6, N_BANDS))
+    alpha[:, 0:4, :] = pick("facade")
+    alpha[:, 4, :] = pick("ground")
+    alpha[:, 5, :] = pick("slab")
+    outer = np.stack([ix == 0, ix == nx - 1, iy == 0, iy == ny - 1], 1)
+    openness = np.where(outer, window_frac, 0.0)
+    s_local = np.stack([np.clip(px - lo[:, 0], 1.0, cw - 1.0), np.clip(py - lo[:, 1], 1.0, cd - 1.0),
+                        np.clip(src[si, 2], 1.0, fh - 1.0)], 1)
+    l_local = np.stack([0.5 * cw, 0.5 * cd, np.minimum(listener_z, 0.5 * fh)], 1)
+    return Rooms(size, alpha, openness, s_local, l_local)
+
+
 def aperture_boxes(size):
     """One aperture per side wall (x-, x+, y-, y+) of each room: a panel box
     flush with the wall, APERTURE_W wide (clipped to the wall) and APERTURE_H

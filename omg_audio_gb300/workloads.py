@@ -329,6 +329,8 @@ class CityCase:
     dome_eyes: np.ndarray        # (n_eyes, 3)
     buildings: np.ndarray        # (n, 6): footprint min x, y, size x, y, height, floor height
     n_bands: int
+    absorption: dict = None      # per-band absorption of the "facade", "slab" and "ground" materials
+    window_frac: float = 0.4     # share of facade cells left open
 
 
 def _grid_quads(p0, u, v, nu, nv):
@@ -352,12 +354,12 @@ def city(seed: int = 5, nx: int = 20, ny: int = 10, pitch: float = 60.0, cell: f
     at 1.5 m."""
     rng = np.random.default_rng(seed)
     rec = Recorder()
-    facade = rec.material(Material(tuple(float(v) for v in rng.uniform(0.02, 0.1, n_bands)), 0.2,
-                                   tuple([0.0] * n_bands)))
-    slab = rec.material(Material(tuple(float(v) for v in rng.uniform(0.01, 0.05, n_bands)), 0.1,
-                                 tuple([0.0] * n_bands)))
-    ground = rec.material(Material(tuple(float(v) for v in rng.uniform(0.02, 0.15, n_bands)), 0.3,
-                                   tuple([0.0] * n_bands)))
+    alpha = {"facade": tuple(float(v) for v in rng.uniform(0.02, 0.1, n_bands))}
+    facade = rec.material(Material(alpha["facade"], 0.2, tuple([0.0] * n_bands)))
+    alpha["slab"] = tuple(float(v) for v in rng.uniform(0.01, 0.05, n_bands))
+    slab = rec.material(Material(alpha["slab"], 0.1, tuple([0.0] * n_bands)))
+    alpha["ground"] = tuple(float(v) for v in rng.uniform(0.02, 0.15, n_bands))
+    ground = rec.material(Material(alpha["ground"], 0.3, tuple([0.0] * n_bands)))
     blocks = []
     quads, mats, surf = [], [], []
 
@@ -408,4 +410,4 @@ def city(seed: int = 5, nx: int = 20, ny: int = 10, pitch: float = 60.0, cell: f
     src = street_points(n_sources)
     lis = street_points(n_sources)
     eyes = street_points(n_dome)
-    return CityCase(rec, src, lis, eyes, np.array(blocks, np.float32), n_bands)
+    return CityCase(rec, src, lis, eyes, np.array(blocks, np.float32), n_bands, alpha, window_frac)
