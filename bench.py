@@ -330,8 +330,10 @@ def surrogate_leg(args, device, city=None):
     sub = test.take(np.arange(n_floor))
     rt_b = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, sub, 4096, seed=8)[0], 0.001))
     rt_c = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, sub, 65536, seed=9)[0], 0.001))
+    rt_d = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, sub, 65536, seed=10)[0], 0.001))
     nz_seed = np.abs(rt_b / rt_t[:n_floor] - 1.0)
     nz_65k = np.abs(rt_t[:n_floor] / rt_c - 1.0)
+    nz_65k_65k = np.abs(rt_d / rt_c - 1.0)
     sur_65k = np.abs(rt_p[:n_floor] / rt_c - 1.0)
 
     def q(a, p):
@@ -404,6 +406,7 @@ def surrogate_leg(args, device, city=None):
             "rooms": n_floor,
             "tracer_4096_vs_4096_other_seed": {"median": q(nz_seed, 50), "p90": q(nz_seed, 90)},
             "tracer_4096_vs_65536": {"median": q(nz_65k, 50), "p90": q(nz_65k, 90)},
+            "tracer_65536_vs_65536_other_seed": {"median": q(nz_65k_65k, 50), "p90": q(nz_65k_65k, 90)},
             "surrogate_vs_65536": {"median": q(sur_65k, 50), "p90": q(sur_65k, 90)}},
         "spread_gate_sweep": sweep,
         "spread_gate_judge": f"the tracer at 65,536 rays on the first {n_floor} test rooms",
@@ -868,7 +871,8 @@ def main():
     ap.add_argument("--surrogate-rooms", type=int, default=131072, help="training rooms (1 M: the full config)")
     ap.add_argument("--surrogate-epochs", type=int, default=60)
     ap.add_argument("--surrogate-test", type=int, default=16384, help="held-out rooms")
-    ap.add_argument("--surrogate-train-rays", type=int, default=1024, help="tracer rays per training room")
+    ap.add_argument("--surrogate-train-rays", type=int, default=8192,
+                    help="tracer rays per training room (the labels' Monte-Carlo noise is the loss floor)")
     ap.add_argument("--surrogate-floor-rooms", type=int, default=2048,
                     help="test rooms traced again (another seed; 65,536 rays) for the judge's noise floor")
     ap.add_argument("--max-bounces", type=int, default=0,

@@ -17,7 +17,9 @@ namespace omg {
 
 struct MlpLayer {
   uint32_t in = 0, out = 0;
-  DevBuf<float> W, b, mW, vW, mb, vb, gW, gb;
+  DevBuf<float> W, b, mW, vW, mb, vb;
+  float* gW = nullptr;    // the gradients: views into the member's gradient block
+  float* gb = nullptr;
   DevBuf<uint16_t> Wh;    // bf16 copy of W [out x in]
   DevBuf<uint16_t> Wht;   // its transpose [in x out]: the K-major operand of dX = dZ . W
 };
@@ -32,7 +34,7 @@ struct MlpBufs {
   DevBuf<float> t;                        // batch targets
   std::vector<DevBuf<float>> Z;           // pre-activations per layer
   std::vector<DevBuf<uint16_t>> A, At;    // bf16 activations per hidden layer, and transposes
-  DevBuf<float> out, dX, dZ, loss;
+  DevBuf<float> out, dX, dZ;
   DevBuf<uint16_t> dZh, dZht;
 };
 
@@ -54,6 +56,9 @@ struct MlpTrainer {
 struct MlpRec {
   omg_mlp_config cfg{};
   std::vector<std::vector<MlpLayer>> members;   // [member][layer]
+  // per member, one block: every layer's gW then gb, then the loss (one memset clears it)
+  std::vector<DevBuf<float>> grads;
+  uint64_t grad_floats = 0;
   // standardization (host and device)
   std::vector<float> x_mean, x_std, y_mean, y_std;
   DevBuf<float> d_x_mean, d_x_std, d_y_mean, d_y_std;
@@ -101,14 +106,13 @@ int32_t ensure_batch(omg_ctx* ctx, const MlpRec& M, MlpBufs& W, uint32_t rows, b
     CK(W.xht.alloc((size_t)rows * M.cfg.n_in));
     CK(W.dZht.alloc((size_t)rows * wide));
   }
-  CK(W.loss.alloc(1));
   W.cap = rows;
   return OMG_OK;
 }
 
-// columns per CTA of a GEMM with n output columns: 128 when that still leaves
-// whole 16-column MMAs, else all of them (<= 256)
-uint32_t n_tile_of(uint32_t n) { return n > 128 ? 128u : ((n + 15) & ~15u); }
+// columns per CTA of a GEMM with n output columns: 64 (more, smaller CTAs:
+// these GEMMs are short and latency-bound), or all of them when fewer
+uint32_t n_tile_of(uint32_t n) { return n > 64 ? 64u : ((n + 15) & ~15u); }
 
 // X0 (bf16, rows x n_in) -> out (f32, rows x n_out); keeps Z and A (and, for
 // training, the transposed activations At) for backward
@@ -154,22 +158,21 @@ int32_t forward(omg_ctx* ctx, MlpRec& M, MlpBufs& W, uint32_t e, uint32_t rows, 
   return OMG_OK;
 }
 
-// gradients of the MSE (targets in W.t) into the layers' gW, gb; the loss into
-// W.loss (both zeroed here first). Every GEMM reads K-major operands: dW =
-// dZ^T X from the transposes dZht and xht / At, dX = dZ W from dZh and Wht.
+// gradients of the MSE (targets in W.t) into the layers' gW, gb and the loss
+// into the member's gradient block (all zeroed here first, in one memset).
+// Every GEMM reads K-major operands: dW = dZ^T X from the transposes dZht and
+// xht / At, dX = dZ W from dZh and Wht.
 int32_t backward(omg_ctx* ctx, MlpRec& M, MlpBufs& W, uint32_t e, uint32_t rows, cudaStream_t s) {
   const uint32_t L = n_layers(M);
   auto& net = M.members[e];
-  CK(cudaMemsetAsync(W.loss.p, 0, 4, s));
-  for (auto& Ly : net) CK(cudaMemsetAsync(Ly.gb.p, 0, (size_t)Ly.out * 4, s));
+  float* loss = M.grads[e].p + M.grad_floats - 1;
+  CK(cudaMemsetAsync(M.grads[e].p, 0, M.grad_floats * 4, s));   // every gW, gb and the loss
   MlpLayer& top = net[L - 1];
-  CK(launch_grad_tile(0, W.out.p, W.t.p, nullptr, rows, M.cfg.n_out, W.dZ.p, W.dZh.p, W.dZht.p, top.gb.p,
-                      W.loss.p, s));
+  CK(launch_grad_tile(0, W.out.p, W.t.p, nullptr, rows, M.cfg.n_out, W.dZ.p, W.dZh.p, W.dZht.p, top.gb, loss, s));
   for (int l = (int)L - 1; l >= 0; l--) {
     MlpLayer& Ly = net[l];
     const uint16_t* xt = l == 0 ? W.xht.p : W.At[l - 1].p;
-    // dW = dZ^T . X  (reduction over the batch, split over grid z)
-    CK(cudaMemsetAsync(Ly.gW.p, 0, (size_t)Ly.out * Ly.in * 4, s));
+    // dW = dZ^T . X  (reduction over the batch, split over grid z; gW zeroed above)
     GemmArgs g{};
     g.A = W.dZht.p;
     g.a_rs = rows;
@@ -181,7 +184,7 @@ int32_t backward(omg_ctx* ctx, MlpRec& M, MlpBufs& W, uint32_t e, uint32_t rows,
     g.N = Ly.in;
     g.K = rows;
     g.n_tile = n_tile_of(Ly.in);
-    g.D = Ly.gW.p;
+    g.D = Ly.gW;
     g.ldd = Ly.in;
     g.accumulate = 1;
     g.err = M.err.p;
@@ -205,7 +208,7 @@ int32_t backward(omg_ctx* ctx, MlpRec& M, MlpBufs& W, uint32_t e, uint32_t rows,
     h.err = M.err.p;
     CK(launch_gemm(h, 1, s));
     CK(launch_grad_tile(1, W.dX.p, W.Z[l - 1].p, nullptr, rows, Ly.in, W.dZ.p, W.dZh.p, W.dZht.p,
-                        net[l - 1].gb.p, nullptr, s));
+                        net[l - 1].gb, nullptr, s));
   }
   return OMG_OK;
 }
@@ -274,11 +277,11 @@ int32_t omg_mlp_create(omg_ctx* ctx, const omg_mlp_config* cfg, uint32_t* id) {
       CK(Ly.Wht.alloc(nw));
       CK(Ly.mW.alloc(nw));
       CK(Ly.vW.alloc(nw));
-      CK(Ly.gW.alloc(nw));
+
       CK(Ly.b.alloc(Ly.out));
       CK(Ly.mb.alloc(Ly.out));
       CK(Ly.vb.alloc(Ly.out));
-      CK(Ly.gb.alloc(Ly.out));
+
       CK(cudaMemcpy(Ly.W.p, w.data(), nw * 4, cudaMemcpyHostToDevice));
       CK(cudaMemset(Ly.mW.p, 0, nw * 4));
       CK(cudaMemset(Ly.vW.p, 0, nw * 4));
@@ -287,6 +290,23 @@ int32_t omg_mlp_create(omg_ctx* ctx, const omg_mlp_config* cfg, uint32_t* id) {
       CK(cudaMemset(Ly.vb.p, 0, Ly.out * 4));
       CK(launch_to_bf16_t(Ly.W.p, Ly.out, Ly.in, Ly.Wh.p, Ly.Wht.p, ctx->stream));
       in = Ly.out;
+    }
+  }
+  // the gradient blocks: per member every layer's gW then gb, then the loss
+  {
+    uint64_t n = 1;
+    for (auto& Ly : M->members[0]) n += (uint64_t)Ly.out * Ly.in + Ly.out;
+    M->grad_floats = n;
+    M->grads.resize(cfg->members);
+    for (uint32_t e = 0; e < cfg->members; e++) {
+      CK(M->grads[e].alloc(n));
+      uint64_t off = 0;
+      for (auto& Ly : M->members[e]) {
+        Ly.gW = M->grads[e].p + off;
+        off += (uint64_t)Ly.out * Ly.in;
+        Ly.gb = M->grads[e].p + off;
+        off += Ly.out;
+      }
     }
   }
   M->x_mean.assign(cfg->n_in, 0.0f);
@@ -405,17 +425,22 @@ int32_t omg_mlp_train(omg_ctx* ctx, uint32_t id, const omg_mlp_train_config* tc,
     CK(cudaStreamSynchronize(s));
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     auto record = [&]() -> int32_t {
-      CK(launch_gather_step(M.X.p, M.cfg.n_in, T.perm.p, T.step.p, spe, B, nullptr, W.xh.p, W.xht.p, s));
-      CK(launch_gather_step(M.Y.p, M.cfg.n_out, T.perm.p, T.step.p, spe, B, W.t.p, nullptr, nullptr, s));
+      CK(launch_gather_pair(M.X.p, M.cfg.n_in, M.Y.p, M.cfg.n_out, T.perm.p, T.step.p, spe, B, W.xh.p, W.xht.p,
+                            W.t.p, s));
       int32_t r;
       if ((r = forward(ctx, M, W, e, B, true, s))) return r;
       if ((r = backward(ctx, M, W, e, B, s))) return r;
+      AdamwTable tab{};
+      uint64_t off = 0;
       for (uint32_t l = 0; l < L; l++) {
         MlpLayer& Ly = M.members[e][l];
-        CK(launch_adamw_layer(Ly.W.p, Ly.mW.p, Ly.vW.p, Ly.gW.p, Ly.Wh.p, Ly.Wht.p, Ly.in, Ly.out, Ly.b.p, Ly.mb.p,
-                              Ly.vb.p, Ly.gb.p, M.sched.p, T.step.p, tc->beta1, tc->beta2, tc->eps,
-                              tc->weight_decay, s));
+        tab.L[l] = AdamwLayer{Ly.W.p, Ly.mW.p, Ly.vW.p, Ly.b.p, Ly.mb.p, Ly.vb.p, Ly.gW, Ly.gb, Ly.Wh.p, Ly.Wht.p,
+                              Ly.in, Ly.out, off};
+        off += (uint64_t)Ly.in * Ly.out + Ly.out;
       }
+      tab.n = L;
+      tab.total = off;
+      CK(launch_adamw_all(tab, M.sched.p, T.step.p, tc->beta1, tc->beta2, tc->eps, tc->weight_decay, s));
       CK(launch_step(T.step.p, s));
       return OMG_OK;
     };
@@ -444,7 +469,7 @@ int32_t omg_mlp_train(omg_ctx* ctx, uint32_t id, const omg_mlp_train_config* tc,
       for (uint32_t e = 0; e < E; e++) CK(cudaGraphLaunch(M.trainers[e]->graph, M.trainers[e]->stream));
     for (uint32_t e = 0; e < E; e++) {
       MlpTrainer& T = *M.trainers[e];
-      CK(cudaMemcpyAsync(T.h_loss.p, T.bufs.loss.p, 4, cudaMemcpyDeviceToHost, T.stream));
+      CK(cudaMemcpyAsync(T.h_loss.p, M.grads[e].p + M.grad_floats - 1, 4, cudaMemcpyDeviceToHost, T.stream));
     }
     // the permutation buffers are refilled next epoch: wait for this one
     for (uint32_t e = 0; e < E; e++) {
@@ -548,13 +573,13 @@ int32_t omg_mlp_grad(omg_ctx* ctx, uint32_t id, uint32_t member, const float* x,
   CK(launch_to_bf16_t(xd.p, n, M.cfg.n_in, W.xh.p, W.xht.p, s));
   if ((rc = forward(ctx, M, W, member, n, true, s))) return rc;
   if ((rc = backward(ctx, M, W, member, n, s))) return rc;
-  CK(cudaMemcpyAsync(M.h_loss.p, W.loss.p, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(M.h_loss.p, M.grads[member].p + M.grad_floats - 1, 4, cudaMemcpyDeviceToHost, s));
   size_t off = 0;
   for (auto& Ly : M.members[member]) {
     if (grads) {
-      CK(cudaMemcpyAsync(grads + off, Ly.gW.p, (size_t)Ly.out * Ly.in * 4, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(grads + off, Ly.gW, (size_t)Ly.out * Ly.in * 4, cudaMemcpyDeviceToHost, s));
       off += (size_t)Ly.out * Ly.in;
-      CK(cudaMemcpyAsync(grads + off, Ly.gb.p, (size_t)Ly.out * 4, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(grads + off, Ly.gb, (size_t)Ly.out * 4, cudaMemcpyDeviceToHost, s));
       off += Ly.out;
     }
   }

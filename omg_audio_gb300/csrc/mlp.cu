@@ -1,17 +1,21 @@
 // The surrogate's dense layers on the tensor cores: a tcgen05 GEMM with the
-// accumulator in TMEM, fused bias + GELU epilogues, and the elementwise and
-// optimizer kernels of training (GELU backward, bias gradients, MSE loss,
-// AdamW on FP32 master weights with BF16 copies).
+// accumulator in TMEM and fused bias + GELU epilogues, and the elementwise and
+// optimizer kernels of training (loss and GELU gradients with fused bias
+// gradients, batch gathers, AdamW on FP32 master weights with BF16 copies).
 //
 // GEMM: D[M x N] = A[M x K] . B[N x K]^T with A, B in BF16 and FP32
-// accumulation. Operands are read through strides, so transposed operands of
-// the backward pass need no copies: element (m, k) of A is A[m a_rs + k a_ks].
-// One CTA of 128 threads computes a 128 x n_tile tile (n_tile <= 256): each
-// round stages a 64-wide K chunk of both operands into shared memory (K-major
-// core matrices, tc_gemm.cuh), one thread issues four K = 16 MMAs and commits
-// them to an mbarrier, and the CTA waits (bounded) before the next round. The
-// epilogue reads the accumulator lanes of each warp with tcgen05.ld. A grid z
-// dimension splits K; the split partials are added atomically.
+// accumulation. Operands are read through strides: element (m, k) of A is
+// A[m a_rs + k a_ks]. One CTA of 128 threads computes a 128 x n_tile tile
+// (n_tile <= 256) in 64-wide K chunks staged into shared memory as K-major
+// core matrices (tc_gemm.cuh); one thread issues four K = 16 MMAs per chunk
+// and commits them to an mbarrier (bounded waits). When both operands are
+// K-major and 16-byte aligned (every GEMM of training: the backward pass reads
+// transposed copies that the producing kernels write), the chunks are staged
+// by a three-deep cp.async pipeline, so the copies of the next chunks run
+// under the current MMAs; otherwise each chunk is staged by plain loads. The
+// epilogue reads the accumulator with tcgen05.ld and writes the row-major
+// outputs through shared memory, whole lines at a time. A grid z dimension
+// splits K; the split partials are added atomically.
 #include <algorithm>
 
 #include <cuda_bf16.h>
@@ -181,7 +185,10 @@ __global__ void __launch_bounds__(128, 1) gemm_kernel(GemmArgs g) {
     for (uint32_t i = 0; i < kStages; i++) tc::mbar_init(&mbar[i], 1);
     failed = 0;
   }
-  if (warp == 0) tc::tmem_alloc(&taddr_s, kMaxTileN);
+  // TMEM columns: the tile's width rounded up to a power of two (>= 32)
+  uint32_t tcols = 32u;
+  while (tcols < ((g.n_tile + 15u) & ~15u)) tcols <<= 1;
+  if (warp == 0) tc::tmem_alloc(&taddr_s, tcols);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -265,87 +272,7 @@ __global__ void __launch_bounds__(128, 1) gemm_kernel(GemmArgs g) {
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(taddr, kMaxTileN);
-}
-
-// dZ = dA * GELU'(Z) (f32 in, bf16 and f32 out)
-__global__ void gelu_back_kernel(const float* __restrict__ dA, const float* __restrict__ Z, float* __restrict__ dZ,
-                                 __nv_bfloat16* __restrict__ dZh, uint64_t n) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const float d = dA[i] * gelu_grad(Z[i]);
-    dZ[i] = d;
-    dZh[i] = __float2bfloat16_rn(d);
-  }
-}
-
-// column sums of X [rows x cols] (bias gradients); one thread per column
-__global__ void colsum_kernel(const float* __restrict__ X, uint32_t rows, uint32_t cols, float* __restrict__ out) {
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cols) return;
-  float s = 0.0f;
-  for (uint32_t r = 0; r < rows; r++) s += X[(uint64_t)r * cols + c];
-  out[c] = s;
-}
-
-// MSE over [rows x cols] with a per-column weight: dY = 2 w (Y - T) / (rows cols),
-// bf16 copy of dY for the GEMMs, per-block partial losses
-__global__ void mse_kernel(const float* __restrict__ Y, const float* __restrict__ T, const float* __restrict__ w,
-                           uint32_t rows, uint32_t cols, float* __restrict__ dY, __nv_bfloat16* __restrict__ dYh,
-                           float* __restrict__ loss_parts) {
-  __shared__ float red[256];
-  const uint64_t n = (uint64_t)rows * cols;
-  const float scale = 2.0f / (float)n;
-  float acc = 0.0f;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const float wc = w ? w[i % cols] : 1.0f;
-    const float e = Y[i] - T[i];
-    acc += wc * e * e;
-    const float d = scale * wc * e;
-    dY[i] = d;
-    dYh[i] = __float2bfloat16_rn(d);
-  }
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (uint32_t s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) loss_parts[blockIdx.x] = red[0] / (float)n;
-}
-
-// AdamW on FP32 master weights; writes the BF16 copy used by the GEMMs.
-__global__ void adamw_kernel(float* __restrict__ W, float* __restrict__ m, float* __restrict__ v,
-                             const float* __restrict__ g, __nv_bfloat16* __restrict__ Wh, uint64_t n, float lr,
-                             float b1, float b2, float eps, float wd, float bc1, float bc2) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const float gi = g[i];
-    const float mi = b1 * m[i] + (1.0f - b1) * gi;
-    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
-    m[i] = mi;
-    v[i] = vi;
-    const float mh = mi / bc1, vh = vi / bc2;
-    float w = W[i];
-    w = w - lr * (mh / (sqrtf(vh) + eps) + wd * w);
-    W[i] = w;
-    if (Wh) Wh[i] = __float2bfloat16_rn(w);
-  }
-}
-
-__global__ void to_bf16_kernel(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, uint64_t n) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-    y[i] = __float2bfloat16_rn(x[i]);
-}
-
-// out[r] = X[idx[r]] (row gather of a [n x cols] f32 matrix), optional bf16 copy
-__global__ void gather_rows_kernel(const float* __restrict__ X, uint32_t cols, const uint32_t* __restrict__ idx,
-                                   uint32_t rows, float* __restrict__ out, __nv_bfloat16* __restrict__ out_h) {
-  const uint64_t n = (uint64_t)rows * cols;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t r = (uint32_t)(i / cols), c = (uint32_t)(i % cols);
-    const float v = X[(uint64_t)idx[r] * cols + c];
-    if (out) out[i] = v;
-    if (out_h) out_h[i] = __float2bfloat16_rn(v);
-  }
+  if (warp == 0) tc::tmem_dealloc(taddr, tcols);
 }
 
 // (x - mean) / std per column, to bf16 (inference inputs)
@@ -457,27 +384,29 @@ __global__ void grad_tile_kernel(uint32_t mode, const float* __restrict__ P, con
   }
 }
 
-// AdamW on one layer's FP32 master weights W [out x in] and biases b [out]
-// (no weight decay on biases), learning rate and bias corrections of step
-// *step from sched (3 floats a step); writes the bf16 copy Wh and its
-// transpose Wht [in x out].
-__global__ void adamw_layer_kernel(float* __restrict__ W, float* __restrict__ mW, float* __restrict__ vW,
-                                   const float* __restrict__ gW, __nv_bfloat16* __restrict__ Wh,
-                                   __nv_bfloat16* __restrict__ Wht, uint32_t in, uint32_t out, float* __restrict__ b,
-                                   float* __restrict__ mb, float* __restrict__ vb, const float* __restrict__ gb,
-                                   const float* __restrict__ sched, const uint32_t* __restrict__ step, float b1,
-                                   float b2, float eps, float wd) {
+__global__ void step_kernel(uint32_t* step) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1u;
+}
+
+// AdamW of every layer of one member in one launch (layer table by value);
+// otherwise as adamw_layer_kernel.
+__global__ void adamw_all_kernel(AdamwTable tab, const float* __restrict__ sched, const uint32_t* __restrict__ step,
+                                 float b1, float b2, float eps, float wd) {
   const uint32_t t = *step;
   const float lr = sched[3u * t], bc1 = sched[3u * t + 1u], bc2 = sched[3u * t + 2u];
-  const uint64_t nw = (uint64_t)in * out, n = nw + out;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+  for (uint64_t gi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; gi < tab.total;
+       gi += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t l = 0;
+    while (l + 1 < tab.n && gi >= tab.L[l + 1].off) l++;
+    const AdamwLayer& Y = tab.L[l];
+    const uint64_t i = gi - Y.off, nw = (uint64_t)Y.in * Y.out;
     const bool isw = i < nw;
-    float* P = isw ? W + i : b + (i - nw);
-    float* M1 = isw ? mW + i : mb + (i - nw);
-    float* V1 = isw ? vW + i : vb + (i - nw);
-    const float gi = isw ? gW[i] : gb[i - nw];
-    const float mi = b1 * *M1 + (1.0f - b1) * gi;
-    const float vi = b2 * *V1 + (1.0f - b2) * gi * gi;
+    float* P = isw ? Y.W + i : Y.b + (i - nw);
+    float* M1 = isw ? Y.mW + i : Y.mb + (i - nw);
+    float* V1 = isw ? Y.vW + i : Y.vb + (i - nw);
+    const float g = isw ? Y.gW[i] : Y.gb[i - nw];
+    const float mi = b1 * *M1 + (1.0f - b1) * g;
+    const float vi = b2 * *V1 + (1.0f - b2) * g * g;
     *M1 = mi;
     *V1 = vi;
     const float mh = mi / bc1, vh = vi / bc2;
@@ -486,31 +415,35 @@ __global__ void adamw_layer_kernel(float* __restrict__ W, float* __restrict__ mW
     *P = x;
     if (isw) {
       const __nv_bfloat16 h = __float2bfloat16_rn(x);
-      Wh[i] = h;
-      const uint32_t o = (uint32_t)(i / in), k = (uint32_t)(i % in);
-      Wht[(uint64_t)k * out + o] = h;
+      static_cast<__nv_bfloat16*>(Y.Wh)[i] = h;
+      const uint32_t o = (uint32_t)(i / Y.in), k = (uint32_t)(i % Y.in);
+      static_cast<__nv_bfloat16*>(Y.Wht)[(uint64_t)k * Y.out + o] = h;
     }
   }
 }
 
-__global__ void step_kernel(uint32_t* step) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1u;
-}
-
-// Rows of this step's batch: out[r] = X[perm[((*step) mod spe) B + r]] (f32,
-// optional), its bf16 copy (optional) and bf16 transpose [cols x rows] (optional).
-__global__ void gather_step_kernel(const float* __restrict__ X, uint32_t cols, const uint32_t* __restrict__ perm,
+// This step's batch rows of the inputs (blockIdx.y 0: bf16 copy and
+// transpose) and of the targets (blockIdx.y 1: f32), as gather_step_kernel.
+__global__ void gather_pair_kernel(const float* __restrict__ X, uint32_t xcols, const float* __restrict__ Y,
+                                   uint32_t ycols, const uint32_t* __restrict__ perm,
                                    const uint32_t* __restrict__ step, uint32_t spe, uint32_t rows,
-                                   float* __restrict__ out, __nv_bfloat16* __restrict__ out_h,
-                                   __nv_bfloat16* __restrict__ out_ht) {
+                                   __nv_bfloat16* __restrict__ xh, __nv_bfloat16* __restrict__ xht,
+                                   float* __restrict__ t) {
   const uint32_t* idx = perm + (uint64_t)((*step) % spe) * rows;
+  const bool isx = blockIdx.y == 0;
+  const uint32_t cols = isx ? xcols : ycols;
+  const float* S = isx ? X : Y;
   const uint64_t n = (uint64_t)rows * cols;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t r = (uint32_t)(i / cols), c = (uint32_t)(i % cols);
-    const float v = X[(uint64_t)idx[r] * cols + c];
-    if (out) out[i] = v;
-    if (out_h) out_h[i] = __float2bfloat16_rn(v);
-    if (out_ht) out_ht[(uint64_t)c * rows + r] = __float2bfloat16_rn(v);
+    const float v = S[(uint64_t)idx[r] * cols + c];
+    if (isx) {
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      xh[i] = h;
+      xht[(uint64_t)c * rows + r] = h;
+    } else {
+      t[i] = v;
+    }
   }
 }
 
@@ -595,32 +528,6 @@ cudaError_t launch_gemm(const GemmArgs& g, uint32_t k_split, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_gelu_back(const float* dA, const float* Z, float* dZ, void* dZh, uint64_t n, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  gelu_back_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
-      dA, Z, dZ, static_cast<__nv_bfloat16*>(dZh), n);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_colsum(const float* X, uint32_t rows, uint32_t cols, float* out, cudaStream_t s) {
-  colsum_kernel<<<(cols + 127) / 128, 128, 0, s>>>(X, rows, cols, out);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_mse(const float* Y, const float* T, const float* w, uint32_t rows, uint32_t cols, float* dY,
-                       void* dYh, float* loss_parts, uint32_t n_parts, cudaStream_t s) {
-  mse_kernel<<<n_parts, 256, 0, s>>>(Y, T, w, rows, cols, dY, static_cast<__nv_bfloat16*>(dYh), loss_parts);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_adamw(float* W, float* m, float* v, const float* g, void* Wh, uint64_t n, float lr, float b1,
-                         float b2, float eps, float wd, float bc1, float bc2, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  adamw_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
-      W, m, v, g, static_cast<__nv_bfloat16*>(Wh), n, lr, b1, b2, eps, wd, bc1, bc2);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_grad_tile(uint32_t mode, const float* P, const float* Q, const float* w, uint32_t rows,
                              uint32_t cols, float* dZ, void* dZh, void* dZht, float* gb, float* loss,
                              cudaStream_t s) {
@@ -630,13 +537,21 @@ cudaError_t launch_grad_tile(uint32_t mode, const float* P, const float* Q, cons
   return cudaGetLastError();
 }
 
-cudaError_t launch_adamw_layer(float* W, float* mW, float* vW, const float* gW, void* Wh, void* Wht, uint32_t in,
-                               uint32_t out, float* b, float* mb, float* vb, const float* gb, const float* sched,
-                               const uint32_t* step, float b1, float b2, float eps, float wd, cudaStream_t s) {
-  const uint64_t n = (uint64_t)in * out + out;
-  adamw_layer_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 1024), 256, 0, s>>>(
-      W, mW, vW, gW, static_cast<__nv_bfloat16*>(Wh), static_cast<__nv_bfloat16*>(Wht), in, out, b, mb, vb, gb,
-      sched, step, b1, b2, eps, wd);
+cudaError_t launch_adamw_all(const AdamwTable& tab, const float* sched, const uint32_t* step, float b1, float b2,
+                             float eps, float wd, cudaStream_t s) {
+  if (tab.total == 0) return cudaSuccess;
+  adamw_all_kernel<<<(uint32_t)std::min<uint64_t>((tab.total + 255) / 256, 1024), 256, 0, s>>>(tab, sched, step, b1,
+                                                                                              b2, eps, wd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_pair(const float* X, uint32_t xcols, const float* Y, uint32_t ycols, const uint32_t* perm,
+                               const uint32_t* step, uint32_t spe, uint32_t rows, void* xh, void* xht, float* t,
+                               cudaStream_t s) {
+  const uint64_t n = (uint64_t)rows * std::max(xcols, ycols);
+  dim3 grid((uint32_t)std::min<uint64_t>((n + 255) / 256, 1024), 2);
+  gather_pair_kernel<<<grid, 256, 0, s>>>(X, xcols, Y, ycols, perm, step, spe, rows,
+                                          static_cast<__nv_bfloat16*>(xh), static_cast<__nv_bfloat16*>(xht), t);
   return cudaGetLastError();
 }
 
@@ -645,35 +560,11 @@ cudaError_t launch_step(uint32_t* step, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_gather_step(const float* X, uint32_t cols, const uint32_t* perm, const uint32_t* step,
-                               uint32_t spe, uint32_t rows, float* out, void* out_h, void* out_ht, cudaStream_t s) {
-  const uint64_t n = (uint64_t)rows * cols;
-  gather_step_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 2048), 256, 0, s>>>(
-      X, cols, perm, step, spe, rows, out, static_cast<__nv_bfloat16*>(out_h), static_cast<__nv_bfloat16*>(out_ht));
-  return cudaGetLastError();
-}
-
 cudaError_t launch_to_bf16_t(const float* x, uint32_t rows, uint32_t cols, void* xh, void* xht, cudaStream_t s) {
   const uint64_t n = (uint64_t)rows * cols;
   if (n == 0) return cudaSuccess;
   to_bf16_t_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 2048), 256, 0, s>>>(
       x, rows, cols, static_cast<__nv_bfloat16*>(xh), static_cast<__nv_bfloat16*>(xht));
-  return cudaGetLastError();
-}
-
-cudaError_t launch_to_bf16(const float* x, void* y, uint64_t n, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  to_bf16_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
-      x, static_cast<__nv_bfloat16*>(y), n);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_gather_rows(const float* X, uint32_t cols, const uint32_t* idx, uint32_t rows, float* out,
-                               void* out_bf16, cudaStream_t s) {
-  if (rows == 0) return cudaSuccess;
-  const uint64_t n = (uint64_t)rows * cols;
-  gather_rows_kernel<<<(uint32_t)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
-      X, cols, idx, rows, out, static_cast<__nv_bfloat16*>(out_bf16));
   return cudaGetLastError();
 }
 

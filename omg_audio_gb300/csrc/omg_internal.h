@@ -334,30 +334,34 @@ struct GemmArgs {
 size_t gemm_smem_bytes();
 cudaError_t gemm_init();
 cudaError_t launch_gemm(const GemmArgs& g, uint32_t k_split, cudaStream_t s);
-cudaError_t launch_gelu_back(const float* dA, const float* Z, float* dZ, void* dZh, uint64_t n, cudaStream_t s);
-cudaError_t launch_colsum(const float* X, uint32_t rows, uint32_t cols, float* out, cudaStream_t s);
-cudaError_t launch_mse(const float* Y, const float* T, const float* w, uint32_t rows, uint32_t cols, float* dY,
-                       void* dYh, float* loss_parts, uint32_t n_parts, cudaStream_t s);
-cudaError_t launch_adamw(float* W, float* m, float* v, const float* g, void* Wh, uint64_t n, float lr, float b1,
-                         float b2, float eps, float wd, float bc1, float bc2, cudaStream_t s);
-cudaError_t launch_to_bf16(const float* x, void* y, uint64_t n, cudaStream_t s);
 // backward elementwise on 32 x 32 tiles: mode 0 the MSE loss gradient of
 // P = outputs against Q = targets (weights w per column, nullable; loss +=),
 // mode 1 dZ = P (dA) * GELU'(Q (Z)); writes dZ, its bf16 copy and transpose,
 // and adds the column sums into gb (zeroed by the caller)
 cudaError_t launch_grad_tile(uint32_t mode, const float* P, const float* Q, const float* w, uint32_t rows,
                              uint32_t cols, float* dZ, void* dZh, void* dZht, float* gb, float* loss, cudaStream_t s);
-// AdamW of one layer (W [out x in] with bf16 copy and transpose, b [out]); the
-// step's learning rate and bias corrections at sched[3 *step]
-cudaError_t launch_adamw_layer(float* W, float* mW, float* vW, const float* gW, void* Wh, void* Wht, uint32_t in,
-                               uint32_t out, float* b, float* mb, float* vb, const float* gb, const float* sched,
-                               const uint32_t* step, float b1, float b2, float eps, float wd, cudaStream_t s);
+// AdamW of every layer of one ensemble member in one launch
+struct AdamwLayer {
+  float *W, *mW, *vW, *b, *mb, *vb;
+  const float *gW, *gb;
+  void *Wh, *Wht;
+  uint32_t in, out;
+  uint64_t off;             // first element of this layer in the launch's index space (W then b)
+};
+constexpr int kMaxAdamwLayers = 17;
+struct AdamwTable {
+  AdamwLayer L[kMaxAdamwLayers];
+  uint32_t n;
+  uint64_t total;
+};
+cudaError_t launch_adamw_all(const AdamwTable& tab, const float* sched, const uint32_t* step, float b1, float b2,
+                             float eps, float wd, cudaStream_t s);
+// inputs (bf16 copy + transpose) and targets (f32) of this step's batch rows
+cudaError_t launch_gather_pair(const float* X, uint32_t xcols, const float* Y, uint32_t ycols, const uint32_t* perm,
+                               const uint32_t* step, uint32_t spe, uint32_t rows, void* xh, void* xht, float* t,
+                               cudaStream_t s);
 cudaError_t launch_step(uint32_t* step, cudaStream_t s);
-cudaError_t launch_gather_step(const float* X, uint32_t cols, const uint32_t* perm, const uint32_t* step,
-                               uint32_t spe, uint32_t rows, float* out, void* out_h, void* out_ht, cudaStream_t s);
 cudaError_t launch_to_bf16_t(const float* x, uint32_t rows, uint32_t cols, void* xh, void* xht, cudaStream_t s);
-cudaError_t launch_gather_rows(const float* X, uint32_t cols, const uint32_t* idx, uint32_t rows, float* out,
-                               void* out_bf16, cudaStream_t s);
 cudaError_t launch_standardize(const float* x, const float* mean, const float* sd, uint32_t cols, uint64_t n,
                                void* out, cudaStream_t s);
 cudaError_t launch_ensemble(const float* y, const float* mean, const float* sd, uint32_t cols, uint64_t n,

@@ -455,7 +455,11 @@ __device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, f
 // runs the survivors in full warps. An epoch whose park signal is never
 // raised (it ended too few rays while rays were still queued) runs its rays
 // to their end, which is only slower.
-template <int NB, bool TIE>
+//
+// WIDE (near-tie rule only): walks on the 4-wide tree. A template parameter,
+// not a runtime flag, so that each variant carries only its own walk: the
+// loop body is then small enough for the instruction cache.
+template <int NB, bool TIE, bool WIDE>
 __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
                                                        uint32_t total_rays, const DScene* __restrict__ scenes,
                                                        const DMat* __restrict__ job_mats,
@@ -463,7 +467,8 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
                                                        const DPanelGroup* __restrict__ groups, float* __restrict__ acc,
                                                     DLaunch* __restrict__ hdr, uint32_t* __restrict__ job_segments,
                                                     uint32_t refill_min, int walk_budget, uint32_t shade_min,
-                                                    bool wide, EpochArgs ea) {
+                                                    EpochArgs ea) {
+  constexpr bool wide = TIE && WIDE;
   const unsigned FULL = 0xffffffffu;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt_mask = (1u << lane) - 1u;
@@ -909,9 +914,14 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
   if (wl)                                                                                                      \
     trace_wl_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels,    \
                                                         groups, acc, hdr, job_segments, steps, wl_shade, wide, ea);  \
+  else if (TIE && wide)                                                                                        \
+    trace_kernel<NB, TIE, true><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels,  \
+                                                           groups, acc, hdr, job_segments, refill, steps,        \
+                                                           shade_min, ea);                                       \
   else                                                                                                         \
-    trace_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, groups, \
-                                                     acc, hdr, job_segments, refill, steps, shade_min, wide, ea)
+    trace_kernel<NB, TIE, false><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, \
+                                                            groups, acc, hdr, job_segments, refill, steps,       \
+                                                            shade_min, ea)
   if (max_nb <= 3) {
     if (tie) OMG_TRACE_LAUNCH(3, true);
     else OMG_TRACE_LAUNCH(3, false);
@@ -926,10 +936,10 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
 cudaError_t preload_trace_kernels() {
   cudaFuncAttributes fa;
   cudaError_t e;
-  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<3, false>)) != cudaSuccess) return e;
-  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<3, true>)) != cudaSuccess) return e;
-  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<8, false>)) != cudaSuccess) return e;
-  return cudaFuncGetAttributes(&fa, trace_kernel<8, true>);
+  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<3, false, false>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<3, true, false>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<8, false, false>)) != cudaSuccess) return e;
+  return cudaFuncGetAttributes(&fa, trace_kernel<8, true, false>);
 }
 
 cudaError_t launch_finalize(const DJob* jobs, uint32_t n_jobs, const float* acc, float* out, uint64_t total_out,
