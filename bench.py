@@ -329,8 +329,9 @@ def surrogate_leg(args, device, city=None):
     n_floor = min(n, args.surrogate_floor_rooms)
     sub = test.take(np.arange(n_floor))
     rt_b = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, sub, 4096, seed=8)[0], 0.001))
-    rt_c = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, sub, 65536, seed=9)[0], 0.001))
-    rt_d = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, sub, 65536, seed=10)[0], 0.001))
+    jr = args.surrogate_judge_rays
+    rt_c = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, sub, jr, seed=9)[0], 0.001))
+    rt_d = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, sub, jr, seed=10)[0], 0.001))
     nz_seed = np.abs(rt_b / rt_t[:n_floor] - 1.0)
     nz_65k = np.abs(rt_t[:n_floor] / rt_c - 1.0)
     nz_65k_65k = np.abs(rt_d / rt_c - 1.0)
@@ -339,8 +340,8 @@ def surrogate_leg(args, device, city=None):
     def q(a, p):
         return float(np.nanpercentile(a, p))
 
-    # the spread gate swept on the noise-floor rooms, judged by the 65,536-ray
-    # tracer (the 4096-ray tracer's own p90 error is above 5 %): answered = in
+    # the spread gate swept on the noise-floor rooms, judged by the tracer at
+    # jr rays (the 4096-ray tracer's own p90 error is above 5 %): answered = in
     # the family and spread <= threshold; the rest fall back to the tracer
     inr = S.in_range(S.features(test))[:n_floor]
     spr = spread[:n_floor]
@@ -405,11 +406,12 @@ def surrogate_leg(args, device, city=None):
         "judge_noise_floor": {
             "rooms": n_floor,
             "tracer_4096_vs_4096_other_seed": {"median": q(nz_seed, 50), "p90": q(nz_seed, 90)},
-            "tracer_4096_vs_65536": {"median": q(nz_65k, 50), "p90": q(nz_65k, 90)},
-            "tracer_65536_vs_65536_other_seed": {"median": q(nz_65k_65k, 50), "p90": q(nz_65k_65k, 90)},
-            "surrogate_vs_65536": {"median": q(sur_65k, 50), "p90": q(sur_65k, 90)}},
+            "judge_rays": jr,
+            "tracer_4096_vs_judge": {"median": q(nz_65k, 50), "p90": q(nz_65k, 90)},
+            "judge_vs_judge_other_seed": {"median": q(nz_65k_65k, 50), "p90": q(nz_65k_65k, 90)},
+            "surrogate_vs_judge": {"median": q(sur_65k, 50), "p90": q(sur_65k, 90)}},
         "spread_gate_sweep": sweep,
-        "spread_gate_judge": f"the tracer at 65,536 rays on the first {n_floor} test rooms",
+        "spread_gate_judge": f"the tracer at {jr} rays on the first {n_floor} test rooms",
         "chosen_gate": chosen,
         "p90_target_met": chosen is not None,
         "city_pairs": city_leg,
@@ -873,8 +875,10 @@ def main():
     ap.add_argument("--surrogate-test", type=int, default=16384, help="held-out rooms")
     ap.add_argument("--surrogate-train-rays", type=int, default=8192,
                     help="tracer rays per training room (the labels' Monte-Carlo noise is the loss floor)")
-    ap.add_argument("--surrogate-floor-rooms", type=int, default=2048,
-                    help="test rooms traced again (another seed; 65,536 rays) for the judge's noise floor")
+    ap.add_argument("--surrogate-floor-rooms", type=int, default=1024,
+                    help="test rooms traced again (another seed; --surrogate-judge-rays) for the judge's noise floor")
+    ap.add_argument("--surrogate-judge-rays", type=int, default=131072,
+                    help="rays of the low-noise judge the spread gate is swept against")
     ap.add_argument("--max-bounces", type=int, default=0,
                     help="profiling variant: cap the bounces (0: the workload's 200)")
     ap.add_argument("--shape", default="",
