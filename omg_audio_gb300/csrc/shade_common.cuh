@@ -28,8 +28,9 @@ struct Hit {
   const DMat* m;
 };
 
-// scene.rs:39-88 — analytic shoebox.
-__device__ __forceinline__ bool box_hit(const DJob& J, const DMat* __restrict__ job_mats, float px, float py,
+// scene.rs:39-88 — analytic shoebox. (Out of line: only shoebox jobs take it,
+// and the persistent kernels' loop stays small for the instruction cache.)
+static __device__ __noinline__ bool box_hit(const DJob& J, const DMat* __restrict__ job_mats, float px, float py,
                                         float pz, float dx, float dy, float dz, Hit& h) {
   if (!(px > 0.0f && px < J.box[0] && py > 0.0f && py < J.box[1] && pz > 0.0f && pz < J.box[2])) return false;
   float bt = FLT_MAX;
@@ -140,6 +141,34 @@ __device__ __forceinline__ uint32_t find_job(const DJob* __restrict__ jobs, uint
 }
 
 
+template <int NB>
+struct Bands {
+  float v[NB];
+};
+
+// The receiver sphere's crossing into the compensated histograms: bin `bin`
+// gets every band's energy and the direction row -d e_mid (tracer.rs:118-126).
+// Out of line: it runs for a few segments in a thousand.
+template <int NB>
+static __device__ __noinline__ void record_arrival(const DJob& J, float* __restrict__ acc, uint32_t bin, Bands<NB> e,
+                                            float dx, float dy, float dz) {
+  const uint32_t nb = J.nb;
+  float* A = acc + J.acc_off;
+  const uint32_t nbb = J.n_bins * nb;
+#pragma unroll
+  for (int b = 0; b < NB; b++)
+    if ((uint32_t)b < nb) acc_add(A + bin * nb + b, A + nbb + bin * nb + b, e.v[b]);
+  float em = e.v[0];
+#pragma unroll
+  for (int b = 1; b < NB; b++)
+    if ((uint32_t)b == J.dir_band) em = e.v[b];
+  float* D = A + 2 * nbb;
+  const uint32_t nd = J.n_bins * 3;
+  acc_add(D + bin * 3 + 0, D + nd + bin * 3 + 0, -(dx * em));
+  acc_add(D + bin * 3 + 1, D + nd + bin * 3 + 1, -(dy * em));
+  acc_add(D + bin * 3 + 2, D + nd + bin * 3 + 2, -(dz * em));
+}
+
 // One segment after its closest hit (tracer.rs:110-200): the receiver test with
 // compensated histogram adds, then advance, absorb, transmit or scatter.
 // Returns true when the ray ends here.
@@ -159,21 +188,10 @@ __device__ __forceinline__ bool shade_segment(const DJob& J, float* __restrict__
         const float arrival = (dist + s) / J.c;
         const float q = arrival / J.bin_dt;
         if (q < (float)J.n_bins) {          // (q as usize) < NBINS, q >= 0
-          const uint32_t bin = (uint32_t)q;
-          float* A = acc + J.acc_off;
-          const uint32_t nbb = J.n_bins * nb;
+          Bands<NB> eb;
 #pragma unroll
-          for (int b = 0; b < NB; b++)
-            if ((uint32_t)b < nb) acc_add(A + bin * nb + b, A + nbb + bin * nb + b, e[b]);
-          float em = e[0];
-#pragma unroll
-          for (int b = 1; b < NB; b++)
-            if ((uint32_t)b == J.dir_band) em = e[b];
-          float* D = A + 2 * nbb;
-          const uint32_t nd = J.n_bins * 3;
-          acc_add(D + bin * 3 + 0, D + nd + bin * 3 + 0, -(dx * em));
-          acc_add(D + bin * 3 + 1, D + nd + bin * 3 + 1, -(dy * em));
-          acc_add(D + bin * 3 + 2, D + nd + bin * 3 + 2, -(dz * em));
+          for (int b = 0; b < NB; b++) eb.v[b] = e[b];
+          record_arrival<NB>(J, acc, (uint32_t)q, eb, dx, dy, dz);
         }
       }
     }

@@ -439,6 +439,45 @@ __device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, f
   return walk_spec(w, S, ox, oy, oz, dx, dy, dz, steps, err);
 }
 
+// A ray parked between two segments: its state into the per-ray records, for
+// the next epoch to restore. (Out of line, as the epoch bookkeeping below: a
+// single-launch trace never runs them, and the persistent loop stays small
+// enough for the instruction cache.)
+template <int NB>
+__device__ __noinline__ void park_ray(const WfState& rs, uint32_t rid, float px, float py, float pz, float dist,
+                                      float dx, float dy, float dz, uint32_t rng_s, Bands<NB> e, uint32_t bounce) {
+  rs.pos[rid] = make_float4(px, py, pz, dist);
+  rs.dir[rid] = make_float4(dx, dy, dz, __uint_as_float(rng_s));
+  float v[8];
+#pragma unroll
+  for (int b = 0; b < 8; b++) v[b] = b < NB ? e.v[b] : 0.0f;
+  rs.e[rid] = make_float4(v[0], v[1], v[2], v[3]);
+  if (NB > 4) rs.e[rs.cap + rid] = make_float4(v[4], v[5], v[6], v[7]);
+  rs.bounce[rid] = bounce;
+}
+
+// An epoch's per-iteration bookkeeping, warp-aggregated (every lane calls it):
+// count the ended rays (and raise the park signal once at most `keep` remain
+// and the queue is drained), append the parked ones to the next epoch's queue.
+__device__ __noinline__ void epoch_tally(const EpochArgs& ea, bool ended, bool parked, uint32_t rid, bool may_park,
+                                         uint32_t n_rays, uint32_t keep, const uint32_t* fetch) {
+  const unsigned FULL = 0xffffffffu;
+  const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
+  const unsigned em = __ballot_sync(FULL, ended);
+  if (em && lane == (uint32_t)(__ffs(em) - 1)) {
+    const uint32_t done_now = atomicAdd(&ea.cur->ended, (uint32_t)__popc(em)) + (uint32_t)__popc(em);
+    if (may_park && n_rays - done_now <= keep && *((volatile const uint32_t*)fetch) >= n_rays)
+      *((volatile uint32_t*)&ea.cur->park) = 1u;
+  }
+  const unsigned pm = __ballot_sync(FULL, parked);
+  if (pm) {
+    uint32_t base = 0;
+    if (lane == (uint32_t)(__ffs(pm) - 1)) base = atomicAdd(&ea.next->n, (uint32_t)__popc(pm));
+    base = __shfl_sync(FULL, base, __ffs(pm) - 1);
+    if (parked) ea.out_q[base + (uint32_t)__popc(pm & lt_mask)] = rid;
+  }
+}
+
 // The tracer. Each lane runs a small state machine so that a lane whose
 // closest-hit walk ends shades its segment and starts the next one at once,
 // while the other lanes of its warp keep walking: per loop iteration a lane
@@ -635,37 +674,17 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
         ended = true;
       } else if (parking) {
         // save the ray between two segments; the next epoch restores it
-        rs.pos[rid] = make_float4(px, py, pz, dist);
-        rs.dir[rid] = make_float4(dx, dy, dz, __uint_as_float(rng.s));
-        float v[8];
+        Bands<NB> eb;
 #pragma unroll
-        for (int b = 0; b < 8; b++) v[b] = b < NB ? e[b] : 0.0f;
-        rs.e[rid] = make_float4(v[0], v[1], v[2], v[3]);
-        if (NB > 4) rs.e[rs.cap + rid] = make_float4(v[4], v[5], v[6], v[7]);
-        rs.bounce[rid] = bounce;
+        for (int b = 0; b < NB; b++) eb.v[b] = e[b];
+        park_ray<NB>(rs, rid, px, py, pz, dist, dx, dy, dz, rng.s, eb, bounce);
         phase = IDLE;
         parked = true;
       } else {
         begin_segment(J);
       }
     }
-    if (ea.cur) {
-      // warp-aggregated: count the ended rays (and raise the park signal),
-      // append the parked ones to the next epoch's queue
-      const unsigned em = __ballot_sync(FULL, ended);
-      if (em && lane == (uint32_t)(__ffs(em) - 1)) {
-        const uint32_t done_now = atomicAdd(&ea.cur->ended, (uint32_t)__popc(em)) + (uint32_t)__popc(em);
-        if (may_park && n_rays - done_now <= keep && *((volatile const uint32_t*)fetch) >= n_rays)
-          *((volatile uint32_t*)&ea.cur->park) = 1u;
-      }
-      const unsigned pm = __ballot_sync(FULL, parked);
-      if (pm) {
-        uint32_t base = 0;
-        if (lane == (uint32_t)(__ffs(pm) - 1)) base = atomicAdd(&ea.next->n, (uint32_t)__popc(pm));
-        base = __shfl_sync(FULL, base, __ffs(pm) - 1);
-        if (parked) ea.out_q[base + (uint32_t)__popc(pm & lt_mask)] = rid;
-      }
-    }
+    if (ea.cur) epoch_tally(ea, ended, parked, rid, may_park, n_rays, keep, fetch);
   }
 }
 
