@@ -362,13 +362,17 @@ def surrogate_leg(args, device, city=None):
     city_leg = None
     if city is not None:
         # config 5's room/source pairs: every building x every source
-        gate = chosen["spread_db_max"] if chosen else sur.threshold_db
+        # the product's gate (RoomSurrogate.threshold_db), or the sweep's
+        # stricter one: these rooms are not the test family's
+        gate = sur.threshold_db
+        if chosen and chosen["spread_db_max"] is not None:
+            gate = min(gate, chosen["spread_db_max"])
         rooms = S.city_rooms(city.buildings, city.sources, city.absorption, city.window_frac)
         sur.predict(rooms.take(np.arange(64)))
         t0 = time.perf_counter()
         cedc, cspread, cok = sur.predict(rooms)
         t_cp = time.perf_counter() - t0
-        ans = S.in_range(S.features(rooms)) & (cspread <= (gate if gate is not None else np.inf))
+        ans = S.in_range(S.features(rooms)) & (cspread <= gate)
         fb = np.nonzero(~ans)[0]
         t0 = time.perf_counter()
         if len(fb):
