@@ -53,12 +53,22 @@ __global__ void reverb_kernel(const DReverbJob* __restrict__ rj, uint32_t n_jobs
 
   float rt60 = 0.5f, fit = 0.5f;
   if (total > 0.0) {
-    // first bins at <= -5 dB and <= -25 dB (EDC is non-increasing)
+    // first bins at <= -5 dB and <= -25 dB. The EDC is non-increasing, so each
+    // lane stops at its first bin past both levels. The dB value is computed
+    // only for a bin within 1e-9 (relative) of a level's energy: elsewhere the
+    // energy ratio decides the same comparison, without a logarithm per bin.
+    const double r5 = sqrt(0.1);            // 10^(-5/10)
+    const double e5 = total * r5, e25 = total * (r5 * 0.01);
+    auto below = [&](double e, double level, double thr) {
+      if (e < thr * (1.0 - 1e-9)) return true;
+      if (e > thr * (1.0 + 1e-9)) return false;
+      return db_of(e, total) <= level;
+    };
     uint32_t f5 = 0xFFFFFFFFu, f25 = 0xFFFFFFFFu;
-    for (uint32_t i = lane; i < n; i += 32) {
-      double d = db_of(edc[i], total);
-      if (d <= -5.0 && f5 == 0xFFFFFFFFu) f5 = i;
-      if (d <= -25.0 && f25 == 0xFFFFFFFFu) f25 = i;
+    for (uint32_t i = lane; i < n && f25 == 0xFFFFFFFFu; i += 32) {
+      const double e = edc[i];
+      if (f5 == 0xFFFFFFFFu && below(e, -5.0, e5)) f5 = i;
+      if (below(e, -25.0, e25)) f25 = i;
     }
     for (int off = 16; off > 0; off >>= 1) {
       f5 = min(f5, __shfl_xor_sync(0xffffffffu, f5, off));
