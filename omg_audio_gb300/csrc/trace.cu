@@ -337,6 +337,7 @@ __device__ __forceinline__ void coop_leaf_rounds(Walk& w, bool own_walk, const f
     }
     const uint32_t total = __shfl_sync(FULL, inc, 31);
     const uint32_t excl = inc - cnt;
+    const uint32_t kmax = __reduce_max_sync(FULL, cnt);
     for (uint32_t k = 0; k < cnt; k++) slots[excl + k] = (uint8_t)lane;
     __syncwarp();
     for (uint32_t base = 0; base < total; base += 32u) {
@@ -359,24 +360,16 @@ __device__ __forceinline__ void coop_leaf_rounds(Walk& w, bool own_walk, const f
         sid = __float_as_uint(p2.w);
         tri = __float_as_uint(p1.w);
       }
-      // each owner takes the hits among its slots of this chunk, in leaf order
-      // (a miss changes nothing): the bits of its slots that hit, lowest first
-      const unsigned hits = __ballot_sync(FULL, hit);
-      uint32_t mine = 0;
-      if (own) {
-        const uint32_t lo = max(excl, base), hi = min(excl + cnt, base + 32u);
-        if (lo < hi) mine = ((hits >> (lo - base)) & ((1u << (hi - lo)) - 1u)) << (lo - excl);
-      }
-      while (__any_sync(FULL, mine != 0u)) {
-        const bool pick = mine != 0u;
-        const uint32_t src = pick ? excl + (uint32_t)(__ffs(mine) - 1) - base : lane;
+      // each owner takes its slots of this chunk in leaf order
+      for (uint32_t k = 0; k < kmax; k++) {
+        const uint32_t q = excl + k;
+        const bool mine = own && k < cnt && q >= base && q < base + 32u;
+        const uint32_t src = mine ? q - base : lane;
         const float tk = __shfl_sync(FULL, t, src);
+        const bool hk = __shfl_sync(FULL, (uint32_t)hit, src) != 0u;
         const uint32_t sk = __shfl_sync(FULL, sid, src), trk = __shfl_sync(FULL, tri, src);
         const uint32_t ik = __shfl_sync(FULL, i, src);
-        if (pick) {
-          walk_take_tie(w, lane_prims, ik, tk, sk, trk);
-          mine &= mine - 1u;
-        }
+        if (mine && hk) walk_take_tie(w, lane_prims, ik, tk, sk, trk);
       }
     }
     __syncwarp();
