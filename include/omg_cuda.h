@@ -40,9 +40,11 @@ extern "C" {
 /* BVH builders for omg_scene_upload */
 #define OMG_BVH_SAH 0            /* the reference's binned-SAH tree (mesh.rs:241-405), built on the host */
 #define OMG_BVH_LBVH 1           /* Morton/Karras LBVH built on the GPU */
-#define OMG_BVH_SAH3 2           /* binned SAH over all three axes (128 bins, leaves <= 4), built on the host:
+#define OMG_BVH_SAH3 2           /* binned SAH over all three axes (128 bins, leaves <= 4), built on the GPU:
                                     fewer node visits than OMG_BVH_SAH; hits equal the reference tree's under
                                     the near-tie rule (tie_mode 1), exact ties may resolve differently without it */
+#define OMG_BVH_SAH3_HOST 3      /* the same tree built on the host (same nodes, boxes and leaf ranges; the
+                                    primitives inside a leaf may be in another order) */
 
 typedef struct omg_ctx omg_ctx;
 

@@ -16,7 +16,7 @@ DOME_BINS = 9
 
 OK, PENDING = 0, 1
 E_INVALID, E_OOM, E_DEVICE, E_TIMEOUT, E_OVERFLOW, E_NOT_FOUND, E_NO_DEVICE = -1, -2, -3, -4, -5, -6, -7
-BVH_SAH, BVH_LBVH, BVH_SAH3 = 0, 1, 2
+BVH_SAH, BVH_LBVH, BVH_SAH3, BVH_SAH3_HOST = 0, 1, 2, 3
 GEOM_BOX, GEOM_MESH = 0, 1
 
 F8 = C.c_float * MAX_BANDS

@@ -20,7 +20,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["trace.cu", "wavefront.cu", "coop.cu", "reverb.cu", "lbvh.cu", "dome.cu", "noalloc.cu", "mlp.cu", "late.cu", "early.cu"]
+CU_SOURCES = ["trace.cu", "wavefront.cu", "coop.cu", "reverb.cu", "lbvh.cu", "sah3.cu", "dome.cu", "noalloc.cu", "mlp.cu", "late.cu", "early.cu"]
 CPP_SOURCES = ["api.cpp", "api_scene.cpp", "api_dome.cpp", "api_mlp.cpp", "api_late.cpp", "api_wire.cpp", "api_early.cpp", "scene.cpp"]
 
 

@@ -43,11 +43,50 @@ int32_t upload_scene_arrays(omg_ctx* ctx, SceneRec& S, const std::vector<float>&
   return OMG_OK;
 }
 
+// The three-axis tree built on the GPU (sah3.cu): the tessellated primitives
+// go up in tessellation order, the tree comes back in build_sah3's form, and
+// the host's primitive arrays are put in its leaf order.
+int32_t build_sah3_on_device(omg_ctx* ctx, SceneRec& S) {
+  const size_t np = S.prim_tri.size();
+  if (np == 0) {
+    S.ref_boxes.clear();
+    S.ref_ab.clear();
+    return OMG_OK;
+  }
+  std::vector<float> pr(np * 12, 0.0f);
+  for (size_t i = 0; i < np; i++) {
+    const float* g = &S.prim_geo[9 * i];
+    float* o = &pr[12 * i];
+    o[0] = g[0]; o[1] = g[1]; o[2] = g[2];
+    o[4] = g[3]; o[5] = g[4]; o[6] = g[5];
+    o[8] = g[6]; o[9] = g[7]; o[10] = g[8];
+  }
+  DevBuf<float4> d;
+  CK(d.alloc(np * 3));
+  CK(cudaMemcpy(d.p, pr.data(), pr.size() * 4, cudaMemcpyHostToDevice));
+  std::vector<uint32_t> perm;
+  CK(sah3_build_device(d.p, (uint32_t)np, S.ref_boxes, S.ref_ab, perm, ctx->stream));
+  std::vector<float> geo(S.prim_geo.size());
+  std::vector<uint32_t> tri(np);
+  std::vector<uint16_t> mat(np);
+  for (size_t i = 0; i < np; i++) {
+    const uint32_t j = perm[i];
+    if (j >= np) return OMG_E_INVALID;
+    std::memcpy(&geo[9 * i], &S.prim_geo[9 * (size_t)j], 9 * sizeof(float));
+    tri[i] = S.prim_tri[j];
+    mat[i] = S.prim_mat[j];
+  }
+  S.prim_geo.swap(geo);
+  S.prim_tri.swap(tri);
+  S.prim_mat.swap(mat);
+  return OMG_OK;
+}
+
 int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
                           const uint16_t* tri_mat, const float* tri_max_edge, const uint16_t* tri_surf,
                           const omg_material* mats, uint32_t nm, uint32_t nb, uint32_t kind, uint32_t* scene_id) {
   if (!ctx || !scene_id || nb == 0 || nb > (uint32_t)MAXB || (nt && (!pos || !idx || !tri_mat)) || (nm && !mats) ||
-      (kind != OMG_BVH_SAH && kind != OMG_BVH_LBVH && kind != OMG_BVH_SAH3))
+      (kind != OMG_BVH_SAH && kind != OMG_BVH_LBVH && kind != OMG_BVH_SAH3 && kind != OMG_BVH_SAH3_HOST))
     return OMG_E_INVALID;
   for (uint32_t t = 0; t < nt; t++) {
     if (tri_mat[t] >= nm) return OMG_E_INVALID;
@@ -95,11 +134,15 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
     }
   }
 
-  if (kind == OMG_BVH_SAH || kind == OMG_BVH_SAH3) {
-    if (kind == OMG_BVH_SAH)
+  if (kind == OMG_BVH_SAH || kind == OMG_BVH_SAH3 || kind == OMG_BVH_SAH3_HOST) {
+    if (kind == OMG_BVH_SAH) {
       build_sah(S->prim_geo, S->prim_tri, S->prim_mat, S->ref_boxes, S->ref_ab);
-    else
+    } else if (kind == OMG_BVH_SAH3_HOST) {
       build_sah3(S->prim_geo, S->prim_tri, S->prim_mat, S->ref_boxes, S->ref_ab);
+    } else {
+      int32_t rc = build_sah3_on_device(ctx, *S);
+      if (rc) return rc;
+    }
     std::vector<float> dev_nodes;
     S->root = flatten_bvh2(S->ref_boxes, S->ref_ab, dev_nodes);
     S->n_nodes = (uint32_t)(dev_nodes.size() / 16);

@@ -17,6 +17,7 @@
 //             to computing them per bounce: same f32 operations, same order)
 #pragma once
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "../../include/omg_cuda.h"
@@ -272,6 +273,13 @@ cudaError_t launch_late_update(const DLateUpdate* up, uint32_t n_up, const float
 cudaError_t lbvh_build(const float4* prims_in, uint32_t n_prims, float4* prims_out, float4* nodes_out,
                        int32_t* root_ref, void* scratch, size_t scratch_bytes, cudaStream_t s);
 size_t lbvh_scratch_bytes(uint32_t n_prims);
+// sah3.cu: the three-axis binned-SAH tree of build_sah3 (scene.cpp), built on
+// the GPU from the primitives in tessellation order (prims: a, e1, e2 per
+// primitive, 3 float4 each). Returns the tree in build_sah3's form and
+// numbering (ref_boxes: 6 floats a node, ref_ab: children or leaf range) and
+// perm[i] = the tessellation index of the primitive at leaf-order position i.
+cudaError_t sah3_build_device(const float4* prims, uint32_t n_prims, std::vector<float>& ref_boxes,
+                              std::vector<uint32_t>& ref_ab, std::vector<uint32_t>& perm, cudaStream_t s);
 // DScene::nodes_f from `nodes` on the device (m: the bound of |coordinate| per
 // axis; pad: near_tie_pad of the primitives)
 cudaError_t grow_nodes(const float4* nodes, float4* out, uint32_t n_nodes, const float m[3], float pad,
