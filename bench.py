@@ -502,6 +502,10 @@ def run_workload(args):
     return 0
 
 
+# the tree builders by name: sah3 is built on the GPU, sah3-host is the same tree built on the host
+BVH_KINDS = {"sah": 0, "lbvh": 1, "sah3": 2, "sah3-host": 3}
+
+
 def workload_summary(args, workload, steps, warmup, case=None, shape=None, autotune=True):
     """One secondary configuration measured (see run_workload): segments/s of
     the trace part (CUDA events, L2 flushed before each step), the roofline by
@@ -510,11 +514,12 @@ def workload_summary(args, workload, steps, warmup, case=None, shape=None, autot
     import torch
     from omg_audio_gb300 import Context, DomeProbe, Job, MeshBuilder, TraceConfig, _lib
     from omg_audio_gb300 import workloads as W
-    bvh = {"sah": _lib.BVH_SAH, "lbvh": _lib.BVH_LBVH, "sah3": _lib.BVH_SAH3}[args.bvh]
+    bvh = BVH_KINDS[args.bvh]
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     t0 = time.perf_counter()
+    upload_s = 0.0     # scene uploads alone: tessellation, tree build, device arrays
     oracle_jobs = []   # (mesh recorder or box, src, lis, n_rays, seed, n_bands, n_bins, max_time) for the CPU leg
     if workload == "shoebox12":
         case = W.shoebox12(seed=1)
@@ -535,7 +540,9 @@ def workload_summary(args, workload, steps, warmup, case=None, shape=None, autot
         for k, r in enumerate(rooms):
             mb = MeshBuilder()
             r.recorder.replay(mb)
+            tu = time.perf_counter()
             sc = ctx.upload_builder(mb, r.n_bands, bvh)
+            upload_s += time.perf_counter() - tu
             scenes.append(sc)
             jobs.append(Job(r.src, r.lis, r.n_rays, seed=100 + k, scene=sc, n_bands=r.n_bands, n_bins=r.n_bins,
                             max_time=r.max_time))
@@ -551,7 +558,9 @@ def workload_summary(args, workload, steps, warmup, case=None, shape=None, autot
                                   max_time=4.0, max_bounces=200, energy_floor=1e-6))
         mb = MeshBuilder()
         case.recorder.replay(mb)
+        tu = time.perf_counter()
         scene = ctx.upload_builder(mb, case.n_bands, bvh)
+        upload_s = time.perf_counter() - tu
         prims = scene.info()["prims"]
         jobs = [Job(tuple(s_), tuple(l_), args.city_rays, seed=500 + k, scene=scene)
                 for k, (s_, l_) in enumerate(zip(case.sources, case.listeners))]
@@ -605,7 +614,7 @@ def workload_summary(args, workload, steps, warmup, case=None, shape=None, autot
     res = batch.read()
     segs = batch.segments()
     line = {"metric": "ray-segments/s", "workload": workload, "desc": desc, "prims": prims,
-            "bvh": args.bvh, "setup_s": setup_s, "steps": steps, "trace_ms": float(np.mean(ms)),
+            "bvh": args.bvh, "setup_s": setup_s, "upload_s": upload_s, "steps": steps, "trace_ms": float(np.mean(ms)),
             "segments": segs, "value": segs / (float(np.mean(ms)) * 1e-3), "unit": "ray-segments/s",
             "autotune": tune, "clocks": clk.summary(),
             "rt60_range": [float(np.nanmin([np.min(rv.rt60) for _, rv in res])),
@@ -657,7 +666,7 @@ def workload_summary(args, workload, steps, warmup, case=None, shape=None, autot
 
 
 def compact_summary(line):
-    keep = {k: line[k] for k in ("desc", "prims", "bvh", "setup_s", "steps", "trace_ms", "segments", "value",
+    keep = {k: line[k] for k in ("desc", "prims", "bvh", "setup_s", "upload_s", "steps", "trace_ms", "segments", "value",
                                  "unit", "autotune", "clocks", "cpu_baseline", "dome") if k in line}
     rf = line.get("roofline", {})
     keep["roofline"] = {k: rf[k] for k in ("bytes_per_segment", "achieved", "peak", "unit", "frac", "n_node",
@@ -706,8 +715,10 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
     mb = MeshBuilder()
     case.recorder.replay(mb)
-    bvh = {"sah": _lib.BVH_SAH, "lbvh": _lib.BVH_LBVH, "sah3": _lib.BVH_SAH3}[args.bvh]
+    bvh = BVH_KINDS[args.bvh]
+    tu = time.perf_counter()
     scene = ctx.upload_builder(mb, 3, bvh)
+    upload_s = time.perf_counter() - tu
     jobs = [Job(src, lis, N_RAYS, seed=1000 + p, scene=scene, panel_offset=0, n_panels=len(case.panels))
             for p, (src, lis) in enumerate(case.pairs[:args.pairs])]
     batch = ctx.batch(jobs, case.panels)
@@ -813,8 +824,8 @@ def run_ours(args):
             "config": config_of(scene.info()["prims"]),
             "tie_rule": "near-tie rule (tie_mode 1: lowest surface id among hits within 1e-6 relative t) on the "
                         f"{args.bvh} tree",
-            "detail": {"bvh": args.bvh, "segments_per_step": segments, "dome_segments_per_step": dome_seg,
-                       "trace_ms": float(np.mean(trace_ms)), "step_ms": float(np.mean(step_ms)),
+            "detail": {"bvh": args.bvh, "upload_s": upload_s, "segments_per_step": segments,
+                       "dome_segments_per_step": dome_seg, "trace_ms": float(np.mean(trace_ms)), "step_ms": float(np.mean(step_ms)),
                        "step_ms_max": float(np.max(step_ms)), "dome_alone_ms": float(np.mean(dome_ms)),
                        "dome": "the 64 fans after the trace, on its stream", "autotune": tune,
                        "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
@@ -863,8 +874,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--bvh", choices=["sah", "lbvh", "sah3"], default=None,
-                    help="sah: the reference's tree; sah3: three-axis binned SAH (default); lbvh: built on the GPU")
+    ap.add_argument("--bvh", choices=list(BVH_KINDS), default=None,
+                    help="sah: the reference's tree (host); sah3: three-axis binned SAH built on the GPU (default); "
+                         "sah3-host: the same tree built on the host; lbvh: Morton LBVH built on the GPU")
     ap.add_argument("--ref-pairs", type=int, default=64)
     ap.add_argument("--pairs", type=int, default=N_PAIRS, help="pairs traced per step (default: the workload's 64)")
     ap.add_argument("--profile", action="store_true", help="launches only (a small case under a profiler)")
