@@ -9,6 +9,7 @@
 // the same f32 sums in the same order), applies the per-listener EMA and
 // writes the 9 bins. The fan is deterministic, so the result is too.
 #include "device_common.cuh"
+#include "walk.cuh"
 
 namespace omg {
 
@@ -33,69 +34,170 @@ __device__ __forceinline__ bool panel_hit(const DDomePanel& p, float ox, float o
   return false;
 }
 
-// dome.rs:328-382. Returns true (escaped) with the throughput in tp.
-template <bool TIE>
+// The escape of one fan ray as a state machine around its closest-hit walks
+// (trace_escape, one event at a time): the ray's position, direction and
+// throughput, and how many events it has taken.
+struct EscapeRay {
+  float px, py, pz, dx, dy, dz;
+  float tp[MAXB];
+  uint32_t ev;
+};
+
+// One event of trace_escape (dome.rs:336-381) after its closest-hit walk:
+// mesh hit (mh, tm, prim) or none. Returns 0 when the ray goes on (the next
+// walk starts from its new position), 1 when it escaped, 2 when it ends
+// without escaping. The same f32 operations as trace_escape.
+__device__ __forceinline__ int escape_event(const DScene& S, const DDomeLaunch& L, EscapeRay& r, bool mh, float tm,
+                                            int prim) {
+  const uint32_t nb = L.nb;
+  const float t_mesh = mh ? tm : FLT_MAX;
+  float t_pan = t_mesh;
+  int pan = -1;
+  for (uint32_t k = 0; k < L.n_panels; k++) {
+    float t;
+    if (panel_hit(L.panels[k], r.px, r.py, r.pz, r.dx, r.dy, r.dz, t_pan, t)) {
+      t_pan = t;
+      pan = (int)k;
+    }
+  }
+  if (pan >= 0) {
+    const DDomePanel& P = L.panels[pan];
+    if (!P.glass) return 2;  // a door leaf blocks
+#pragma unroll
+    for (int b = 0; b < MAXB; b++)
+      if ((uint32_t)b < nb) r.tp[b] = r.tp[b] * P.t2[b];
+    const float adv = t_pan + 1e-3f;
+    r.px = r.px + r.dx * adv;
+    r.py = r.py + r.dy * adv;
+    r.pz = r.pz + r.dz * adv;
+    return 0;
+  }
+  const bool escaped = r.pz > -0.05f || r.dz > 0.05f;
+  if (!mh) return escaped ? 1 : 2;
+  if (tm > 80.0f) return escaped ? 1 : 2;
+  const float4 p0 = __ldg(S.prims + 3 * prim);
+  const float4 p1 = __ldg(S.prims + 3 * prim + 1);
+  const DMat& M = S.mats[__float_as_uint(p0.w)];
+#pragma unroll
+  for (int b = 0; b < MAXB; b++)
+    if ((uint32_t)b < nb) r.tp[b] = r.tp[b] * (1.0f - M.absorption[b]);
+  if (r.tp[1] < 2e-3f) return 2;
+  const float4 nn = __ldg(S.normals + __float_as_uint(p1.w));
+  const float nx = nn.x, ny = nn.y, nz = nn.z;
+  const float dn = r.dx * nx + r.dy * ny + r.dz * nz;
+  float ox = nx, oy = ny, oz = nz;
+  if (dn > 0.0f) { ox = nx * -1.0f; oy = ny * -1.0f; oz = nz * -1.0f; }
+  const float hx = r.px + r.dx * tm, hy = r.py + r.dy * tm, hz = r.pz + r.dz * tm;
+  const float k2 = 2.0f * dn;
+  r.dx = r.dx - nx * k2;
+  r.dy = r.dy - ny * k2;
+  r.dz = r.dz - nz * k2;
+  normalize3(r.dx, r.dy, r.dz);
+  r.px = hx + ox * 1e-3f;
+  r.py = hy + oy * 1e-3f;
+  r.pz = hz + oz * 1e-3f;
+  return 0;
+}
+
+// dome.rs:328-382 under the reference's first-found rule (tie_mode 0): each
+// event's closest hit by the reference's ordered walk. Returns true (escaped)
+// with the throughput in tp.
 __device__ bool trace_escape(const DScene& S, const DDomeLaunch& L, float px, float py, float pz, float dx, float dy,
                              float dz, float tp[MAXB], uint32_t& events) {
-  const uint32_t nb = L.nb;
+  EscapeRay r{px, py, pz, dx, dy, dz, {}, 0u};
 #pragma unroll
-  for (int b = 0; b < MAXB; b++) tp[b] = 1.0f;
+  for (int b = 0; b < MAXB; b++) r.tp[b] = 1.0f;
+  int e = 2;
   for (uint32_t ev = 0; ev < L.max_events; ev++) {
     events++;
     float tm = FLT_MAX;
     int prim = 0;
-    // under the near-tie rule the 4-wide tree gives the same hit in half the
-    // dependent steps (this kernel has one thread per fan ray: latency-bound)
-    const bool mh = (TIE && S.nodes4) ? mesh_closest4(S, px, py, pz, dx, dy, dz, tm, prim, &L.hdr->error)
-                                      : mesh_closest<TIE>(S, px, py, pz, dx, dy, dz, tm, prim, &L.hdr->error);
-    const float t_mesh = mh ? tm : FLT_MAX;
-    float t_pan = t_mesh;
-    int pan = -1;
-    for (uint32_t k = 0; k < L.n_panels; k++) {
-      float t;
-      if (panel_hit(L.panels[k], px, py, pz, dx, dy, dz, t_pan, t)) {
-        t_pan = t;
-        pan = (int)k;
+    const bool mh = mesh_closest<false>(S, r.px, r.py, r.pz, r.dx, r.dy, r.dz, tm, prim, &L.hdr->error);
+    e = escape_event(S, L, r, mh, tm, prim);
+    if (e != 0) break;
+  }
+#pragma unroll
+  for (int b = 0; b < MAXB; b++) tp[b] = r.tp[b];
+  return e == 1;
+}
+
+// The specular escape of every (listener, fan ray) under the near-tie rule,
+// one lane each, with the persistent tracer's walk: the node phase lane by
+// lane (walk_spec_nodes, the grown binary boxes), then the pending leaves
+// tested by the whole warp (coop_leaf_rounds). The closest hit under this
+// rule does not depend on the walk, so each event sees the hit
+// any other near-tie walk finds; the events follow in trace_escape's f32 operations. Lanes
+// past the last ray take part in the warp's leaf rounds only.
+constexpr uint32_t kEscThreads = 128;
+__global__ void __launch_bounds__(kEscThreads) dome_escape_walk_kernel(DDomeLaunch L, uint32_t loop_guard) {
+  __shared__ uint8_t s_slots[kEscThreads / 32][256];
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t total = L.n_eyes * L.n_rays;
+  const DScene& S = *L.scene;
+  uint32_t* err = &L.hdr->error;
+  EscapeRay r;
+  int walk_stack_ref[STACK_DEPTH];
+  float walk_stack_t[STACK_DEPTH];
+  Walk w;
+  w.stack_ref = walk_stack_ref;
+  w.stack_t = walk_stack_t;
+  w.cur = kDone;
+  w.leaf = 0;
+  bool active = gid < total && L.max_events > 0;
+  int status = 2;
+  uint32_t events = 0;
+  if (gid < total) {
+    const uint32_t eye = gid / L.n_rays, j = gid % L.n_rays;
+    const uint32_t i = (uint32_t)((uint64_t)j * L.n_fan / L.n_rays);  // dome.rs:434
+    const float4 f = L.fan[i];
+    r.px = L.eyes[3 * eye]; r.py = L.eyes[3 * eye + 1]; r.pz = L.eyes[3 * eye + 2];
+    r.dx = f.x; r.dy = f.y; r.dz = f.z;
+#pragma unroll
+    for (int b = 0; b < MAXB; b++) r.tp[b] = 1.0f;
+    r.ev = 0;
+    if (active) {
+      walk_begin<true>(w, S, r.px, r.py, r.pz, r.dx, r.dy, r.dz, false);
+      events++;
+    }
+  }
+  uint32_t iters = 0;
+  while (__any_sync(0xffffffffu, active)) {
+    if (++iters > loop_guard) {
+      atomicOr(err, 8u);
+      active = false;
+      break;
+    }
+    bool over = false;
+    if (active) {
+      int st = 1 << 30;   // the node phase runs until the warp's lanes hold leaves (bounded by the walk budget)
+      over = walk_spec_nodes(w, S, r.px, r.py, r.pz, r.dx, r.dy, r.dz, st, err);
+    }
+    coop_leaf_rounds(w, active && !over, S.prims, r.px, r.py, r.pz, r.dx, r.dy, r.dz, s_slots[threadIdx.x >> 5],
+                     kCoopRounds, err);
+    if (active) {
+      if (!over && w.cur == kDone && w.leaf == 0) over = !walk_restart_fixed(w, S.root, S.walk_budget);
+      if (over) {
+        const int e = escape_event(S, L, r, walk_have(w), w.t_best, w.prim_best);
+        r.ev++;
+        if (e != 0) {
+          status = e;
+          active = false;
+        } else if (r.ev >= L.max_events) {
+          status = 2;
+          active = false;
+        } else {
+          walk_begin<true>(w, S, r.px, r.py, r.pz, r.dx, r.dy, r.dz, false);
+          events++;
+        }
       }
     }
-    if (pan >= 0) {
-      const DDomePanel& P = L.panels[pan];
-      if (!P.glass) return false;  // a door leaf blocks
-#pragma unroll
-      for (int b = 0; b < MAXB; b++)
-        if ((uint32_t)b < nb) tp[b] = tp[b] * P.t2[b];
-      const float adv = t_pan + 1e-3f;
-      px = px + dx * adv;
-      py = py + dy * adv;
-      pz = pz + dz * adv;
-      continue;
-    }
-    const bool escaped = pz > -0.05f || dz > 0.05f;
-    if (!mh) return escaped;
-    if (tm > 80.0f) return escaped;
-    const float4 p0 = __ldg(S.prims + 3 * prim);
-    const float4 p1 = __ldg(S.prims + 3 * prim + 1);
-    const DMat& M = S.mats[__float_as_uint(p0.w)];
-#pragma unroll
-    for (int b = 0; b < MAXB; b++)
-      if ((uint32_t)b < nb) tp[b] = tp[b] * (1.0f - M.absorption[b]);
-    if (tp[1] < 2e-3f) return false;
-    const float4 nn = __ldg(S.normals + __float_as_uint(p1.w));
-    const float nx = nn.x, ny = nn.y, nz = nn.z;
-    const float dn = dx * nx + dy * ny + dz * nz;
-    float ox = nx, oy = ny, oz = nz;
-    if (dn > 0.0f) { ox = nx * -1.0f; oy = ny * -1.0f; oz = nz * -1.0f; }
-    const float hx = px + dx * tm, hy = py + dy * tm, hz = pz + dz * tm;
-    const float k2 = 2.0f * dn;
-    dx = dx - nx * k2;
-    dy = dy - ny * k2;
-    dz = dz - nz * k2;
-    normalize3(dx, dy, dz);
-    px = hx + ox * 1e-3f;
-    py = hy + oy * 1e-3f;
-    pz = hz + oz * 1e-3f;
   }
-  return false;
+  if (gid < total) {
+    float* o = L.ray_tp + (uint64_t)gid * L.nb;
+    for (uint32_t b = 0; b < L.nb; b++) o[b] = r.tp[b];
+    L.ray_escape[gid] = status == 1 ? 1 : 0;
+    atomicAdd(&L.events[0], events);
+  }
 }
 
 // One warp's shared memory for the straight-through segment of one fan ray.
@@ -308,10 +410,10 @@ __device__ void through_warp(const DScene& S, const DDomeLaunch& L, ThroughSmem&
   }
 }
 
-// The specular escape of every (listener, fan ray), one thread each: its
-// transmission goes to ray_tp and its escape flag to ray_escape; the
-// straight-through kernel then completes the rays that need it.
-template <bool TIE>
+// The specular escape of every (listener, fan ray) under the first-found
+// rule, one thread each: its transmission goes to ray_tp and its escape flag
+// to ray_escape; the straight-through kernel then completes the rays that
+// need it.
 __global__ void dome_escape_kernel(DDomeLaunch L) {
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= L.n_eyes * L.n_rays) return;
@@ -322,7 +424,7 @@ __global__ void dome_escape_kernel(DDomeLaunch L) {
   const float ex = L.eyes[3 * eye], ey = L.eyes[3 * eye + 1], ez = L.eyes[3 * eye + 2];
   float bp[MAXB];
   uint32_t events = 0;
-  const bool esc = trace_escape<TIE>(S, L, ex, ey, ez, f.x, f.y, f.z, bp, events);
+  const bool esc = trace_escape(S, L, ex, ey, ez, f.x, f.y, f.z, bp, events);
   float* o = L.ray_tp + (uint64_t)gid * L.nb;
   for (uint32_t b = 0; b < L.nb; b++) o[b] = bp[b];
   L.ray_escape[gid] = esc ? 1 : 0;
@@ -362,16 +464,20 @@ __global__ void __launch_bounds__(32 * kThroughWarps) dome_through_kernel(DDomeL
 }
 
 // dome.rs:452-477 per listener: bins in fan order, EMA, directions. The
-// block stages the listener's rays (fan direction with its bin, transmission)
-// in shared memory, kDomeChunk at a time; thread k < 9 then sums bin k over
-// them in fan order (the same f32 sums in the same order as one loop).
+// block stages the listener's rays kDomeChunk at a time: every thread turns
+// one ray into its terms (tp / n_rays per band, the direction weighted by
+// max(tp[1], 0.2 tp[0]), its bin, or no bin when tp[0] <= 1e-9); then lane
+// k < 9 of the first warp adds the terms of bin k's rays in fan order (the
+// same f32 sums in the same order as the reference's one loop), finding them
+// 32 at a time by ballots.
 constexpr uint32_t kDomeChunk = 256;
 constexpr uint32_t kDomeBinThreads = 128;
 __global__ void __launch_bounds__(kDomeBinThreads) dome_bins_kernel(DDomeLaunch L, float ema_alpha) {
-  __shared__ float4 s_fan[kDomeChunk];
-  __shared__ float s_tp[kDomeChunk * MAXB];
+  __shared__ float s_c[kDomeChunk * MAXB];
+  __shared__ float s_w[kDomeChunk * 3];
+  __shared__ uint32_t s_bin[kDomeChunk];
   const uint32_t eye = blockIdx.x;
-  const uint32_t k = threadIdx.x;  // bin 0..8; the other threads only stage
+  const uint32_t k = threadIdx.x;  // bin 0..8 in the first warp
   const uint32_t nb = L.nb;
   const bool primed = L.primed[eye] != 0u;
   float e[MAXB];
@@ -382,23 +488,39 @@ __global__ void __launch_bounds__(kDomeBinThreads) dome_bins_kernel(DDomeLaunch 
   const float* tp_eye = L.ray_tp + (uint64_t)eye * L.n_rays * nb;
   for (uint32_t j0 = 0; j0 < L.n_rays; j0 += kDomeChunk) {
     const uint32_t m = L.n_rays - j0 < kDomeChunk ? L.n_rays - j0 : kDomeChunk;
-    for (uint32_t q = threadIdx.x; q < m; q += blockDim.x)
-      s_fan[q] = L.fan[(uint32_t)((uint64_t)(j0 + q) * L.n_fan / L.n_rays)];
-    for (uint32_t q = threadIdx.x; q < m * nb; q += blockDim.x) s_tp[q] = tp_eye[(uint64_t)j0 * nb + q];
+    for (uint32_t q = threadIdx.x; q < m; q += blockDim.x) {
+      const float4 f = L.fan[(uint32_t)((uint64_t)(j0 + q) * L.n_fan / L.n_rays)];
+      const float* tp = tp_eye + (uint64_t)(j0 + q) * nb;
+      const float t0 = tp[0];
+      if (t0 > 1e-9f) {
+        for (uint32_t b = 0; b < nb; b++) s_c[q * nb + b] = tp[b] / nr;
+        const float w = fmaxf(tp[1], t0 * 0.2f);
+        s_w[3 * q] = f.x * w;
+        s_w[3 * q + 1] = f.y * w;
+        s_w[3 * q + 2] = f.z * w;
+        s_bin[q] = (uint32_t)__float_as_int(f.w);
+      } else {
+        s_bin[q] = 0xFFFFFFFFu;
+      }
+    }
     __syncthreads();
-    if (k < 9) {
-      for (uint32_t q = 0; q < m; q++) {
-        const float4 f = s_fan[q];
-        if ((uint32_t)__float_as_int(f.w) != k) continue;
-        const float* tp = s_tp + q * nb;
-        if (tp[0] > 1e-9f) {
+    if (threadIdx.x < 32) {
+      for (uint32_t q0 = 0; q0 < m; q0 += 32) {
+        const uint32_t my_bin = q0 + k < m ? s_bin[q0 + k] : 0xFFFFFFFFu;
+        uint32_t mine = 0;
+        for (uint32_t bin = 0; bin < 9; bin++) {
+          const uint32_t bm = __ballot_sync(0xffffffffu, my_bin == bin);
+          if (k == bin) mine = bm;
+        }
+        while (mine) {
+          const uint32_t q = q0 + (uint32_t)(__ffs(mine) - 1);
+          mine &= mine - 1u;
 #pragma unroll
           for (int b = 0; b < MAXB; b++)
-            if ((uint32_t)b < nb) e[b] = e[b] + tp[b] / nr;
-          const float w = fmaxf(tp[1], tp[0] * 0.2f);
-          sx = sx + f.x * w;
-          sy = sy + f.y * w;
-          sz = sz + f.z * w;
+            if ((uint32_t)b < nb) e[b] = e[b] + s_c[q * nb + b];
+          sx = sx + s_w[3 * q];
+          sy = sy + s_w[3 * q + 1];
+          sz = sz + s_w[3 * q + 2];
         }
       }
     }
@@ -466,8 +588,11 @@ cudaError_t build_dome_fan(float4* fan, uint32_t n, cudaStream_t s) {
 cudaError_t launch_dome(const DDomeLaunch& L, cudaStream_t s) {
   const uint64_t total = (uint64_t)L.n_eyes * L.n_rays;
   if (total == 0) return cudaSuccess;
-  if (L.tie) dome_escape_kernel<true><<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);
-  else dome_escape_kernel<false><<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);
+  if (L.tie)
+    dome_escape_walk_kernel<<<(uint32_t)((total + kEscThreads - 1) / kEscThreads), kEscThreads, 0, s>>>(
+        L, kDefaultLoopGuard);
+  else
+    dome_escape_kernel<<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);
   dome_through_kernel<<<(uint32_t)((total + kThroughWarps - 1) / kThroughWarps), 32 * kThroughWarps, 0, s>>>(L);
   dome_bins_kernel<<<L.n_eyes, kDomeBinThreads, 0, s>>>(L, 0.35f);
   return cudaGetLastError();
