@@ -186,9 +186,18 @@ SCATTERING = 0.1
 
 
 def sample_rooms(n: int, seed: int) -> Rooms:
+    """n rooms of the training family. Absorption: half the rooms draw each of
+    their 18 values independently from U[ALPHA_LO, ALPHA_HI]; the other half
+    draw a room level from the log-uniform distribution on that range and
+    scatter every value around it (a factor exp(N(0, 0.35^2)), clipped to the
+    range), so that rooms whose surfaces are all hard, or all soft, are as
+    common as the rest (independent draws almost never give them)."""
     rng = np.random.default_rng(seed)
     size = rng.uniform(SIZE_LO, SIZE_HI, (n, 3))
     alpha = rng.uniform(ALPHA_LO, ALPHA_HI, (n, 6, N_BANDS))
+    level = np.exp(rng.uniform(np.log(ALPHA_LO), np.log(ALPHA_HI), (n, 1, 1)))
+    near = np.clip(level * np.exp(0.35 * rng.standard_normal((n, 6, N_BANDS))), ALPHA_LO, ALPHA_HI)
+    alpha = np.where(rng.random((n, 1, 1)) < 0.5, alpha, near)
     openness = rng.uniform(0.0, 1.0, (n, 4))
     # 0 to 4 apertures per room
     n_ap = rng.integers(0, 5, n)

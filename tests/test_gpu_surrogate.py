@@ -103,8 +103,8 @@ def test_training_lowers_the_loss(ctx):
 
 
 def test_room_surrogate_gains_over_sabine_falls_back_and_checkpoints(tmp_path):
-    """Trained on tracer echograms of the config-1 room family (small: 16k rooms
-    at 512 rays), the surrogate's RT60 beats the Sabine formula (the method
+    """Trained on tracer echograms of the config-1 room family (small: 32k rooms
+    at 1024 rays), the surrogate's RT60 beats the Sabine formula (the method
     without the network) against the tracer at 4096 rays; a room outside the
     training family is answered by the tracer; a checkpoint reloads to the same
     predictions."""
@@ -112,10 +112,10 @@ def test_room_surrogate_gains_over_sabine_falls_back_and_checkpoints(tmp_path):
     from omg_audio_gb300 import surrogate as S
     with Context(TraceConfig(n_bands=3, n_bins=2000, bin_dt=0.001, max_time=2.0, max_bounces=200,
                              energy_floor=1e-6, timeout_ms=60000)) as ctx:
-        train = S.sample_rooms(16384, seed=3)
-        bins, _ = S.trace_rooms(ctx, train, 512, seed=10)
-        sur = S.RoomSurrogate(ctx, members=2, hidden=128)
-        sur.fit(train, S.edc_db(bins, 0.001), epochs=25, batch=2048, lr=2e-3, lr_final=2e-5)
+        train = S.sample_rooms(32768, seed=3)
+        bins, _ = S.trace_rooms(ctx, train, 1024, seed=10)
+        sur = S.RoomSurrogate(ctx, members=2, hidden=256)
+        sur.fit(train, S.edc_db(bins, 0.001), epochs=40, batch=2048, lr=2e-3, lr_final=2e-5)
         test = S.sample_rooms(512, seed=4)
         bt, _ = S.trace_rooms(ctx, test, 4096, seed=20)
         rt = S.rt60_from_edc(S.edc_db(bt, 0.001))
