@@ -729,7 +729,8 @@ def run_ours(args):
     cfg = dict(CFG)
     if args.max_bounces:
         cfg["max_bounces"] = args.max_bounces
-    ctx = Context(TraceConfig(device=local, timeout_ms=60000, tie_mode=1, **cfg))
+    ctx = Context(TraceConfig(device=local, timeout_ms=60000, tie_mode=1, tri_test=1 if args.watertight else 0,
+                              **cfg))
     # a dedicated stream: the library launches on it and the events are recorded on it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -843,6 +844,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
             "config": config_of(scene.info()["prims"]),
+            "tri_test": ("watertight (Woop, Benthin, Wald 2013) on the exact vertices" if args.watertight
+                         else "the reference's Moller-Trumbore with its epsilons"),
             "tie_rule": "near-tie rule (tie_mode 1: lowest surface id among hits within 1e-6 relative t) on the "
                         f"{args.bvh} tree",
             "detail": {"bvh": args.bvh, "upload_s": upload_s, "segments_per_step": segments,
@@ -925,6 +928,8 @@ def main():
     ap.add_argument("--workload", choices=["multiroom", "shoebox12", "rooms256", "city"], default="multiroom",
                     help="multiroom: the headline (default); rooms256 and city print their own line")
     ap.add_argument("--city-rays", type=int, default=1 << 20, help="rays per source of the city workload")
+    ap.add_argument("--watertight", action="store_true",
+                    help="the watertight ray-triangle test (omg_params.tri_test 1) instead of the reference's")
     ap.add_argument("--no-extra-workloads", dest="extra_workloads", action="store_false",
                     help="skip the rooms256 and city summaries of the headline line")
     ap.add_argument("--extra-steps", type=int, default=3, help="timed steps of each extra workload")

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define OMG_ABI_VERSION 2
+#define OMG_ABI_VERSION 3
 #define OMG_MAX_BANDS 8
 #define OMG_DOME_BINS 9          /* dome.rs:30: 8 azimuth sectors + zenith */
 
@@ -87,7 +87,19 @@ typedef struct omg_params {
                                     a sound tree reaches. Smaller values cap it. */
     uint32_t loop_guard;         /* loop iterations of one warp of a persistent trace kernel
                                     before it stops (flag 8); 0 = 2^22 */
+    uint32_t tri_test;           /* ray-triangle test of the closest-hit queries: OMG_TRI_REFERENCE
+                                    or OMG_TRI_WATERTIGHT (needs tie_mode 1; omg_create returns
+                                    NULL otherwise) */
 } omg_params;
+
+/* Ray-triangle tests (omg_params.tri_test) */
+#define OMG_TRI_REFERENCE 0      /* the reference's Moller-Trumbore with its epsilons (mesh.rs:437-456)
+                                    on a, b - a, c - a: hits equal the reference's */
+#define OMG_TRI_WATERTIGHT 1     /* Woop, Benthin, Wald 2013 on the exact vertices: a ray through an edge
+                                    or vertex shared by two triangles hits one of them; scenes uploaded
+                                    to such a context keep the vertices beside the primitives (48 B a
+                                    primitive). The dome's straight-through seep and the early
+                                    reflections keep the reference's test. */
 
 /* LateBackend::trace job (late.rs:28-40): analytic shoebox [0,size]^3, walls in
  * Shoebox order x-,x+,y-,y+,z-,z+ (scene.rs:23-26). */

@@ -32,7 +32,7 @@ class omg_params(C.Structure):
                 ("max_bounces", C.c_uint32), ("energy_floor", C.c_float), ("receiver_radius", C.c_float),
                 ("wall_eps", C.c_float), ("speed_of_sound", C.c_float), ("dir_band", C.c_uint32),
                 ("device", C.c_int32), ("timeout_ms", C.c_uint32), ("tie_mode", C.c_uint32),
-                ("walk_budget", C.c_uint32), ("loop_guard", C.c_uint32)]
+                ("walk_budget", C.c_uint32), ("loop_guard", C.c_uint32), ("tri_test", C.c_uint32)]
 
 
 class omg_box_job(C.Structure):

@@ -57,6 +57,7 @@ DScene scene_view(const SceneRec& s, uint32_t walk_cap) {
   d.nodes4 = s.n_nodes4 ? s.nodes4.p : nullptr;
   d.nodes4c = s.n_nodes4 ? s.nodes4c.p : nullptr;
   d.nodes_f = s.nodes_f.p;
+  d.prims_wt = s.prims_wt.p;
   for (int a = 0; a < 3; a++) d.fast_m[a] = s.fast_m[a];
   d.root4 = s.root4;
   d.n_nodes4 = s.n_nodes4;
@@ -333,7 +334,8 @@ int32_t record_launch(omg_ctx* ctx, BatchRec& B, cudaStream_t s, int parts = 3) 
     if (eff.tail_mode == 2 && !B.coop_ok) eff.tail_mode = 0;
     CK(launch_wavefront(B.d_jobs.p, B.n_jobs, B.total_rays, B.max_nb, ctx->d_scenes.p, B.d_job_mats.p,
                         B.d_panels.p, B.d_groups.p, B.d_acc.p, B.d_hdr.p, B.d_seg.p, B.wf, B.d_ep_q.p,
-                        B.d_ep_ctl.p, eff, ctx->n_sms, ctx->prm.tie_mode != 0, s));
+                        B.d_ep_ctl.p, eff, ctx->n_sms, ctx->prm.tie_mode != 0, s,
+                        ctx->prm.tri_test == OMG_TRI_WATERTIGHT));
   }
   if (parts & 2) {
     CK(launch_finalize(B.d_jobs.p, B.n_jobs, B.d_acc.p, B.d_out.p, B.n_out, s));
@@ -587,7 +589,9 @@ omg_ctx* omg_create(const omg_params* p) {
   if (p) prm = *p;
   else omg_params_default(&prm);
   if (prm.n_bands == 0 || prm.n_bands > OMG_MAX_BANDS || prm.n_bins == 0 || !(prm.bin_dt > 0.0f) ||
-      prm.dir_band >= prm.n_bands || !(prm.speed_of_sound > 0.0f))
+      prm.dir_band >= prm.n_bands || !(prm.speed_of_sound > 0.0f) ||
+      (prm.tri_test != OMG_TRI_REFERENCE && prm.tri_test != OMG_TRI_WATERTIGHT) ||
+      (prm.tri_test == OMG_TRI_WATERTIGHT && prm.tie_mode != 1))
     return nullptr;
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n <= prm.device || prm.device < 0) {

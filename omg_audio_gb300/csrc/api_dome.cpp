@@ -208,6 +208,7 @@ int32_t dome_submit(omg_ctx* ctx, DomeRec& D, const float* eyes, uint32_t n_eyes
   L.hdr = D.hdr.p;
   L.events = D.events.p;
   L.tie = ctx->prm.tie_mode;
+  L.wt = ctx->prm.tri_test == OMG_TRI_WATERTIGHT ? 1u : 0u;
   CK(launch_dome(L, s));
   CK(cudaMemcpyAsync(D.h_energy.p, D.energy.p, 9ull * nb * n_eyes * 4, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(D.h_dir.p, D.dir.p, 27ull * n_eyes * 4, cudaMemcpyDeviceToHost, s));

@@ -43,10 +43,33 @@ int32_t upload_scene_arrays(omg_ctx* ctx, SceneRec& S, const std::vector<float>&
   return OMG_OK;
 }
 
+// The exact vertices of every primitive in leaf order (watertight contexts):
+// A, B, C in .xyz with the primitive's own .w words (material, triangle,
+// surface), so a walk reads its ids from either array. vtx: 9 floats per
+// primitive in tessellation order; perm: tessellation index per position.
+int32_t upload_exact_vertices(omg_ctx* ctx, SceneRec& S, const std::vector<float>& vtx,
+                              const std::vector<uint32_t>& perm, const std::vector<uint16_t>& psurf) {
+  const size_t np = S.prim_tri.size();
+  if (np == 0) return OMG_OK;
+  if (perm.size() != np || vtx.size() != 9 * np) return OMG_E_INVALID;
+  std::vector<float> pr(np * 12);
+  for (size_t i = 0; i < np; i++) {
+    const float* v = &vtx[9 * (size_t)perm[i]];
+    float* o = &pr[12 * i];
+    const uint32_t m = S.prim_mat[i], t = S.prim_tri[i], s = psurf.empty() ? 0u : psurf[i];
+    o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; std::memcpy(&o[3], &m, 4);
+    o[4] = v[3]; o[5] = v[4]; o[6] = v[5]; std::memcpy(&o[7], &t, 4);
+    o[8] = v[6]; o[9] = v[7]; o[10] = v[8]; std::memcpy(&o[11], &s, 4);
+  }
+  CK(S.prims_wt.alloc(np * 3));
+  CK(cudaMemcpy(S.prims_wt.p, pr.data(), pr.size() * 4, cudaMemcpyHostToDevice));
+  return OMG_OK;
+}
+
 // The three-axis tree built on the GPU (sah3.cu): the tessellated primitives
 // go up in tessellation order, the tree comes back in build_sah3's form, and
 // the host's primitive arrays are put in its leaf order.
-int32_t build_sah3_on_device(omg_ctx* ctx, SceneRec& S) {
+int32_t build_sah3_on_device(omg_ctx* ctx, SceneRec& S, std::vector<uint32_t>* perm_out) {
   const size_t np = S.prim_tri.size();
   if (np == 0) {
     S.ref_boxes.clear();
@@ -79,6 +102,7 @@ int32_t build_sah3_on_device(omg_ctx* ctx, SceneRec& S) {
   S.prim_geo.swap(geo);
   S.prim_tri.swap(tri);
   S.prim_mat.swap(mat);
+  if (perm_out) perm_out->swap(perm);
   return OMG_OK;
 }
 
@@ -103,7 +127,11 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
   S->n_tris = nt;
   S->n_bands = nb;
   S->bvh_kind = kind;
-  tessellate(pos, idx, nt, tri_mat, tri_max_edge, S->prim_geo, S->prim_tri, S->prim_mat);
+  // watertight contexts keep every primitive's exact vertices (prims_wt)
+  const bool wt = ctx->prm.tri_test == OMG_TRI_WATERTIGHT;
+  std::vector<float> vtx;
+  std::vector<uint32_t> perm;
+  tessellate(pos, idx, nt, tri_mat, tri_max_edge, S->prim_geo, S->prim_tri, S->prim_mat, wt ? &vtx : nullptr);
   S->n_prims = (uint32_t)S->prim_tri.size();
   if (S->n_prims >= (1u << 28)) return OMG_E_INVALID;
   std::vector<float> normals;
@@ -136,11 +164,11 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
 
   if (kind == OMG_BVH_SAH || kind == OMG_BVH_SAH3 || kind == OMG_BVH_SAH3_HOST) {
     if (kind == OMG_BVH_SAH) {
-      build_sah(S->prim_geo, S->prim_tri, S->prim_mat, S->ref_boxes, S->ref_ab);
+      build_sah(S->prim_geo, S->prim_tri, S->prim_mat, S->ref_boxes, S->ref_ab, wt ? &perm : nullptr);
     } else if (kind == OMG_BVH_SAH3_HOST) {
-      build_sah3(S->prim_geo, S->prim_tri, S->prim_mat, S->ref_boxes, S->ref_ab);
+      build_sah3(S->prim_geo, S->prim_tri, S->prim_mat, S->ref_boxes, S->ref_ab, wt ? &perm : nullptr);
     } else {
-      int32_t rc = build_sah3_on_device(ctx, *S);
+      int32_t rc = build_sah3_on_device(ctx, *S, wt ? &perm : nullptr);
       if (rc) return rc;
     }
     std::vector<float> dev_nodes;
@@ -150,6 +178,7 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
     for (uint32_t i = 0; i < S->n_prims; i++) psurf[i] = tsurf[S->prim_tri[i]];
     int32_t rc = upload_scene_arrays(ctx, *S, S->prim_geo, S->prim_tri, S->prim_mat, psurf, normals, dmats, tsurf);
     if (rc) return rc;
+    if (wt && (rc = upload_exact_vertices(ctx, *S, vtx, perm, psurf))) return rc;
     CK(S->nodes.alloc(S->n_nodes * 4));
     if (S->n_nodes)
       CK(cudaMemcpy(S->nodes.p, dev_nodes.data(), dev_nodes.size() * 4, cudaMemcpyHostToDevice));
@@ -211,6 +240,14 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
       CK(cudaStreamSynchronize(ctx->stream));
       std::swap(S->prims.p, sorted.p);
       std::swap(S->prims.n, sorted.n);
+      if (wt) {
+        // the leaf order: the sorted keys' low words (lbvh.cu keeps them past
+        // its 64-byte bounds block)
+        std::vector<unsigned long long> keys(S->n_prims);
+        CK(cudaMemcpy(keys.data(), scratch.p + 64, keys.size() * 8, cudaMemcpyDeviceToHost));
+        perm.resize(S->n_prims);
+        for (uint32_t i = 0; i < S->n_prims; i++) perm[i] = (uint32_t)(keys[i] & 0xFFFFFFFFull);
+      }
       // host copy of the leaf-ordered primitives for export
       std::vector<float> pr((size_t)S->n_prims * 12);
       CK(cudaMemcpy(pr.data(), S->prims.p, pr.size() * 4, cudaMemcpyDeviceToHost));
@@ -223,6 +260,10 @@ int32_t scene_upload_impl(omg_ctx* ctx, const float* pos, uint32_t nv, const uin
         std::memcpy(&t, &o[7], 4);
         S->prim_mat[i] = (uint16_t)m;
         S->prim_tri[i] = t;
+      }
+      if (wt) {
+        for (uint32_t i = 0; i < S->n_prims; i++) psurf[i] = tsurf[S->prim_tri[i]];
+        if ((rc = upload_exact_vertices(ctx, *S, vtx, perm, psurf))) return rc;
       }
       // grown boxes for the near-tie walks: the bound from the primitives
       float mx[3] = {0.0f, 0.0f, 0.0f};

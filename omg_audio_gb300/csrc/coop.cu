@@ -103,6 +103,7 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
   uint32_t rid = kNone;
   const float4* nodes = nullptr;
   const float4* prims = nullptr;
+  bool pwt = false;   // watertight context: prims holds the exact vertices
   float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, ix = 0, iy = 0, iz = 0;
   int cur = kDoneC, sp = 0;
   bool have = false;
@@ -119,7 +120,8 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
     ix = __frcp_rn(dx); iy = __frcp_rn(dy); iz = __frcp_rn(dz);
     const DScene& S = scenes[J.scene];
     nodes = S.nodes4c;
-    prims = S.prims;
+    pwt = S.prims_wt != nullptr;
+    prims = pwt ? S.prims_wt : S.prims;
     // a shoebox ray (its hit is found when it is shaded) or an empty scene:
     // the walk ends at its first step without reading a node
     const bool walkable = J.geom == OMG_GEOM_MESH && S.n_prims != 0u && nodes != nullptr;
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(256, 4) trace_coop_kernel(const DJob* __restri
         uint32_t ls = s_best, ltr = tri_best;
         int lp = prim_best;
         TieState lts = ts;
-        if (leaf) leaf_test<true>(prims, ref, ox, oy, oz, dx, dy, dz, lh, lt, lc, lp, ls, ltr, lts);
+        if (leaf) leaf_test<true>(prims, ref, ox, oy, oz, dx, dy, dz, lh, lt, lc, lp, ls, ltr, lts, pwt);
 #pragma unroll
         for (int m = 1; m <= 2; m <<= 1) {
           const bool oh = __shfl_xor_sync(FULL, (int)lh, m) != 0;

@@ -159,6 +159,82 @@ __device__ __forceinline__ bool ray_tri(const float4& p0, const float4& p1, cons
   return false;
 }
 
+// Watertight ray-triangle test (Woop, Benthin, Wald 2013, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1)) on the exact vertices A, B, C (.xyz).
+// The vertices are translated to the ray origin and sheared so that the ray
+// runs along +z: kz is the axis of the largest |d_a| (the first of equal
+// ones), kx and ky the next two, swapped when d_kz < 0 so that the winding
+// stays. The signs of the 2D edge functions U, V, W decide the hit; an edge
+// shared by two triangles gives both of them the same value with opposite
+// signs (the same products of the same sheared coordinates), and a value that
+// rounds to 0 is computed again in FP64 (exact products of f32 values), so a
+// ray through a shared edge or vertex hits at least one of its triangles.
+// Both faces count, and a hit needs t > 1e-5, as the reference's test
+// (mesh.rs:455). Every step rounds as written (explicit round-to-nearest
+// operations). ray_tri_wt is the out-of-line copy for walks that choose the
+// test at run time; kernels compiled for watertight scenes inline the body.
+__device__ __forceinline__ float pick3(float a, float b, float c, int k) { return k == 0 ? a : (k == 1 ? b : c); }
+
+__device__ __forceinline__ bool ray_tri_wt_body(const float4 A4, const float4 B4, const float4 C4, float ox,
+                                                float oy, float oz, float dx, float dy, float dz, float& tout) {
+  const float adx = fabsf(dx), ady = fabsf(dy), adz = fabsf(dz);
+  int kz = 0;
+  if (ady > adx) kz = 1;
+  if (adz > (kz == 0 ? adx : ady)) kz = 2;
+  int kx = kz == 2 ? 0 : kz + 1;
+  int ky = kx == 2 ? 0 : kx + 1;
+  const float dkz = pick3(dx, dy, dz, kz);
+  if (dkz < 0.0f) {
+    const int k = kx;
+    kx = ky;
+    ky = k;
+  }
+  const float Sx = __fdiv_rn(pick3(dx, dy, dz, kx), dkz);
+  const float Sy = __fdiv_rn(pick3(dx, dy, dz, ky), dkz);
+  const float Sz = __fdiv_rn(1.0f, dkz);
+  const float ax = __fsub_rn(A4.x, ox), ay = __fsub_rn(A4.y, oy), az = __fsub_rn(A4.z, oz);
+  const float bx = __fsub_rn(B4.x, ox), by = __fsub_rn(B4.y, oy), bz = __fsub_rn(B4.z, oz);
+  const float cx = __fsub_rn(C4.x, ox), cy = __fsub_rn(C4.y, oy), cz = __fsub_rn(C4.z, oz);
+  const float akz = pick3(ax, ay, az, kz), bkz = pick3(bx, by, bz, kz), ckz = pick3(cx, cy, cz, kz);
+  const float Ax = __fsub_rn(pick3(ax, ay, az, kx), __fmul_rn(Sx, akz));
+  const float Ay = __fsub_rn(pick3(ax, ay, az, ky), __fmul_rn(Sy, akz));
+  const float Bx = __fsub_rn(pick3(bx, by, bz, kx), __fmul_rn(Sx, bkz));
+  const float By = __fsub_rn(pick3(bx, by, bz, ky), __fmul_rn(Sy, bkz));
+  const float Cx = __fsub_rn(pick3(cx, cy, cz, kx), __fmul_rn(Sx, ckz));
+  const float Cy = __fsub_rn(pick3(cx, cy, cz, ky), __fmul_rn(Sy, ckz));
+  float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+  float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+  float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = __double2float_rn(__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx)));
+    V = __double2float_rn(__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx)));
+    W = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax)));
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+  const float det = __fadd_rn(__fadd_rn(U, V), W);
+  if (det == 0.0f) return false;
+  const float Az = __fmul_rn(Sz, akz), Bz = __fmul_rn(Sz, bkz), Cz = __fmul_rn(Sz, ckz);
+  const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+  const float t = __fdiv_rn(T, det);
+  if (!(t > 1e-5f)) return false;
+  tout = t;
+  return true;
+}
+
+static __device__ __noinline__ bool ray_tri_wt(const float4 A4, const float4 B4, const float4 C4, float ox, float oy,
+                                               float oz, float dx, float dy, float dz, float& tout) {
+  return ray_tri_wt_body(A4, B4, C4, ox, oy, oz, dx, dy, dz, tout);
+}
+
+// The ray-triangle test of the closest-hit walks: the watertight test on the
+// exact vertices (DScene::prims_wt) in watertight contexts (wt), else the
+// reference's test on a, e1, e2 (DScene::prims).
+__device__ __forceinline__ bool tri_hit(bool wt, const float4& p0, const float4& p1, const float4& p2, float ox,
+                                        float oy, float oz, float dx, float dy, float dz, float& tout) {
+  return wt ? ray_tri_wt(p0, p1, p2, ox, oy, oz, dx, dy, dz, tout)
+            : ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, tout);
+}
+
 // mesh.rs:484-541 — ordered closest-hit traversal over the child-box BVH2.
 // Visit order, culling (t_enter >= best) and the strict `<` on hits are the
 // reference's, so over the reference tree the same triangle wins every tie.
@@ -229,7 +305,8 @@ __device__ __forceinline__ bool tie_take(float t, uint32_t s, uint32_t tr, bool 
 template <bool TIE>
 __device__ __forceinline__ bool leaf_test(const float4* __restrict__ prims, int leaf, float ox, float oy, float oz,
                                           float dx, float dy, float dz, bool& have, float& t_best, float& t_cull,
-                                          int& prim_best, uint32_t& s_best, uint32_t& tri_best, TieState& ts) {
+                                          int& prim_best, uint32_t& s_best, uint32_t& tri_best, TieState& ts,
+                                          bool wt = false) {
   const uint32_t code = ~(uint32_t)leaf;
   const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
   for (uint32_t i = start; i < end; i++) {
@@ -237,7 +314,7 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ prims, int 
     const float4 p1 = __ldg(prims + 3 * i + 1);
     const float4 p2 = __ldg(prims + 3 * i + 2);
     float t;
-    if (ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) {
+    if (tri_hit(wt, p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) {
       if (!TIE) {
         if (!have || t < t_best) {
           have = true;
@@ -275,7 +352,8 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
   // near-tie walks use the grown boxes (DScene::nodes_f): they find every hit
   // of every primitive, whatever the tree (the exact test on them)
   const float4* __restrict__ nodes = (TIE && S.nodes_f) ? S.nodes_f : S.nodes;
-  const float4* __restrict__ prims = S.prims;
+  const bool wt = S.prims_wt != nullptr;
+  const float4* __restrict__ prims = wt ? S.prims_wt : S.prims;
   bool have = false;
   t_best = FLT_MAX;
   float t_cull = FLT_MAX;            // TIE: t_min * (1 + 1e-6); else best; FLT_MAX before the first hit
@@ -351,7 +429,8 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
           atomicOr(err, 4u);
           return have;
         }
-        leaf_test<TIE>(prims, cur, ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best, ts);
+        leaf_test<TIE>(prims, cur, ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best, ts,
+                       wt);
         cur = pop();
       } else {
         if (leaf == 0 && cur < 0) {  // a leaf reached outside the node loop (e.g. a leaf root)
@@ -364,7 +443,7 @@ __device__ __forceinline__ bool mesh_closest(const DScene& S, float ox, float oy
             return have;
           }
           leaf_test<TIE>(prims, leaf, ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best,
-                         ts);
+                         ts, wt);
           leaf = 0;
           if (cur < 0) {
             leaf = cur;
@@ -402,7 +481,7 @@ __device__ __forceinline__ int bvh4_step(const float4* __restrict__ nodes, const
                                          float ox, float oy, float oz, float dx, float dy, float dz, float ix,
                                          float iy, float iz, bool& have, float& t_best, float& t_cull,
                                          int& prim_best, uint32_t& s_best, uint32_t& tri_best, TieState& ts,
-                                         int* stack_ref, float* stack_t, int& sp, uint32_t* err) {
+                                         int* stack_ref, float* stack_t, int& sp, uint32_t* err, bool wt = false) {
   const float4* nd = nodes + 8 * cur;
   const float4 lx = __ldg(nd + 0), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
   const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5), rf = __ldg(nd + 6);
@@ -431,7 +510,8 @@ __device__ __forceinline__ int bvh4_step(const float4* __restrict__ nodes, const
       if (r[j] < 0 && t[j] <= bt) { bt = t[j]; bk = j; }
     if (bk < 0) break;
     if (bt <= t_cull)
-      leaf_test<true>(prims, r[bk], ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best, ts);
+      leaf_test<true>(prims, r[bk], ox, oy, oz, dx, dy, dz, have, t_best, t_cull, prim_best, s_best, tri_best, ts,
+                      wt);
     r[bk] = kDone4;
     t[bk] = FLT_MAX;
   }
@@ -479,8 +559,9 @@ __device__ __forceinline__ bool mesh_closest4(const DScene& S, float ox, float o
         atomicOr(err, 4u);
         return have;
       }
-      cur = bvh4_step(S.nodes4, S.prims, cur, ox, oy, oz, dx, dy, dz, ix, iy, iz, have, t_best, t_cull, prim_best,
-                      s_best, tri_best, ts, stack_ref, stack_t, sp, err);
+      cur = bvh4_step(S.nodes4, S.prims_wt ? S.prims_wt : S.prims, cur, ox, oy, oz, dx, dy, dz, ix, iy, iz, have,
+                      t_best, t_cull, prim_best, s_best, tri_best, ts, stack_ref, stack_t, sp, err,
+                      S.prims_wt != nullptr);
     }
     if (!ts.amb || ts.fixed) break;
     // a second walk with the final near-tie window (see TieState)

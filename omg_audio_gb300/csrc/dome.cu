@@ -129,6 +129,7 @@ __device__ bool trace_escape(const DScene& S, const DDomeLaunch& L, float px, fl
 // any other near-tie walk finds; the events follow in trace_escape's f32 operations. Lanes
 // past the last ray take part in the warp's leaf rounds only.
 constexpr uint32_t kEscThreads = 128;
+template <bool WT>
 __global__ void __launch_bounds__(kEscThreads) dome_escape_walk_kernel(DDomeLaunch L, uint32_t loop_guard) {
   __shared__ uint8_t s_slots[kEscThreads / 32][256];
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -172,8 +173,8 @@ __global__ void __launch_bounds__(kEscThreads) dome_escape_walk_kernel(DDomeLaun
       int st = 1 << 30;   // the node phase runs until the warp's lanes hold leaves (bounded by the walk budget)
       over = walk_spec_nodes(w, S, r.px, r.py, r.pz, r.dx, r.dy, r.dz, st, err);
     }
-    coop_leaf_rounds(w, active && !over, S.prims, r.px, r.py, r.pz, r.dx, r.dy, r.dz, s_slots[threadIdx.x >> 5],
-                     kCoopRounds, err);
+    coop_leaf_rounds<WT>(w, active && !over, WT ? S.prims_wt : S.prims, WT, r.px, r.py, r.pz, r.dx, r.dy, r.dz,
+                         s_slots[threadIdx.x >> 5], kCoopRounds, err);
     if (active) {
       if (!over && w.cur == kDone && w.leaf == 0) over = !walk_restart_fixed(w, S.root, S.walk_budget);
       if (over) {
@@ -588,8 +589,11 @@ cudaError_t build_dome_fan(float4* fan, uint32_t n, cudaStream_t s) {
 cudaError_t launch_dome(const DDomeLaunch& L, cudaStream_t s) {
   const uint64_t total = (uint64_t)L.n_eyes * L.n_rays;
   if (total == 0) return cudaSuccess;
-  if (L.tie)
-    dome_escape_walk_kernel<<<(uint32_t)((total + kEscThreads - 1) / kEscThreads), kEscThreads, 0, s>>>(
+  if (L.tie && L.wt)
+    dome_escape_walk_kernel<true><<<(uint32_t)((total + kEscThreads - 1) / kEscThreads), kEscThreads, 0, s>>>(
+        L, kDefaultLoopGuard);
+  else if (L.tie)
+    dome_escape_walk_kernel<false><<<(uint32_t)((total + kEscThreads - 1) / kEscThreads), kEscThreads, 0, s>>>(
         L, kDefaultLoopGuard);
   else
     dome_escape_kernel<<<(uint32_t)((total + 127) / 128), 128, 0, s>>>(L);

@@ -77,6 +77,11 @@ struct DScene {
   // (n_nodes4 + 1).
   uint32_t walk_budget;
   uint32_t walk_budget4;
+  // Watertight contexts (omg_params.tri_test): the exact vertices A, B, C of
+  // every primitive as (A, material), (B, triangle), (C, surface), the same
+  // .w words as prims; the closest-hit walks then test these with the
+  // watertight test. Null: the reference's test on prims.
+  const float4* prims_wt;
 };
 constexpr int32_t kEmpty4 = 0x7FFFFFFE;
 
@@ -219,11 +224,12 @@ struct EpochArgs {
 
 // ----------------------------------------------------------- kernel launchers
 // trace.cu. `ep`: one epoch of an epoch chain (null: a single launch).
+// wt: the context's scenes carry exact vertices (watertight test)
 cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays, uint32_t max_nb,
                          const DScene* scenes, const DMat* job_mats, const DPanel* panels,
                          const DPanelGroup* groups, float* acc,
                          DLaunch* hdr, uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie,
-                         cudaStream_t s, const EpochArgs* ep = nullptr);
+                         cudaStream_t s, const EpochArgs* ep = nullptr, bool wt = false);
 // trace.cu: load the per-lane trace kernel variants launch_trace may pick for a
 // single launch (3 and 8 bands, with and without the near-tie rule) now, so
 // that a later launch does not wait for the driver's lazy module loading.
@@ -240,7 +246,7 @@ cudaError_t launch_wavefront(const DJob* jobs, uint32_t n_jobs, uint32_t total_r
                              const DScene* scenes, const DMat* job_mats, const DPanel* panels,
                              const DPanelGroup* groups, float* acc, DLaunch* hdr, uint32_t* job_segments,
                              const WfState& st, uint32_t* ep_q, EpochCtl* ep_ctl, const LaunchShape& shape,
-                             int n_sms, bool tie, cudaStream_t s);
+                             int n_sms, bool tie, cudaStream_t s, bool wt = false);
 cudaError_t launch_finalize(const DJob* jobs, uint32_t n_jobs, const float* acc, float* out, uint64_t total_out,
                             cudaStream_t s);
 cudaError_t launch_raycast(const DScene* scene, const float* o, const float* d, uint32_t n, float* t,
@@ -314,6 +320,7 @@ struct DDomeLaunch {
   DLaunch* hdr;
   uint32_t* events;           // escape events + through calls (2 counters)
   uint32_t tie;               // near-tie rule of the escape raycasts (omg_params.tie_mode)
+  uint32_t wt;                // the scene carries exact vertices (watertight test)
 };
 cudaError_t launch_dome(const DDomeLaunch& L, cudaStream_t s);
 

@@ -64,6 +64,7 @@ struct SceneRec {
   DevBuf<float4> nodes4;          // 4-wide collapse of `nodes` (host-built trees)
   DevBuf<float4> nodes4c;         // the same, child by child
   DevBuf<float4> nodes_f;         // binary nodes with grown boxes (fused multiply-add slab test)
+  DevBuf<float4> prims_wt;        // watertight contexts: exact vertices A, B, C per primitive (prims' .w words)
   float fast_m[3] = {0, 0, 0};
   int32_t root4 = 0;
   uint32_t n_nodes4 = 0;

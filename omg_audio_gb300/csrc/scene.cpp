@@ -96,6 +96,7 @@ struct Prim {
   F3 a, e1, e2;
   uint32_t tri;
   uint16_t material;
+  uint32_t id;    // tessellation index (carried, never compared)
 };
 
 struct RefNode {  // mesh.rs:52-58
@@ -224,7 +225,7 @@ uint32_t build_node(std::vector<RefNode>& nodes, std::vector<Prim>& prims, size_
 // mesh.rs:241-287 — tessellate (longest edge at its midpoint, LIFO work list).
 void tessellate(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
                 const float* tri_max_edge, std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri,
-                std::vector<uint16_t>& prim_mat) {
+                std::vector<uint16_t>& prim_mat, std::vector<float>* prim_vtx) {
   struct W {
     F3 a, b, c;
     uint32_t t;
@@ -236,6 +237,7 @@ void tessellate(const float* pos, const uint32_t* idx, uint32_t n_tris, const ui
   prim_geo.clear();
   prim_tri.clear();
   prim_mat.clear();
+  if (prim_vtx) prim_vtx->clear();
   while (!work.empty()) {
     W w = work.back();
     work.pop_back();
@@ -262,6 +264,10 @@ void tessellate(const float* pos, const uint32_t* idx, uint32_t n_tris, const ui
     F3 e1 = sub(b, a), e2 = sub(c, a);
     const float g[9] = {a.x, a.y, a.z, e1.x, e1.y, e1.z, e2.x, e2.y, e2.z};
     prim_geo.insert(prim_geo.end(), g, g + 9);
+    if (prim_vtx) {
+      const float v[9] = {a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z};
+      prim_vtx->insert(prim_vtx->end(), v, v + 9);
+    }
     prim_tri.push_back(w.t);
     prim_mat.push_back(tri_mat[w.t]);
   }
@@ -270,12 +276,12 @@ void tessellate(const float* pos, const uint32_t* idx, uint32_t n_tris, const ui
 // Reference SAH tree over the tessellated prims (reorders them into leaf
 // order). ref_boxes/ref_ab receive the reference's node array.
 void build_sah(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, std::vector<uint16_t>& prim_mat,
-               std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab) {
+               std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab, std::vector<uint32_t>* perm) {
   size_t n = prim_tri.size();
   std::vector<Prim> prims(n);
   for (size_t i = 0; i < n; i++) {
     const float* g = &prim_geo[9 * i];
-    prims[i] = {{g[0], g[1], g[2]}, {g[3], g[4], g[5]}, {g[6], g[7], g[8]}, prim_tri[i], prim_mat[i]};
+    prims[i] = {{g[0], g[1], g[2]}, {g[3], g[4], g[5]}, {g[6], g[7], g[8]}, prim_tri[i], prim_mat[i], (uint32_t)i};
   }
   std::vector<RefNode> nodes;
   ref_boxes.clear();
@@ -283,8 +289,10 @@ void build_sah(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, st
   if (n == 0) return;
   nodes.reserve(2 * n / kLeafSize + 8);
   build_node(nodes, prims, 0, n);
+  if (perm) perm->resize(n);
   for (size_t i = 0; i < n; i++) {
     const Prim& p = prims[i];
+    if (perm) (*perm)[i] = p.id;
     const float g[9] = {p.a.x, p.a.y, p.a.z, p.e1.x, p.e1.y, p.e1.z, p.e2.x, p.e2.y, p.e2.z};
     std::memcpy(&prim_geo[9 * i], g, sizeof(g));
     prim_tri[i] = p.tri;
@@ -440,7 +448,7 @@ struct Sah3Builder {
 }  // namespace
 
 void build_sah3(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, std::vector<uint16_t>& prim_mat,
-                std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab) {
+                std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab, std::vector<uint32_t>* perm) {
   const size_t n = prim_tri.size();
   ref_boxes.clear();
   ref_ab.clear();
@@ -463,7 +471,9 @@ void build_sah3(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, s
   std::vector<float> geo(prim_geo.size());
   std::vector<uint32_t> tri(n);
   std::vector<uint16_t> mat(n);
+  if (perm) perm->resize(n);
   for (size_t i = 0; i < n; i++) {
+    if (perm) (*perm)[i] = P[i].id;
     std::memcpy(&geo[9 * i], &prim_geo[9 * (size_t)P[i].id], 9 * sizeof(float));
     tri[i] = prim_tri[P[i].id];
     mat[i] = prim_mat[P[i].id];

@@ -42,15 +42,17 @@ struct MeshBuilder {
   void abox(const float mn[3], const float mx[3], uint32_t m);
 };
 
+// prim_vtx (optional): the exact vertices a, b, c of every primitive (9 floats).
 void tessellate(const float* pos, const uint32_t* idx, uint32_t n_tris, const uint16_t* tri_mat,
                 const float* tri_max_edge, std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri,
-                std::vector<uint16_t>& prim_mat);
+                std::vector<uint16_t>& prim_mat, std::vector<float>* prim_vtx = nullptr);
+// perm (optional): the tessellation index of the primitive at each leaf-order position.
 void build_sah(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, std::vector<uint16_t>& prim_mat,
-               std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab);
+               std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab, std::vector<uint32_t>* perm = nullptr);
 // Binned SAH over all three axes (128 bins, leaves <= 4), same output form as
 // build_sah; for walks under the near-tie rule, whose hit is tree-independent.
 void build_sah3(std::vector<float>& prim_geo, std::vector<uint32_t>& prim_tri, std::vector<uint16_t>& prim_mat,
-                std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab);
+                std::vector<float>& ref_boxes, std::vector<uint32_t>& ref_ab, std::vector<uint32_t>* perm = nullptr);
 // Returns the root ref; dev_nodes gets 16 floats per internal node.
 int32_t flatten_bvh2(const std::vector<float>& ref_boxes, const std::vector<uint32_t>& ref_ab,
                      std::vector<float>& dev_nodes);

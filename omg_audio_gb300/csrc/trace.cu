@@ -28,7 +28,7 @@ __device__ __forceinline__ bool walk_steps(Walk& w, const DScene& S, float ox, f
                                            float dy, float dz, int steps, bool wide, uint32_t* err) {
   if (TIE && wide && S.nodes4) return walk4_steps(w, S, ox, oy, oz, dx, dy, dz, steps, err);
   const float4* __restrict__ nodes = S.nodes;
-  const float4* __restrict__ prims = S.prims;
+  const float4* __restrict__ prims = S.prims;   // the first-found rule: the reference's test (no watertight context)
   if (!TIE) {
     // the reference's order: each node or leaf as it is reached
     while (steps-- > 0 && w.cur != kDone) {
@@ -140,7 +140,7 @@ __device__ __noinline__ void epoch_tally(const EpochArgs& ea, bool ended, bool p
 // WIDE (near-tie rule only): walks on the 4-wide tree. A template parameter,
 // not a runtime flag, so that each variant carries only its own walk: the
 // loop body is then small enough for the instruction cache.
-template <int NB, bool TIE, bool WIDE>
+template <int NB, bool TIE, bool WIDE, bool WT>
 __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
                                                        uint32_t total_rays, const DScene* __restrict__ scenes,
                                                        const DMat* __restrict__ job_mats,
@@ -279,14 +279,16 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
       if (!shade_now) {
         const bool wk = phase == WALK;
         const float4* lp = nullptr;
-        bool over = false;
+        bool over = false, lwt = false;
         if (wk) {
           const DScene& S = scenes[jobs[ji].scene];
-          lp = S.prims;
+          lwt = WT && S.prims_wt != nullptr;
+          lp = lwt ? S.prims_wt : S.prims;
           int st = walk_budget;
           over = walk_spec_nodes(w, S, px, py, pz, dx, dy, dz, st, err);
         }
-        coop_leaf_rounds(w, wk && !over, lp, px, py, pz, dx, dy, dz, s_slots[threadIdx.x >> 5], kCoopRounds, err);
+        coop_leaf_rounds<WT>(w, wk && !over, lp, lwt, px, py, pz, dx, dy, dz, s_slots[threadIdx.x >> 5],
+                             kCoopRounds, err);
         if (wk) {
           const DScene& S = scenes[jobs[ji].scene];
           // an ambiguous near-tie window: the walk starts over in fixed mode
@@ -548,7 +550,7 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
                          const DScene* scenes, const DMat* job_mats, const DPanel* panels,
                          const DPanelGroup* groups, float* acc, DLaunch* hdr,
                          uint32_t* job_segments, const LaunchShape& shape, int n_sms, bool tie, cudaStream_t s,
-                         const EpochArgs* ep) {
+                         const EpochArgs* ep, bool wt) {
   if (n_jobs == 0 || total_rays == 0) return cudaSuccess;
   EpochArgs ea{};
   if (ep) ea = *ep;
@@ -576,13 +578,17 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
     trace_wl_kernel<NB, TIE><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels,    \
                                                         groups, acc, hdr, job_segments, steps, wl_shade, wide, ea);  \
   else if (TIE && wide)                                                                                        \
-    trace_kernel<NB, TIE, true><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels,  \
-                                                           groups, acc, hdr, job_segments, refill, steps,        \
-                                                           shade_min, ea);                                       \
+    trace_kernel<NB, TIE, true, false><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats,   \
+                                                                  panels, groups, acc, hdr, job_segments, refill, \
+                                                                  steps, shade_min, ea);                          \
+  else if (TIE && wt)                                                                                          \
+    trace_kernel<NB, TIE, false, true><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats,   \
+                                                                  panels, groups, acc, hdr, job_segments, refill, \
+                                                                  steps, shade_min, ea);                          \
   else                                                                                                         \
-    trace_kernel<NB, TIE, false><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats, panels, \
-                                                            groups, acc, hdr, job_segments, refill, steps,       \
-                                                            shade_min, ea)
+    trace_kernel<NB, TIE, false, false><<<blocks, threads, 0, s>>>(jobs, n_jobs, total_rays, scenes, job_mats,  \
+                                                                   panels, groups, acc, hdr, job_segments, refill,\
+                                                                   steps, shade_min, ea)
   if (max_nb <= 3) {
     if (tie) OMG_TRACE_LAUNCH(3, true);
     else OMG_TRACE_LAUNCH(3, false);
@@ -597,10 +603,10 @@ cudaError_t launch_trace(const DJob* jobs, uint32_t n_jobs, uint32_t total_rays,
 cudaError_t preload_trace_kernels() {
   cudaFuncAttributes fa;
   cudaError_t e;
-  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<3, false, false>)) != cudaSuccess) return e;
-  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<3, true, false>)) != cudaSuccess) return e;
-  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<8, false, false>)) != cudaSuccess) return e;
-  return cudaFuncGetAttributes(&fa, trace_kernel<8, true, false>);
+  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<3, false, false, false>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<3, true, false, false>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&fa, trace_kernel<8, false, false, false>)) != cudaSuccess) return e;
+  return cudaFuncGetAttributes(&fa, trace_kernel<8, true, false, false>);
 }
 
 cudaError_t launch_finalize(const DJob* jobs, uint32_t n_jobs, const float* acc, float* out, uint64_t total_out,

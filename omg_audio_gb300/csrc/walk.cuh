@@ -132,9 +132,10 @@ __device__ __forceinline__ void walk_take_tie(Walk& w, const float4* __restrict_
   }
 }
 
-// One leaf of a near-tie walk, its primitives in order.
+// One leaf of a near-tie walk, its primitives in order (prims: the exact
+// vertices in watertight contexts, wt).
 __device__ __forceinline__ void walk_leaf_tie(Walk& w, const float4* __restrict__ prims, int leaf, float ox,
-                                              float oy, float oz, float dx, float dy, float dz) {
+                                              float oy, float oz, float dx, float dy, float dz, bool wt) {
   const uint32_t code = ~(uint32_t)leaf;
   const uint32_t start = code >> 3, end = start + (code & 7u) + 1u;
   for (uint32_t i = start; i < end; i++) {
@@ -142,7 +143,7 @@ __device__ __forceinline__ void walk_leaf_tie(Walk& w, const float4* __restrict_
     const float4 p1 = __ldg(prims + 3 * i + 1);
     const float4 p2 = __ldg(prims + 3 * i + 2);
     float t;
-    if (!ray_tri(p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) continue;
+    if (!tri_hit(wt, p0, p1, p2, ox, oy, oz, dx, dy, dz, t)) continue;
     walk_take_tie(w, prims, i, t, __float_as_uint(p2.w), __float_as_uint(p1.w));
   }
 }
@@ -174,8 +175,9 @@ __device__ __forceinline__ bool walk4_steps(Walk& w, const DScene& S, float ox, 
     ts.t_min = w.t_min;
     ts.amb = (w.flags & kWalkAmb) != 0u;
     ts.fixed = (w.flags & kWalkFixed) != 0u;
-    w.cur = bvh4_step(S.nodes4, S.prims, w.cur, ox, oy, oz, dx, dy, dz, w.ix, w.iy, w.iz, have, w.t_best, t_cull,
-                      pb, sb, tb, ts, w.stack_ref, w.stack_t, w.sp, err);
+    w.cur = bvh4_step(S.nodes4, S.prims_wt ? S.prims_wt : S.prims, w.cur, ox, oy, oz, dx, dy, dz, w.ix, w.iy, w.iz,
+                      have, w.t_best, t_cull, pb, sb, tb, ts, w.stack_ref, w.stack_t, w.sp, err,
+                      S.prims_wt != nullptr);
     w.prim_best = have ? pb : -1;
     w.t_min = ts.t_min;
     w.flags = (ts.amb ? kWalkAmb : 0u) | (ts.fixed ? kWalkFixed : 0u);
@@ -257,7 +259,8 @@ __device__ __forceinline__ bool walk_spec_nodes(Walk& w, const DScene& S, float 
 // postponed leaves one after another.
 __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, float oy, float oz, float dx,
                                           float dy, float dz, int steps, uint32_t* err) {
-  const float4* __restrict__ prims = S.prims;
+  const bool wt = S.prims_wt != nullptr;
+  const float4* __restrict__ prims = wt ? S.prims_wt : S.prims;
   if (walk_spec_nodes(w, S, ox, oy, oz, dx, dy, dz, steps, err)) return true;
   while (w.leaf < 0 && steps > 0) {
     steps--;
@@ -267,7 +270,7 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
       w.leaf = 0;
       return true;
     }
-    walk_leaf_tie(w, prims, w.leaf, ox, oy, oz, dx, dy, dz);
+    walk_leaf_tie(w, prims, w.leaf, ox, oy, oz, dx, dy, dz, wt);
     w.leaf = 0;
     if (w.cur < 0) {
       w.leaf = w.cur;
@@ -291,12 +294,16 @@ __device__ __forceinline__ bool walk_spec(Walk& w, const DScene& S, float ox, fl
 // so the near-tie state sees the sequence walk_leaf_tie would give it. After a
 // round, a walk whose next node is a leaf postpones it, and rounds repeat
 // while any lane holds a leaf (at most `rounds`).
-__device__ __forceinline__ void coop_leaf_rounds(Walk& w, bool own_walk, const float4* lane_prims, float ox,
-                                                 float oy, float oz, float dx, float dy, float dz,
+// WT: the warp may hold walks of watertight scenes (the owner's flag is then
+// read); false compiles the reference's test alone.
+template <bool WT>
+__device__ __forceinline__ void coop_leaf_rounds(Walk& w, bool own_walk, const float4* lane_prims, bool wt,
+                                                 float ox, float oy, float oz, float dx, float dy, float dz,
                                                  uint8_t* __restrict__ slots, int rounds, uint32_t* err) {
   const unsigned FULL = 0xffffffffu;
   const uint32_t lane = threadIdx.x & 31u;
-  const unsigned long long my_prims = reinterpret_cast<unsigned long long>(lane_prims);
+  // the owner's primitives, its watertight flag in bit 0 (the arrays are 16-byte aligned)
+  const unsigned long long my_prims = reinterpret_cast<unsigned long long>(lane_prims) | ((WT && wt) ? 1ull : 0ull);
   while (rounds-- > 0) {
     bool own = own_walk && w.leaf < 0;
     if (__ballot_sync(FULL, own) == 0u) break;
@@ -335,7 +342,8 @@ __device__ __forceinline__ void coop_leaf_rounds(Walk& w, bool own_walk, const f
       const uint32_t o_start = __shfl_sync(FULL, start, o), o_excl = __shfl_sync(FULL, excl, o);
       const float rx = __shfl_sync(FULL, ox, o), ry = __shfl_sync(FULL, oy, o), rz = __shfl_sync(FULL, oz, o);
       const float sx = __shfl_sync(FULL, dx, o), sy = __shfl_sync(FULL, dy, o), sz = __shfl_sync(FULL, dz, o);
-      const float4* P = reinterpret_cast<const float4*>(__shfl_sync(FULL, my_prims, o));
+      const unsigned long long op = __shfl_sync(FULL, my_prims, o);
+      const float4* P = reinterpret_cast<const float4*>(WT ? (op & ~1ull) : op);
       const uint32_t i = o_start + (p - o_excl);
       float t = 0.0f;
       bool hit = false;
@@ -344,7 +352,9 @@ __device__ __forceinline__ void coop_leaf_rounds(Walk& w, bool own_walk, const f
         const float4 p0 = __ldg(P + 3 * i + 0);
         const float4 p1 = __ldg(P + 3 * i + 1);
         const float4 p2 = __ldg(P + 3 * i + 2);
-        hit = ray_tri(p0, p1, p2, rx, ry, rz, sx, sy, sz, t);
+        // WT kernels serve watertight contexts, whose scenes all carry the exact vertices
+        hit = WT ? ray_tri_wt_body(p0, p1, p2, rx, ry, rz, sx, sy, sz, t)
+                 : ray_tri(p0, p1, p2, rx, ry, rz, sx, sy, sz, t);
         sid = __float_as_uint(p2.w);
         tri = __float_as_uint(p1.w);
       }

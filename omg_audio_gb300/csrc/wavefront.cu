@@ -230,12 +230,12 @@ cudaError_t launch_wavefront(const DJob* jobs, uint32_t n_jobs, uint32_t total_r
                              const DScene* scenes, const DMat* job_mats, const DPanel* panels,
                              const DPanelGroup* groups, float* acc, DLaunch* hdr, uint32_t* job_segments,
                              const WfState& st, uint32_t* ep_q, EpochCtl* ep_ctl, const LaunchShape& shape,
-                             int n_sms, bool tie, cudaStream_t s) {
+                             int n_sms, bool tie, cudaStream_t s, bool wt) {
   const bool staged = st.ctl && ep_q && ep_ctl && st.cap >= total_rays;
   const bool rounds = staged && shape.wf_iters > 0;
   if (!staged || (!rounds && shape.epochs == 0 && shape.mode == 0))
     return launch_trace(jobs, n_jobs, total_rays, max_nb, scenes, job_mats, panels, groups, acc, hdr, job_segments,
-                        shape, n_sms, tie, s);
+                        shape, n_sms, tie, s, nullptr, wt);
   if (n_jobs == 0 || total_rays == 0) return cudaSuccess;
   if (rounds) {
     cudaError_t e;
@@ -267,7 +267,7 @@ cudaError_t launch_wavefront(const DJob* jobs, uint32_t n_jobs, uint32_t total_r
     LaunchShape sk = shape;
     if (k > 0) sk.mode = shape.tail_mode;
     cudaError_t e = launch_trace(jobs, n_jobs, total_rays, max_nb, scenes, job_mats, panels, groups, acc, hdr,
-                                 job_segments, sk, n_sms, tie, s, &a);
+                                 job_segments, sk, n_sms, tie, s, &a, wt);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

@@ -44,12 +44,13 @@ class TraceConfig:
     tie_mode: int = 0          # 0: reference first-found; 1: lowest surface id among near-ties
     walk_budget: int = 0       # visits of one closest-hit walk before it stops (flag 4); 0: structural bound
     loop_guard: int = 0        # per-warp loop iterations of a persistent trace kernel (flag 8); 0: 2^22
+    tri_test: int = 0          # 0: the reference's Moller-Trumbore; 1: watertight (needs tie_mode 1)
 
     def to_c(self) -> _lib.omg_params:
         p = _lib.omg_params()
         for k in ("n_bands", "n_bins", "bin_dt", "max_time", "max_bounces", "energy_floor", "receiver_radius",
                   "wall_eps", "speed_of_sound", "dir_band", "device", "timeout_ms", "tie_mode", "walk_budget",
-                  "loop_guard"):
+                  "loop_guard", "tri_test"):
             setattr(p, k, getattr(self, k))
         return p
 

@@ -62,6 +62,7 @@ pub struct OmgParams {
     pub tie_mode: u32,
     pub walk_budget: u32,
     pub loop_guard: u32,
+    pub tri_test: u32,
 }
 
 #[repr(C)]
@@ -125,7 +126,7 @@ extern "C" {
 }
 
 /// The ABI version this binding was written against (OMG_ABI_VERSION).
-pub const ABI_VERSION: i32 = 2;
+pub const ABI_VERSION: i32 = 3;
 
 fn mat(m: &Material) -> OmgMaterial {
     let mut o = OmgMaterial::default();

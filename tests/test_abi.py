@@ -27,7 +27,7 @@ def test_bindings_cover_the_header(built_lib):
 
 def test_abi_version_and_status_strings(built_lib):
     from omg_audio_gb300 import _lib
-    assert built_lib.omg_abi_version() == 2
+    assert built_lib.omg_abi_version() == 3
     assert _lib.status_string(0) == "ok"
     assert _lib.status_string(_lib.E_TIMEOUT) == "timeout"
 
@@ -46,7 +46,7 @@ def test_params_default_are_reference_constants(built_lib):
 def test_struct_sizes_match_the_header(built_lib):
     from omg_audio_gb300 import _lib
     assert C.sizeof(_lib.omg_material) == 68
-    assert C.sizeof(_lib.omg_params) == 15 * 4
+    assert C.sizeof(_lib.omg_params) == 16 * 4
     assert C.sizeof(_lib.omg_panel) == 24 + 68
     assert C.sizeof(_lib.omg_reverb) == 3 * 32 + 8
     assert C.sizeof(_lib.omg_late_state) == 2 * 32 + 16 + 8
