@@ -28,7 +28,9 @@ int32_t wait_event(omg_ctx* ctx, cudaEvent_t ev, uint32_t timeout_ms) {
       ctx->last_error = "timeout waiting for the device";
       return OMG_E_TIMEOUT;
     }
-    std::this_thread::sleep_for(std::chrono::microseconds(20));
+    // a yielding spin: the calling thread waits for this result anyway, and a
+    // timed sleep would wake up tens of microseconds after the event
+    std::this_thread::yield();
   }
 }
 
