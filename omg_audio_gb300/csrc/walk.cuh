@@ -345,29 +345,31 @@ __device__ __forceinline__ void coop_leaf_rounds(Walk& w, bool own_walk, const f
       const unsigned long long op = __shfl_sync(FULL, my_prims, o);
       const float4* P = reinterpret_cast<const float4*>(WT ? (op & ~1ull) : op);
       const uint32_t i = o_start + (p - o_excl);
-      float t = 0.0f;
-      bool hit = false;
-      uint32_t sid = 0, tri = 0;
+      // the slot's hit distance, infinity for a miss
+      float t = __int_as_float(0x7f800000);
       if (act) {
         const float4 p0 = __ldg(P + 3 * i + 0);
         const float4 p1 = __ldg(P + 3 * i + 1);
         const float4 p2 = __ldg(P + 3 * i + 2);
+        float th;
         // WT kernels serve watertight contexts, whose scenes all carry the exact vertices
-        hit = WT ? ray_tri_wt_body(p0, p1, p2, rx, ry, rz, sx, sy, sz, t)
-                 : ray_tri(p0, p1, p2, rx, ry, rz, sx, sy, sz, t);
-        sid = __float_as_uint(p2.w);
-        tri = __float_as_uint(p1.w);
+        const bool hit = WT ? ray_tri_wt_body(p0, p1, p2, rx, ry, rz, sx, sy, sz, th)
+                            : ray_tri(p0, p1, p2, rx, ry, rz, sx, sy, sz, th);
+        if (hit) t = th;
       }
-      // each owner takes its slots of this chunk in leaf order
+      // each owner takes its slots of this chunk in leaf order: the distance
+      // from the slot's lane; its primitive (the owner's start + k) and that
+      // primitive's surface and triangle ids the owner reads itself, for hits
       for (uint32_t k = 0; k < kmax; k++) {
         const uint32_t q = excl + k;
         const bool mine = own && k < cnt && q >= base && q < base + 32u;
         const uint32_t src = mine ? q - base : lane;
         const float tk = __shfl_sync(FULL, t, src);
-        const bool hk = __shfl_sync(FULL, (uint32_t)hit, src) != 0u;
-        const uint32_t sk = __shfl_sync(FULL, sid, src), trk = __shfl_sync(FULL, tri, src);
-        const uint32_t ik = __shfl_sync(FULL, i, src);
-        if (mine && hk) walk_take_tie(w, lane_prims, ik, tk, sk, trk);
+        if (mine && tk < __int_as_float(0x7f800000)) {
+          const uint32_t ik = start + k;
+          const float* pw = reinterpret_cast<const float*>(lane_prims + 3 * ik);
+          walk_take_tie(w, lane_prims, ik, tk, __float_as_uint(__ldg(pw + 11)), __float_as_uint(__ldg(pw + 7)));
+        }
       }
     }
     __syncwarp();
