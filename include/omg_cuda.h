@@ -64,7 +64,8 @@ typedef struct omg_material {
  * 3 bands (lib.rs:22), direction band 1 (tracer.rs:123-125). */
 typedef struct omg_params {
     uint32_t n_bands;
-    uint32_t n_bins;
+    uint32_t n_bins;             /* at most 19,370 for the reverb estimate (one band's curve in shared
+                                    memory); calls with more return an error */
     float bin_dt;
     float max_time;
     uint32_t max_bounces;

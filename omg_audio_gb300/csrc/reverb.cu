@@ -1,7 +1,9 @@
 // estimate_reverb on the GPU (crates/omg-core/src/tracer.rs:204-257): one warp
 // per (echogram, band). FP64 is used only here, for the Schroeder backward
 // integral and the line fit. The late level is the reference's own f32 sum of
-// the bins from 80 ms on, in its order (tracer.rs:246-254), by one lane.
+// the bins from 80 ms on, in its order (tracer.rs:246-254), by one lane. The
+// warp first stages the band's bins in shared memory (coalesced loads), so the
+// sequential sums read shared memory instead of waiting on one load each.
 #include <cfloat>
 
 #include "omg_internal.h"
@@ -15,8 +17,10 @@ __device__ __forceinline__ double db_of(double e, double total) {
 }
 
 __global__ void reverb_kernel(const DReverbJob* __restrict__ rj, uint32_t n_jobs, const float* __restrict__ bins,
-                              omg_reverb* __restrict__ out, const uint32_t* __restrict__ job_segments) {
-  extern __shared__ double edc[];
+                              omg_reverb* __restrict__ out, const uint32_t* __restrict__ job_segments,
+                              uint32_t max_bins) {
+  extern __shared__ double edc[];           // max_bins doubles, then the band's bins (max_bins floats)
+  float* sb = reinterpret_cast<float*>(edc + max_bins);
   const uint32_t j = blockIdx.x, b = blockIdx.y;
   const DReverbJob R = rj[j];
   const uint32_t lane = threadIdx.x;
@@ -31,13 +35,15 @@ __global__ void reverb_kernel(const DReverbJob* __restrict__ rj, uint32_t n_jobs
   }
   const uint32_t n = R.n_bins, nb = R.nb;
   const float* B = bins + R.bins_off;
+  for (uint32_t i = lane; i < n; i += 32) sb[i] = B[(uint64_t)i * nb + b];
+  __syncwarp();
   // per-lane contiguous chunk, sequential backward sum, then a suffix scan of
   // the chunk totals across the warp
   const uint32_t chunk = (n + 31) / 32;
   const uint32_t lo = lane * chunk, hi = min(n, lo + chunk);
   double run = 0.0;
   for (int64_t i = (int64_t)hi - 1; i >= (int64_t)lo; i--) {
-    run += (double)B[(uint64_t)i * nb + b];
+    run += (double)sb[i];
     edc[i] = run;
   }
   // exclusive suffix of chunk totals: sum over lanes > lane
@@ -107,7 +113,7 @@ __global__ void reverb_kernel(const DReverbJob* __restrict__ rj, uint32_t n_jobs
     const float q = 0.080f / R.bin_dt;
     const uint64_t ls = (q >= 0.0f) ? (uint64_t)q : 0;
     float late = 0.0f;
-    for (uint64_t i = ls; i < n; i++) late += B[i * nb + b];
+    for (uint64_t i = ls; i < n; i++) late += sb[i];
     out[j].level[b] = fminf(sqrtf(late), 0.7f);
     if (b == 0) out[j].segments = job_segments ? job_segments[j] : 0;
   }
@@ -118,13 +124,14 @@ __global__ void reverb_kernel(const DReverbJob* __restrict__ rj, uint32_t n_jobs
 cudaError_t launch_reverb(const DReverbJob* rj, uint32_t n_jobs, uint32_t max_bins, const float* bins,
                           omg_reverb* out, const uint32_t* job_segments, cudaStream_t s) {
   if (n_jobs == 0) return cudaSuccess;
-  size_t smem = (size_t)max_bins * sizeof(double);
+  size_t smem = (size_t)max_bins * (sizeof(double) + sizeof(float));
+  if (smem > 227 * 1024) return cudaErrorInvalidValue;   // more than 19,370 bins: beyond a block's shared memory
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(reverb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
   dim3 grid(n_jobs, OMG_MAX_BANDS);
-  reverb_kernel<<<grid, 32, smem, s>>>(rj, n_jobs, bins, out, job_segments);
+  reverb_kernel<<<grid, 32, smem, s>>>(rj, n_jobs, bins, out, job_segments, max_bins);
   return cudaGetLastError();
 }
 
