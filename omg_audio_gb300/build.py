@@ -59,7 +59,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                      "-Xcompiler", "-fPIC", *inc, "-c", os.path.join(CSRC, f), "-o", obj])
     for f in CPP_SOURCES:
         obj = os.path.join(BUILD, f + ".o")
-        jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
+        jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wall", "-Wno-unused-function",
                      "-I", os.path.join(CUDA_HOME, "include"), *inc, "-c", os.path.join(CSRC, f), "-o", obj])
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         outs = list(ex.map(_run, jobs))
@@ -68,7 +68,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             sys.stderr.write(o)
     objs = [os.path.join(BUILD, f + ".o") for f in CU_SOURCES + CPP_SOURCES]
     tmp = LIB + ".tmp"
-    _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lrt", "-lpthread", "-ldl"])
+    _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lrt", "-lpthread", "-ldl", "-lgomp"])
     os.replace(tmp, LIB)
     # ptxas register / spill report for the record
     with open(os.path.join(BUILD, "ptxas.txt"), "w") as fh:
