@@ -9,7 +9,8 @@ on f32 operations the device repeats exactly, so the two trees must be equal:
   - traces over the two trees under the near-tie rule: identical segment
     counts and bit-identical echograms.
 Scenes: the 12-triangle shoebox (one block builds the whole tree), the
-40-room scene (large-node levels, then blocks), a random triangle soup, and
+40-room scene (large-node levels, then blocks), the 1 M-triangle city (1.94 M
+primitives, 13 large-node levels), a random triangle soup, and
 a degenerate scene whose 6000 triangles share (or nearly share, within 4e-7)
 one centre, so that nodes of more than 2048 and of fewer primitives fall back
 to object-median splits (host: nth_element by centre and index).
@@ -77,6 +78,7 @@ def _rows_by_leaf(ex):
 SCENES = {
     "shoebox12": lambda: ("recorder", W.shoebox12(seed=1).recorder),
     "multiroom": lambda: ("recorder", W.multiroom().recorder),
+    "city": lambda: ("recorder", W.city(seed=5).recorder),
     "soup": lambda: ("mesh", _soup(20000, 1)),
     "coincident": lambda: ("mesh", _coincident(3000, 3000, 500, 2)),
 }
