@@ -390,8 +390,11 @@ def surrogate_leg(args, device, city=None):
         cj, city_sweep = None, []
         if len(aj):
             rj = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, rooms.take(aj), jr, seed=33)[0], 0.001))
+            rj2 = S.rt60_from_edc(S.edc_db(S.trace_rooms(ctx, rooms.take(aj), jr, seed=34)[0], 0.001))
             ej = np.abs(crt_p[aj] / rj - 1.0)
-            cj = {"pairs": int(len(aj)), "median": q(ej, 50), "p90": q(ej, 90)}
+            ejj = np.abs(rj2 / rj - 1.0)
+            cj = {"pairs": int(len(aj)), "median": q(ej, 50), "p90": q(ej, 90),
+                  "judge_vs_judge_other_seed": {"median": q(ejj, 50), "p90": q(ejj, 90)}}
             # the spread gate swept on the judged pairs, with the tracer's time
             # for the pairs each gate sends back
             tr_pair = t_all / len(rooms)
