@@ -914,7 +914,7 @@ def main():
     ap.add_argument("--early-listeners", type=int, default=8,
                     help="listeners of the world early-reflection leg (0 skips it)")
     ap.add_argument("--surrogate-rooms", type=int, default=131072, help="training rooms (1 M: the full config)")
-    ap.add_argument("--surrogate-epochs", type=int, default=60)
+    ap.add_argument("--surrogate-epochs", type=int, default=120)
     ap.add_argument("--surrogate-test", type=int, default=16384, help="held-out rooms")
     ap.add_argument("--surrogate-train-rays", type=int, default=8192,
                     help="tracer rays per training room (the labels' Monte-Carlo noise is the loss floor)")
