@@ -64,8 +64,9 @@ typedef struct omg_material {
  * 3 bands (lib.rs:22), direction band 1 (tracer.rs:123-125). */
 typedef struct omg_params {
     uint32_t n_bands;
-    uint32_t n_bins;             /* at most 19,370 for the reverb estimate (one band's curve in shared
-                                    memory); calls with more return an error */
+    uint32_t n_bins;             /* at most 19,370 (the reverb estimate holds one band's curve in
+                                    shared memory): omg_create, a job or omg_estimate_reverb asking
+                                    for more is refused (NULL / OMG_E_INVALID) */
     float bin_dt;
     float max_time;
     uint32_t max_bounces;

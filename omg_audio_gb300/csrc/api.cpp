@@ -187,7 +187,7 @@ int32_t fill_batch(omg_ctx* ctx, BatchRec& B, const omg_job* jobs, uint32_t n_jo
     uint32_t nb = j.n_bands ? j.n_bands : P.n_bands;
     uint32_t n_bins = j.n_bins ? j.n_bins : P.n_bins;
     float max_time = j.max_time > 0.0f ? j.max_time : P.max_time;
-    if (nb == 0 || nb > (uint32_t)MAXB || n_bins == 0 || j.n_rays == 0) return OMG_E_INVALID;
+    if (nb == 0 || nb > (uint32_t)MAXB || n_bins == 0 || n_bins > kMaxBins || j.n_rays == 0) return OMG_E_INVALID;
     if (P.dir_band >= nb) return OMG_E_INVALID;
     if (!finite3(j.src) || !finite3(j.lis)) return OMG_E_INVALID;
     if ((uint64_t)j.panel_offset + j.n_panels > n_panels) return OMG_E_INVALID;
@@ -600,7 +600,8 @@ omg_ctx* omg_create(const omg_params* p) {
   omg_params prm;
   if (p) prm = *p;
   else omg_params_default(&prm);
-  if (prm.n_bands == 0 || prm.n_bands > OMG_MAX_BANDS || prm.n_bins == 0 || !(prm.bin_dt > 0.0f) ||
+  if (prm.n_bands == 0 || prm.n_bands > OMG_MAX_BANDS || prm.n_bins == 0 || prm.n_bins > kMaxBins ||
+      !(prm.bin_dt > 0.0f) ||
       prm.dir_band >= prm.n_bands || !(prm.speed_of_sound > 0.0f) ||
       (prm.tri_test != OMG_TRI_REFERENCE && prm.tri_test != OMG_TRI_WATERTIGHT) ||
       (prm.tri_test == OMG_TRI_WATERTIGHT && prm.tie_mode != 1))

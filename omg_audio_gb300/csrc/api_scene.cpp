@@ -426,7 +426,8 @@ int32_t omg_raycast(omg_ctx* ctx, uint32_t id, const float* o, const float* d, u
 // ------------------------------------------------------------------ reverb
 int32_t omg_estimate_reverb(omg_ctx* ctx, const float* bins, uint32_t n_bins, uint32_t nb, float bin_dt,
                             uint32_t n_jobs, omg_reverb* out) {
-  if (!ctx || !bins || !out || !n_bins || !nb || nb > (uint32_t)MAXB || !n_jobs || !(bin_dt > 0.0f))
+  if (!ctx || !bins || !out || !n_bins || n_bins > kMaxBins || !nb || nb > (uint32_t)MAXB || !n_jobs ||
+      !(bin_dt > 0.0f))
     return OMG_E_INVALID;
   uint64_t per = (uint64_t)n_bins * nb, total = per * n_jobs;
   if (ctx->r_bins.n < total) CK(ctx->r_bins.alloc(total));

@@ -25,7 +25,10 @@
 namespace omg {
 
 constexpr int MAXB = OMG_MAX_BANDS;
-constexpr int STACK_DEPTH = 64;           // mesh.rs:492 (64-entry traversal stack)
+constexpr int STACK_DEPTH = 64;
+// Histogram bins of one echogram at most: the reverb estimate holds one band's
+// curve (an FP64 and an f32 value a bin) in a block's 227 KB of shared memory.
+constexpr uint32_t kMaxBins = 19370;           // mesh.rs:492 (64-entry traversal stack)
 
 // tracer.rs:148-182 per material: p = clamp(max_b T_b^2, 0.02, 0.5) when
 // > 1e-5 else 0; transmitted weight T_b^2 / p; reflected weight

@@ -9,8 +9,9 @@ histograms within 1e-5 per bin on bins holding >= 1e-6 of the band total):
 - a shoebox job whose source lies outside the box (the ray is transmitted out:
   scene.rs:41-47 returns no hit);
 - a listener at the source;
-- invalid requests (a job without rays, alone or in a batch) rejected with OMG_E_INVALID, the context
-  still usable afterwards;
+- invalid requests (a job without rays, alone or in a batch; bin counts above
+  the reverb estimate's bound) rejected with OMG_E_INVALID, the context still
+  usable afterwards;
 - a host wait that runs out (OMG_E_TIMEOUT) while the batch keeps running, and a
   later read of the finished batch.
 """
@@ -96,6 +97,27 @@ def test_invalid_requests_are_rejected(ctx):
                          Job((1, 1, 1), (2, 2, 2), 0, box_size=(6, 4, 3), box_walls=walls)])
     e, rv = ctx.trace_box((6, 4, 3), walls, (1, 1, 1), (2, 2, 2), 256, seed=1)   # still usable
     assert rv.segments >= 256 and np.isfinite(e.bins).all()
+
+
+def test_bin_counts_above_the_reverb_bound_are_refused(ctx):
+    """A bin count above 19,370 (the reverb estimate holds one band's curve in
+    a block's 227 KB of shared memory) is refused up front: omg_create returns
+    NULL, a job and an omg_estimate_reverb call get OMG_E_INVALID. The bound
+    itself works, and the context stays usable."""
+    with pytest.raises(Exception):
+        Context(TraceConfig(n_bins=19371))
+    walls = [M.CONCRETE] * 6
+    with pytest.raises(_lib.OmgError) as ex:
+        ctx.trace_batch([Job((1, 1, 1), (2, 2, 2), 64, box_size=(6, 4, 3), box_walls=walls, n_bins=19371)])
+    assert ex.value.status == _lib.E_INVALID
+    with pytest.raises(_lib.OmgError) as ex:
+        ctx.estimate_reverb(np.ones((19371, 3), np.float32))
+    assert ex.value.status == _lib.E_INVALID
+    bins = np.exp(-np.arange(19370, dtype=np.float64) / 2000.0)[:, None].repeat(3, 1).astype(np.float32)
+    rv = ctx.estimate_reverb(bins, bin_dt=0.001)
+    assert np.all(np.isfinite(rv.rt60)) and np.all(rv.rt60 > 0)
+    e, rv2 = ctx.trace_box((6, 4, 3), walls, (1, 1, 1), (2, 2, 2), 256, seed=1)   # still usable
+    assert rv2.segments >= 256
 
 
 def test_host_wait_times_out_and_the_context_stays_usable(oracle):
