@@ -140,6 +140,14 @@ __device__ __noinline__ void epoch_tally(const EpochArgs& ea, bool ended, bool p
 // WIDE (near-tie rule only): walks on the 4-wide tree. A template parameter,
 // not a runtime flag, so that each variant carries only its own walk: the
 // loop body is then small enough for the instruction cache.
+//
+// Registers: the launch bound (256, 4) caps a thread at 64. Across the loop a
+// lane keeps only what the walk reads (the ray, its job, the walk state); the
+// segment's hit is computed in the shading pass from the walk's result, and
+// the state that only the refill and the shading pass touch (energies,
+// distance, stream, segment count, ray id) lives in shared memory, a column
+// per thread. The near-tie kernel then has 16 bytes of spill stores, against
+// 184 with that state in registers.
 template <int NB, bool TIE, bool WIDE, bool WT>
 __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
                                                        uint32_t total_rays, const DScene* __restrict__ scenes,
@@ -156,21 +164,20 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
   enum { IDLE = 0, WALK = 1, SHADE = 2 };
   int phase = IDLE;
   bool exhausted = false;
-  uint32_t ji = 0, rid = 0;
-  float px = 0, py = 0, pz = 0, dx = 0, dy = 0, dz = 0, dist = 0;
-  float e[NB];
-#pragma unroll
-  for (int b = 0; b < NB; b++) e[b] = 0.0f;
-  Pcg rng;
-  rng.s = 0;
-  uint32_t bounce = 0, segs = 0;
+  uint32_t ji = 0;
+  float px = 0, py = 0, pz = 0, dx = 0, dy = 0, dz = 0;
+  // the ray's state that only the refill and the shading pass touch, a column
+  // per thread in shared memory rather than registers across the walk:
+  // energies, distance travelled, stream, segments so far, ray id
+  __shared__ float s_e[NB][kMaxWarps * 32];
+  __shared__ float s_dist[kMaxWarps * 32];
+  __shared__ uint32_t s_rng[kMaxWarps * 32], s_bounce[kMaxWarps * 32], s_rid[kMaxWarps * 32];
+  const uint32_t me = threadIdx.x;
   int walk_stack_ref[STACK_DEPTH];
   float walk_stack_t[STACK_DEPTH];
   Walk w;
   w.stack_ref = walk_stack_ref;
   w.stack_t = walk_stack_t;
-  Hit h;
-  bool have = false;
   uint32_t* err = &hdr->error;
   const WfState& rs = ea.st;
   const uint32_t* rq = ea.in_q;
@@ -182,12 +189,10 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
   uint32_t iters = 0;   // loop guard (warp-uniform: every lane runs every iteration)
   __shared__ uint8_t s_slots[kMaxWarps][256];   // coop_leaf_rounds' slot lists, one per warp
 
-  // begin one segment from (p, d): the box hit directly, or a mesh walk
+  // begin one segment from (p, d): a mesh walk, or (a shoebox) the shading
+  // pass at once, which computes the box hit
   auto begin_segment = [&](const DJob& J) {
     if (J.geom == OMG_GEOM_BOX) {
-      h.t = FLT_MAX;
-      h.m = nullptr;
-      have = box_hit(J, job_mats, px, py, pz, dx, dy, dz, h);
       phase = SHADE;
     } else {
       walk_begin<TIE>(w, scenes[J.scene], px, py, pz, dx, dy, dz, wide);
@@ -211,31 +216,34 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
         const uint32_t k = base + (uint32_t)__popc(idle & lt_mask);
         if (k < n_rays) {
           if (rq) {
-            rid = rq[k];
+            const uint32_t rid = rq[k];
             ji = find_job(jobs, n_jobs, rid);
             const float4 P = rs.pos[rid], D = rs.dir[rid];
-            px = P.x; py = P.y; pz = P.z; dist = P.w;
+            px = P.x; py = P.y; pz = P.z;
             dx = D.x; dy = D.y; dz = D.z;
-            rng.s = __float_as_uint(D.w);
             const float4 e0 = rs.e[rid];
             const float4 e1 = NB > 4 ? rs.e[rs.cap + rid] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             const float ev[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
 #pragma unroll
-            for (int b = 0; b < NB; b++) e[b] = ev[b];
-            bounce = rs.bounce[rid];
-            segs = bounce;
+            for (int b = 0; b < NB; b++) s_e[b][me] = ev[b];
+            s_dist[me] = P.w;
+            s_rng[me] = __float_as_uint(D.w);
+            s_bounce[me] = rs.bounce[rid];
+            s_rid[me] = rid;
           } else {
-            rid = k;
+            const uint32_t rid = k;
             ji = find_job(jobs, n_jobs, rid);
             const DJob& J = jobs[ji];
+            Pcg rng;
             rng.init(J.seed, rid - J.ray_base);
             unit_sphere(rng, dx, dy, dz);
             px = J.src[0]; py = J.src[1]; pz = J.src[2];
 #pragma unroll
-            for (int b = 0; b < NB; b++) e[b] = J.e0[b];
-            dist = 0.0f;
-            bounce = 0;
-            segs = 0;
+            for (int b = 0; b < NB; b++) s_e[b][me] = J.e0[b];
+            s_dist[me] = 0.0f;
+            s_rng[me] = rng.s;
+            s_bounce[me] = 0u;
+            s_rid[me] = rid;
           }
           begin_segment(jobs[ji]);
         }
@@ -255,24 +263,8 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
     const unsigned ready = __ballot_sync(FULL, phase == SHADE);
     const bool shade_now = ready != 0u && (walking == 0u || __popc(ready) >= (int)shade_min);
 
-    // ---- closest-hit walk, at most walk_budget steps this iteration
-    // the walk is over: its hit (normal of the original triangle, against d)
-    auto finish_walk = [&](const DScene& S) {
-      have = walk_have(w);
-      h.t = FLT_MAX;
-      h.m = nullptr;
-      if (have) {
-        const float4 p0 = __ldg(S.prims + 3 * w.prim_best + 0);
-        const float4 p1 = __ldg(S.prims + 3 * w.prim_best + 1);
-        const float4 nn = __ldg(S.normals + __float_as_uint(p1.w));
-        float nx = nn.x, ny = nn.y, nz = nn.z;
-        if (nx * dx + ny * dy + nz * dz > 0.0f) { nx = nx * -1.0f; ny = ny * -1.0f; nz = nz * -1.0f; }
-        h.t = w.t_best;
-        h.nx = nx; h.ny = ny; h.nz = nz;
-        h.m = S.mats + __float_as_uint(p0.w);
-      }
-      phase = SHADE;
-    };
+    // ---- closest-hit walk, at most walk_budget steps this iteration; a lane
+    // whose walk is over waits to shade, its result kept in w until then
     if (TIE && !wide) {
       // near-tie walks on the binary tree: the node phase lane by lane, then
       // the pending leaves tested by the whole warp together
@@ -293,27 +285,55 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
           const DScene& S = scenes[jobs[ji].scene];
           // an ambiguous near-tie window: the walk starts over in fixed mode
           if (!over && w.cur == kDone && w.leaf == 0) over = !walk_restart_fixed(w, S.root, S.walk_budget);
-          if (over) finish_walk(S);
+          if (over) phase = SHADE;
         }
       }
     } else if (!shade_now && phase == WALK) {
       const DJob& J = jobs[ji];
       const DScene& S = scenes[J.scene];
-      if (walk_steps<TIE>(w, S, px, py, pz, dx, dy, dz, walk_budget, wide, err)) finish_walk(S);
+      if (walk_steps<TIE>(w, S, px, py, pz, dx, dy, dz, walk_budget, wide, err)) phase = SHADE;
     }
 
     // ---- one segment of the bounce loop (tracer.rs:103-200)
     bool ended = false, parked = false;
     if (shade_now && phase == SHADE) {
       const DJob& J = jobs[ji];
+      // the segment's closest hit: the shoebox's, or the walk's (normal of
+      // the original triangle, against d)
+      Hit h;
+      h.t = FLT_MAX;
+      h.m = nullptr;
+      bool have;
+      if (J.geom == OMG_GEOM_BOX) {
+        have = box_hit(J, job_mats, px, py, pz, dx, dy, dz, h);
+      } else {
+        const DScene& S = scenes[J.scene];
+        have = walk_have(w);
+        if (have) {
+          const float4 p0 = __ldg(S.prims + 3 * w.prim_best + 0);
+          const float4 p1 = __ldg(S.prims + 3 * w.prim_best + 1);
+          const float4 nn = __ldg(S.normals + __float_as_uint(p1.w));
+          float nx = nn.x, ny = nn.y, nz = nn.z;
+          if (nx * dx + ny * dy + nz * dz > 0.0f) { nx = nx * -1.0f; ny = ny * -1.0f; nz = nz * -1.0f; }
+          h.t = w.t_best;
+          h.nx = nx; h.ny = ny; h.nz = nz;
+          h.m = S.mats + __float_as_uint(p0.w);
+        }
+      }
       if (J.n_groups) have = panels_hit(J, panels, groups, job_mats, px, py, pz, dx, dy, dz, have, h);
-      segs++;
       const float t_hit = have ? h.t : FLT_MAX;
+      float e[NB];
+#pragma unroll
+      for (int b = 0; b < NB; b++) e[b] = s_e[b][me];
+      float dist = s_dist[me];
+      Pcg rng;
+      rng.s = s_rng[me];
+      uint32_t bounce = s_bounce[me];
       bool done = shade_segment<NB>(J, acc, h, have, t_hit, px, py, pz, dx, dy, dz, dist, e, rng);
       bounce++;
       if (!done && bounce >= J.max_bounces) done = true;
       if (done) {
-        atomicAdd(job_segments + ji, segs);
+        atomicAdd(job_segments + ji, bounce);
         phase = IDLE;
         ended = true;
       } else if (parking) {
@@ -321,14 +341,19 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
         Bands<NB> eb;
 #pragma unroll
         for (int b = 0; b < NB; b++) eb.v[b] = e[b];
-        park_ray<NB>(rs, rid, px, py, pz, dist, dx, dy, dz, rng.s, eb, bounce);
+        park_ray<NB>(rs, s_rid[me], px, py, pz, dist, dx, dy, dz, rng.s, eb, bounce);
         phase = IDLE;
         parked = true;
       } else {
+#pragma unroll
+        for (int b = 0; b < NB; b++) s_e[b][me] = e[b];
+        s_dist[me] = dist;
+        s_rng[me] = rng.s;
+        s_bounce[me] = bounce;
         begin_segment(J);
       }
     }
-    if (ea.cur) epoch_tally(ea, ended, parked, rid, may_park, n_rays, keep, fetch);
+    if (ea.cur) epoch_tally(ea, ended, parked, s_rid[me], may_park, n_rays, keep, fetch);
   }
 }
 

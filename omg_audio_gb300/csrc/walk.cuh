@@ -20,9 +20,8 @@ struct Walk {
   int prim_best;     // the winner so far (-1: no hit yet)
   float t_best;
   float t_min;       // TIE: exact nearest hit so far (FLT_MAX: none); the window is t_min (1 + 1e-6)
-  uint32_t flags;    // TIE: kWalkAmb, kWalkFixed (TieState, device_common.cuh)
+  uint32_t flags;    // TIE: kWalkAmb, kWalkFixed (TieState, device_common.cuh); kWalkFast
   float ix, iy, iz;
-  bool fast;         // the fused multiply-add slab test applies (origin within the margin, no d_a near 0)
   uint32_t budget;
   int* stack_ref;
   float* stack_t;
@@ -32,6 +31,8 @@ struct Walk {
 // bound is recomputed from t_min): the walk's scalars live in registers next
 // to the ray's, under the persistent kernels' 64-register cap.
 constexpr uint32_t kWalkAmb = 1u, kWalkFixed = 2u;
+// the fused multiply-add slab test applies (origin within the margin, no d_a near 0)
+constexpr uint32_t kWalkFast = 4u;
 
 __device__ __forceinline__ bool walk_have(const Walk& w) { return w.prim_best >= 0; }
 
@@ -68,15 +69,15 @@ __device__ __forceinline__ void walk_begin(Walk& w, const DScene& S, float ox, f
   w.prim_best = -1;
   w.t_best = FLT_MAX;
   w.t_min = FLT_MAX;
-  w.flags = 0u;
   w.ix = __frcp_rn(dx);
   w.iy = __frcp_rn(dy);
   w.iz = __frcp_rn(dz);
   // the margin 2^-19 M_a covers the fma slab test's rounding for |o_a| <= 7 M_a;
   // the test also needs finite products (no direction component near 0)
   const float kTiny = 8.673617379884035e-19f;   // 2^-60
-  w.fast = fabsf(ox) <= 7.0f * S.fast_m[0] && fabsf(oy) <= 7.0f * S.fast_m[1] && fabsf(oz) <= 7.0f * S.fast_m[2] &&
-           fabsf(dx) >= kTiny && fabsf(dy) >= kTiny && fabsf(dz) >= kTiny;
+  const bool fast = fabsf(ox) <= 7.0f * S.fast_m[0] && fabsf(oy) <= 7.0f * S.fast_m[1] &&
+                    fabsf(oz) <= 7.0f * S.fast_m[2] && fabsf(dx) >= kTiny && fabsf(dy) >= kTiny && fabsf(dz) >= kTiny;
+  w.flags = fast ? kWalkFast : 0u;
   w.budget = S.walk_budget;
 }
 
@@ -180,7 +181,7 @@ __device__ __forceinline__ bool walk4_steps(Walk& w, const DScene& S, float ox, 
                       S.prims_wt != nullptr);
     w.prim_best = have ? pb : -1;
     w.t_min = ts.t_min;
-    w.flags = (ts.amb ? kWalkAmb : 0u) | (ts.fixed ? kWalkFixed : 0u);
+    w.flags = (w.flags & kWalkFast) | (ts.amb ? kWalkAmb : 0u) | (ts.fixed ? kWalkFixed : 0u);
   }
   if (w.cur == kDone) walk_restart_fixed(w, S.root4, S.walk_budget);
   return w.cur == kDone;
@@ -212,7 +213,7 @@ __device__ __forceinline__ bool walk_spec_nodes(Walk& w, const DScene& S, float 
     const float tmax = walk_cull<true>(w);   // infinite before the first hit; the final window in fixed mode
     float ta, tb;
     bool h0, h1;
-    if (w.fast) {
+    if (w.flags & kWalkFast) {
       const float oix = ox * w.ix, oiy = oy * w.iy, oiz = oz * w.iz;
       h0 = ray_aabb_fma(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, oix, oiy, oiz, w.ix, w.iy, w.iz, tmax, ta);
       h1 = ray_aabb_fma(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, oix, oiy, oiz, w.ix, w.iy, w.iz, tmax, tb);
