@@ -145,9 +145,9 @@ __device__ __noinline__ void epoch_tally(const EpochArgs& ea, bool ended, bool p
 // lane keeps only what the walk reads (the ray, its job, the walk state); the
 // segment's hit is computed in the shading pass from the walk's result, and
 // the state that only the refill and the shading pass touch (energies,
-// distance, stream, segment count, ray id) lives in shared memory, a column
-// per thread. The near-tie kernel then has 16 bytes of spill stores, against
-// 184 with that state in registers.
+// distance, stream, segment count, ray id) lives, for up to 4 bands, in shared
+// memory, a column per thread. The 3-band near-tie kernel then has 16 bytes of
+// spill stores, against 184 with that state in registers.
 template <int NB, bool TIE, bool WIDE, bool WT>
 __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ jobs, uint32_t n_jobs,
                                                        uint32_t total_rays, const DScene* __restrict__ scenes,
@@ -166,13 +166,48 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
   bool exhausted = false;
   uint32_t ji = 0;
   float px = 0, py = 0, pz = 0, dx = 0, dy = 0, dz = 0;
-  // the ray's state that only the refill and the shading pass touch, a column
-  // per thread in shared memory rather than registers across the walk:
-  // energies, distance travelled, stream, segments so far, ray id
-  __shared__ float s_e[NB][kMaxWarps * 32];
-  __shared__ float s_dist[kMaxWarps * 32];
-  __shared__ uint32_t s_rng[kMaxWarps * 32], s_bounce[kMaxWarps * 32], s_rid[kMaxWarps * 32];
-  const uint32_t me = threadIdx.x;
+  // the ray's state that only the refill and the shading pass touch
+  // (energies, distance travelled, stream, segments so far, ray id): for up to
+  // 4 bands a column per thread in shared memory, so that it holds no
+  // registers across the walk; for 8 bands in registers (there the shared
+  // copy's loads and stores in every shading pass cost more than it saves)
+  constexpr bool kColdShared = NB <= 4;
+  constexpr int kCols = kColdShared ? kMaxWarps * 32 : 1;
+  __shared__ float s_e[kColdShared ? NB : 1][kCols];
+  __shared__ float s_dist[kCols];
+  __shared__ uint32_t s_rng[kCols], s_bounce[kCols], s_rid[kCols];
+  const uint32_t me = kColdShared ? threadIdx.x : 0u;
+  float r_e[NB];
+  float r_dist = 0.0f;
+  uint32_t r_rng = 0, r_bounce = 0, r_rid = 0;
+  auto cold_save = [&](const float* ev, float dist, uint32_t rng_s, uint32_t bounce) {
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+      if constexpr (kColdShared) s_e[b][me] = ev[b];
+      else r_e[b] = ev[b];
+    }
+    if constexpr (kColdShared) {
+      s_dist[me] = dist;
+      s_rng[me] = rng_s;
+      s_bounce[me] = bounce;
+    } else {
+      r_dist = dist;
+      r_rng = rng_s;
+      r_bounce = bounce;
+    }
+  };
+  auto cold_load = [&](float* ev, float& dist, uint32_t& rng_s, uint32_t& bounce) {
+#pragma unroll
+    for (int b = 0; b < NB; b++) ev[b] = kColdShared ? s_e[b][me] : r_e[b];
+    dist = kColdShared ? s_dist[me] : r_dist;
+    rng_s = kColdShared ? s_rng[me] : r_rng;
+    bounce = kColdShared ? s_bounce[me] : r_bounce;
+  };
+  auto cold_set_rid = [&](uint32_t rid) {
+    if constexpr (kColdShared) s_rid[me] = rid;
+    else r_rid = rid;
+  };
+  auto cold_rid = [&]() { return kColdShared ? s_rid[me] : r_rid; };
   int walk_stack_ref[STACK_DEPTH];
   float walk_stack_t[STACK_DEPTH];
   Walk w;
@@ -224,12 +259,8 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
             const float4 e0 = rs.e[rid];
             const float4 e1 = NB > 4 ? rs.e[rs.cap + rid] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             const float ev[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
-#pragma unroll
-            for (int b = 0; b < NB; b++) s_e[b][me] = ev[b];
-            s_dist[me] = P.w;
-            s_rng[me] = __float_as_uint(D.w);
-            s_bounce[me] = rs.bounce[rid];
-            s_rid[me] = rid;
+            cold_save(ev, P.w, __float_as_uint(D.w), rs.bounce[rid]);
+            cold_set_rid(rid);
           } else {
             const uint32_t rid = k;
             ji = find_job(jobs, n_jobs, rid);
@@ -238,12 +269,8 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
             rng.init(J.seed, rid - J.ray_base);
             unit_sphere(rng, dx, dy, dz);
             px = J.src[0]; py = J.src[1]; pz = J.src[2];
-#pragma unroll
-            for (int b = 0; b < NB; b++) s_e[b][me] = J.e0[b];
-            s_dist[me] = 0.0f;
-            s_rng[me] = rng.s;
-            s_bounce[me] = 0u;
-            s_rid[me] = rid;
+            cold_save(J.e0, 0.0f, rng.s, 0u);
+            cold_set_rid(rid);
           }
           begin_segment(jobs[ji]);
         }
@@ -322,13 +349,10 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
       }
       if (J.n_groups) have = panels_hit(J, panels, groups, job_mats, px, py, pz, dx, dy, dz, have, h);
       const float t_hit = have ? h.t : FLT_MAX;
-      float e[NB];
-#pragma unroll
-      for (int b = 0; b < NB; b++) e[b] = s_e[b][me];
-      float dist = s_dist[me];
+      float e[NB], dist;
       Pcg rng;
-      rng.s = s_rng[me];
-      uint32_t bounce = s_bounce[me];
+      uint32_t bounce;
+      cold_load(e, dist, rng.s, bounce);
       bool done = shade_segment<NB>(J, acc, h, have, t_hit, px, py, pz, dx, dy, dz, dist, e, rng);
       bounce++;
       if (!done && bounce >= J.max_bounces) done = true;
@@ -341,19 +365,15 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const DJob* __restrict__ 
         Bands<NB> eb;
 #pragma unroll
         for (int b = 0; b < NB; b++) eb.v[b] = e[b];
-        park_ray<NB>(rs, s_rid[me], px, py, pz, dist, dx, dy, dz, rng.s, eb, bounce);
+        park_ray<NB>(rs, cold_rid(), px, py, pz, dist, dx, dy, dz, rng.s, eb, bounce);
         phase = IDLE;
         parked = true;
       } else {
-#pragma unroll
-        for (int b = 0; b < NB; b++) s_e[b][me] = e[b];
-        s_dist[me] = dist;
-        s_rng[me] = rng.s;
-        s_bounce[me] = bounce;
+        cold_save(e, dist, rng.s, bounce);
         begin_segment(J);
       }
     }
-    if (ea.cur) epoch_tally(ea, ended, parked, s_rid[me], may_park, n_rays, keep, fetch);
+    if (ea.cur) epoch_tally(ea, ended, parked, cold_rid(), may_park, n_rays, keep, fetch);
   }
 }
 
