@@ -233,8 +233,8 @@ def test_multiroom_pairs_vs_fp64(ctx_tie, oracle, pair):
     scene.release()
 
 
-def test_panel_over_the_hole_seals_it(ctx):
-    """mesh_parity.rs:87-119: a leaf over the doorway cuts the outside energy to < 15 %."""
+def _holed_room(ctx):
+    """mesh_parity.rs:16-29: the shell with a doorway in the x = 8 wall, on the GPU."""
     mb = MeshBuilder()
     m = mb.material(M.CONCRETE)
     v = lambda x, y, z: (x, y, z)
@@ -246,7 +246,47 @@ def test_panel_over_the_hole_seals_it(ctx):
     mb.quad(v(8, 0, 0), v(8, 2.5, 0), v(8, 2.5, 3), v(8, 0, 3), m)
     mb.quad(v(8, 3.5, 0), v(8, 6, 0), v(8, 6, 3), v(8, 3.5, 3), m)
     mb.quad(v(8, 2.5, 2.1), v(8, 3.5, 2.1), v(8, 3.5, 3), v(8, 2.5, 3), m)
-    scene = ctx.upload_builder(mb)
+    return ctx.upload_builder(mb)
+
+
+def test_mesh_tracer_matches_the_cpu_tracer(ctx, oracle):
+    """mesh_parity.rs:36-86, with its tolerances: the GPU mesh tracer (its own
+    per-ray streams) against the reference's CPU tracer (the f32 oracle with the
+    reference's xorshift stream, seeds 400-403) on the holed room, 4 traces of
+    16384 rays averaged on each side, for a listener inside and one outside:
+    RT60 ratio in [0.8, 1.25) inside (outside, the sparse tail's decay fit is no
+    statistic), level within 2 dB, late directions with dot > 0.9 and
+    anisotropy within 0.15 (from 50 ms on)."""
+    from test_oracle_golden import holed_room
+    from omg_audio_gb300.tracer import Echogram
+    O = oracle
+    mesh = holed_room(O).build("f32")
+    scene = _holed_room(ctx)
+    src = (2.0, 3.0, 1.5)
+    db = lambda v: 20.0 * np.log10(np.maximum(v, 1e-9))
+    for name, lis in (("inside", (6.0, 2.0, 1.6)), ("outside", (11.0, 3.0, 1.6))):
+        cpu, gpu = Echogram(300, 3, 0.010), Echogram(300, 3, 0.010)
+        for k in range(4):
+            b, d, _ = O.trace_mesh(mesh, src, lis, 16384, rng="xorshift", seed=400 + k)
+            cpu.ema(Echogram.wrap(b.astype(np.float32), d.astype(np.float32), 0.010), 1.0 / (k + 1))
+            e, _ = ctx.trace_world(scene, src, lis, 16384, seed=0xC6D2 ^ ((k * 0x85EBCA6B) & 0xFFFFFFFF))
+            gpu.ema(e, 1.0 / (k + 1))
+        rc, lc, _ = O.estimate_reverb(cpu.bins, 0.010)
+        rg, lg, _ = O.estimate_reverb(gpu.bins, 0.010)
+        print(f"{name}: rt60 cpu {rc} gpu {rg}, level cpu {lc} gpu {lg}")
+        if name == "inside":
+            assert np.all((rg / rc >= 0.8) & (rg / rc < 1.25)), (name, rg / rc)
+        assert np.all(np.abs(db(lg) - db(lc)) < 2.0), (name, db(lg) - db(lc))
+        dc, ac = cpu.late_direction(0.05)
+        dg, ag = gpu.late_direction(0.05)
+        assert float(dc @ dg) > 0.9, (name, dc, dg)
+        assert abs(ac - ag) < 0.15, (name, ac, ag)
+    scene.release()
+
+
+def test_panel_over_the_hole_seals_it(ctx):
+    """mesh_parity.rs:87-119: a leaf over the doorway cuts the outside energy to < 15 %."""
+    scene = _holed_room(ctx)
     src, lis = (2, 3, 1.5), (11, 3, 1.6)
     open_, _ = ctx.trace_world(scene, src, lis, 16384, seed=7)
     leaf = ((7.96, 2.5, 0.0), (8.04, 3.5, 2.1), M.WOOD_PANEL)
